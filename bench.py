@@ -1,0 +1,332 @@
+"""Benchmark of the PIC/DSMC time step: particle-steps/s on one GB300.
+
+Workload (BASELINE configuration 1, plain FP64): 200 mm cube at h = 2 mm
+(6.0e6 tets, 1.03e6 nodes), 1e7 Ti+ from a 20 mm disk (Thompson energies,
+cosine-law directions), Ar 0.5 Pa VHS, dt = 5e-9 s, Poisson every 10 steps,
+re-sort every 20. Synthetic, seeded inputs (no dataset is involved).
+
+value: alive-particle steps processed in the K timed steps / device time of
+those steps (CUDA events on the library's stream), inputs resident in HBM.
+e2e:   the same metric through the C ABI with host buffers: upload of the
+particle state from pinned memory, K steps with the per-step stats read
+(the reference's stop check), download of the particles and surface counters.
+roofline: the fused step kernel (push + walk + collide + settle), algorithmic
+bytes = 112 B per alive particle + 152 B per occupied tet, over its
+CUDA-event time; peak from MEASURED_PEAKS.json.
+cpu_baseline / --impl reference: the FP64 CPU oracle (OpenMP restatement of
+the reference step; the reference itself does not build here) on a bounded
+sample of the same workload, all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s"
+UNIT = "particle-steps/s"
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def dist_info():
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower() in ("active", "0x1", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def build_workload(args):
+    from start_gb300.workloads import workload1
+
+    cells = args.cells
+    w = workload1(n_particles=args.particles, cells=cells, seed=0, steps=args.warmup + args.steps)
+    w.params["precision"] = 1 if args.precision == "mixed" else 0
+    return w
+
+
+def cpu_sample(w, n_sample, steps, threads=None):
+    """Times the CPU oracle on the first n_sample particles of the workload:
+    one untimed deposit + cold solve, then `steps` steps of the full loop
+    (warm-started solve at the first, as in steady state)."""
+    import oracle
+
+    if threads:
+        oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    o = oracle.Oracle(w.mesh, w.params)
+    t_setup = time.perf_counter() - t0
+    o.set_particles(w.pos[:n_sample], w.vel[:n_sample])
+    o.gather(want_rho=False)
+    o.solve(want_phi=False, raise_on_nonconvergence=False)
+    s0 = o.stats()["particle_steps"]
+    t0 = time.perf_counter()
+    o.run(steps, raise_on_nonconvergence=False)
+    dt = time.perf_counter() - t0
+    s1 = o.stats()["particle_steps"]
+    o.close()
+    return (s1 - s0) / dt, dict(setup_s=t_setup, timed_s=dt, particle_steps=s1 - s0, threads=oracle.get_threads())
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    w = build_workload(args)
+    n_sample = min(args.cpu_sample, len(w.pos))
+    vals = []
+    info = {}
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_sample(w, n_sample, 1)
+    for _ in range(max(1, min(args.steps, 3))):
+        v, info = cpu_sample(w, n_sample, args.cpu_steps)
+        vals.append(v)
+    v = float(np.median(vals))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded workload generator)",
+        "config": config_dict(args, w),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": info.get("threads"), "kind": "port",
+                         "sample": f"{n_sample} of {len(w.pos)} particles, {args.cpu_steps} full-loop steps "
+                                   f"(deposit + warm PCG + push/walk/collide/settle) on the full mesh"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference itself needs CGAL/Trilinos/Gmsh (absent); the timed CPU path is the FP64 "
+                "OpenMP oracle port of its step",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_dict(args, w):
+    return {"workload": w.name, "n_particles": int(len(w.pos)), "n_tets": int(w.mesh.n_tets),
+            "n_nodes": int(w.mesh.n_nodes), "n_triangles": int(w.mesh.n_triangles),
+            "collision_model": "VHS", "poisson_every": w.params["poisson_every"],
+            "resort_every": w.params["resort_every"], "dt": w.params["dt"], "precision": args.precision,
+            "l2_policy": "inputs larger than L2 (particles 560 MB, mesh ~1.4 GB)",
+            "timed_steps_start_at": args.warmup}
+
+
+def run_gpu(args):
+    import torch
+
+    from start_gb300 import StartPIC
+
+    rank, world, local = dist_info()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    w = build_workload(args)
+    w.params["device"] = local
+    eng = StartPIC(w.mesh, w.params)
+    eng.set_particles(w.pos, w.vel)
+    stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=local)
+    eng.run(args.warmup)
+    eng.synchronize()
+    eng.profile_enable(True)
+    st0 = eng.stats()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    eng.run(args.steps, raise_on_nonconvergence=False)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    st1 = eng.stats()
+    prof = eng.profile()
+    eng.profile_enable(False)
+    ps = st1["particle_steps"] - st0["particle_steps"]
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        c = torch.tensor([float(ps)], device="cuda")
+        torch.distributed.all_reduce(c)
+        ps = int(c.item())
+    value = ps / (ms / 1e3)
+    peak, peak_src = measured_peak()
+    step_bw = prof["step_bytes"] / (prof["step_ms"] / 1e3) / 1e9 if prof["step_ms"] > 0 else None
+    roof = {"kernel": "k_step64 (push + walk + collide + settle)", "bound": "hbm",
+            "achieved": step_bw, "peak": peak, "unit": "GB/s",
+            "frac": (step_bw / peak) if step_bw else None,
+            "traffic": args.traffic, "peak_source": peak_src,
+            "bytes_per_launch": prof["step_bytes"] / max(1, prof["step_launches"]),
+            "ms_per_launch": prof["step_ms"] / max(1, prof["step_launches"])}
+    breakdown = {k: prof[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")}
+    breakdown["pcg_iters"] = prof["pcg_iters"]
+    breakdown["pcg_GBps"] = prof["pcg_bytes"] / (prof["pcg_ms"] / 1e3) / 1e9 if prof["pcg_ms"] > 0 else None
+    breakdown["deposit_GBps"] = (prof["deposit_bytes"] / (prof["deposit_ms"] / 1e3) / 1e9
+                                 if prof["deposit_ms"] > 0 else None)
+    breakdown["occupied_tets"] = prof["occupied_tets"]
+
+    # e2e through the C ABI with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        n = len(w.pos)
+        pos_h = torch.from_numpy(w.pos).pin_memory().numpy()
+        vel_h = torch.from_numpy(w.vel).pin_memory().numpy()
+        out_pos = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+        out_vel = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.set_particles(pos_h, vel_h)
+        s_start = eng.stats()["particle_steps"]
+        for _ in range(args.steps):
+            eng.run(1, raise_on_nonconvergence=False)  # returns the step's stats (D2H)
+        counts = eng.triangle_counts()
+        p = eng.particles()
+        out_pos[:] = p["pos"]
+        out_vel[:] = p["vel"]
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
+        ps_e2e = eng.stats()["particle_steps"] - s_start
+        h2d = (pos_h.nbytes + vel_h.nbytes) / args.steps
+        d2h = (out_pos.nbytes + out_vel.nbytes + n * 8 + counts.nbytes) / args.steps + 96
+        e2e = {"value": ps_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "seconds": t_e2e, "note": "job-level: upload, K steps from step 0 (cold first Poisson solve), "
+                                         "per-step stats read, download; host wall clock"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, info = cpu_sample(w, min(args.cpu_sample, len(w.pos)), args.cpu_steps)
+        cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
+               "sample": f"{min(args.cpu_sample, len(w.pos))} of {len(w.pos)} particles, {args.cpu_steps} "
+                         f"full-loop steps on the full mesh (one warm PCG solve)", "timed_s": info["timed_s"]}
+    eng.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded workload generator)", "config": config_dict(args, w),
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown,
+            "alive_particles": {"start": st0["n_alive"], "end": st1["n_alive"]},
+            "cg_iters_last": st1["cg_iters_last"],
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--particles", type=int, default=10_000_000)
+    ap.add_argument("--cells", type=int, default=100)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per launch of the step kernel, if captured")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,207 @@
+/*
+ * start_gpu.h -- C ABI of the GB300 particle-in-cell / DSMC time step.
+ *
+ * The library (libstart_gpu.so) replaces the per-step calls that Start's
+ * ModelingMainDriver makes into its ParticleInCellEngine
+ * (src/ModelingMainDriver.cpp:146-184):
+ *
+ *   NodeChargeDensityProcessor::gather   -> spg_gather
+ *     (include/ParticleInCellEngine/NodeChargeDensityProcessor.hpp:39-46)
+ *   ChargeDensityEquationSolver::solve   -> spg_solve
+ *     (include/ParticleInCellEngine/ChargeDensityEquationSolver.hpp:38-42,
+ *      which calls MatrixEquationSolver::solve / calculateElectricField,
+ *      src/FiniteElementMethod/Solvers/MatrixEquationSolver.cpp:359-427)
+ *   ParticleDynamicsProcessor::process   -> spg_process
+ *     (include/ParticleInCellEngine/ParticleDynamicsProcessor/ParticleDynamicsProcessor.hpp:154-170)
+ *   the whole time loop                  -> spg_run
+ *     (src/ModelingMainDriver.cpp:132-220)
+ *   SurfaceMesh triangle counters        -> spg_get_triangle_counts
+ *     (include/Geometry/Mesh/Surface/TriangleCell.hpp:17-23, read by
+ *      src/DataHandling/TriangleMeshHdf5Manager.cpp:97-140)
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 (SPG_OK) or a negative
+ *     spg_status code. No C++ exception crosses this boundary.
+ *   - spg_last_error(h) returns a message for the last failure on h;
+ *     spg_last_error(NULL) returns the last failure of spg_create on the
+ *     calling thread.
+ *   - The handle owns all device memory and one CUDA stream. Caller buffers
+ *     are host memory; they are copied in and out inside the call.
+ *   - One handle per host thread at a time.
+ *   - Units are SI (metres, seconds, volts, coulombs, kilograms). The
+ *     reference keeps mesh coordinates in millimetres; convert on load.
+ *   - Particle identity: particle k of spg_set_particles keeps id k for the
+ *     whole run; every getter returns particles in id order.
+ */
+#ifndef START_GPU_H
+#define START_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPG_ABI_VERSION 1
+
+typedef enum spg_status {
+    SPG_OK = 0,
+    SPG_E_INVALID = -1,        /* bad argument (null pointer, size mismatch, bad enum) */
+    SPG_E_CUDA = -2,           /* a CUDA runtime call failed */
+    SPG_E_BAD_MESH = -3,       /* degenerate tet, bad node index, non-manifold face */
+    SPG_E_NOT_CONVERGED = -4,  /* PCG hit cg_max_iter; the iterate is kept */
+    SPG_E_LOST_PARTICLES = -5, /* some particle left the mesh or hit max_crossings */
+    SPG_E_NO_DEVICE = -6,      /* no CUDA device / wrong architecture */
+    SPG_E_OOM = -7,            /* device allocation failed */
+    SPG_E_STATE = -8           /* call order (e.g. process before set_particles) */
+} spg_status;
+
+typedef enum spg_collision_model {
+    SPG_COLL_NONE = 0,
+    SPG_COLL_HS = 1,  /* src/Particle/PhysicsCore/CollisionModel/HSModel.cpp:6-42 */
+    SPG_COLL_VHS = 2, /* .../VHSModel.cpp:6-52 */
+    SPG_COLL_VSS = 3  /* .../VSSModel.cpp:6-54 */
+} spg_collision_model;
+
+typedef enum spg_precision {
+    SPG_FP64 = 0,  /* plain form: FP64 state, push, walk and PCG */
+    SPG_MIXED = 1  /* FP32 tet-local state and push; FP32-SpMV PCG in FP64 refinement */
+} spg_precision;
+
+/* Particle flag bits returned by spg_get_particles. */
+#define SPG_FLAG_SETTLED 1u /* crossed a surface triangle; position = hit point */
+#define SPG_FLAG_LOST 2u    /* left the mesh through a face with no triangle, or walk cap */
+
+/* Tet mesh. Node index = gmsh node tag - 1 (GSMAssembler.cpp:10-72). */
+typedef struct spg_mesh_desc {
+    int64_t n_nodes;
+    const double *node_xyz;        /* [3*n_nodes] */
+    int64_t n_tets;
+    const int32_t *tet_nodes;      /* [4*n_tets]; either orientation */
+    int64_t n_triangles;
+    const int32_t *tri_nodes;      /* [3*n_triangles]; surface triangles, id = row */
+    int64_t n_dirichlet;
+    const int32_t *dirichlet_nodes; /* [n_dirichlet] */
+    const double *dirichlet_values; /* [n_dirichlet] volts */
+} spg_mesh_desc;
+
+typedef struct spg_params {
+    double dt;                /* time step [s] */
+    double charge;            /* charge of one physical particle [C] */
+    double mass;              /* projectile mass [kg] */
+    double weight;            /* physical particles per macro-particle */
+    int32_t collision_model;  /* spg_collision_model */
+    int32_t precision;        /* spg_precision */
+    double gas_mass;          /* background gas molecule mass [kg] */
+    double gas_concentration; /* n [m^-3]; P*N_A/(R*T) in the reference (Utilities.cpp:132-149) */
+    double hs_diameter;       /* HS collision diameter d: sigma = pi*d^2 */
+    double vhs_dref;          /* VHS/VSS reference diameter */
+    double omega;             /* viscosity-temperature index */
+    double alpha;             /* VSS deflection parameter */
+    double kT_ref;            /* k*T_ref [J]; 297*1.380658e-23 in Constants.hpp:12 */
+    double epsilon0;          /* vacuum permittivity [F/m] */
+    double min_velocity;      /* particles slower than this are not moved (Constants.hpp:50) */
+    double bbox_expansion;    /* surface bbox expansion factor (Constants.hpp, 1.01) */
+    uint64_t seed;            /* Philox key for collisions */
+    int32_t poisson_every;    /* spg_run: deposit + solve every N steps */
+    int32_t resort_every;     /* spg_run: re-sort particles by tet every N steps (0 = never) */
+    int32_t max_crossings;    /* tet-walk cap per particle per step */
+    int32_t cg_max_iter;      /* PCG iteration cap */
+    double cg_rtol;           /* PCG stop: ||r||_2 <= cg_rtol * ||b||_2 */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t reserved0;
+} spg_params;
+
+typedef struct spg_stats {
+    int64_t step;             /* steps taken so far */
+    int64_t n_particles;
+    int64_t n_alive;          /* neither settled nor lost */
+    int64_t n_settled;
+    int64_t n_lost;
+    int64_t particle_steps;   /* cumulative alive-particle steps processed */
+    int64_t collisions;       /* cumulative gas collisions */
+    int64_t crossings;        /* cumulative tet-face crossings */
+    int64_t cg_iters_total;
+    int32_t cg_iters_last;
+    int32_t cg_solves;
+    double cg_relres_last;
+} spg_stats;
+
+/* Cumulative device timings (CUDA events on the handle's stream), enabled by
+ * spg_profile_enable. Times in milliseconds, bytes are algorithmic bytes. */
+typedef struct spg_profile {
+    double step_ms;      int64_t step_launches;    double step_bytes;
+    double deposit_ms;   int64_t deposit_launches; double deposit_bytes;
+    double pcg_ms;       int64_t pcg_solves;       double pcg_bytes; int64_t pcg_iters;
+    double efield_ms;    int64_t efield_launches;
+    double sort_ms;      int64_t sort_launches;    double sort_bytes;
+    int64_t kernel_launches; /* every kernel this library launched while profiling */
+    int64_t occupied_tets;   /* tets holding alive particles at the last re-sort */
+} spg_profile;
+
+typedef struct spg_handle spg_handle;
+
+const char *spg_version(void);
+void spg_default_params(spg_params *p);
+const char *spg_last_error(const spg_handle *h);
+
+/* Builds the device mesh, P1 stiffness (closed form, GSMAssembler.cpp:10-118),
+ * symmetric Dirichlet elimination and surface-triangle face map. */
+int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle **out);
+int spg_destroy(spg_handle *h);
+
+/* Mesh counters: [n_nodes, n_tets, n_triangles, n_boundary_faces, nnz, n_dirichlet]. */
+int spg_mesh_info(const spg_handle *h, int64_t info[6]);
+
+/* Uploads particles (SoA-free interleaved xyz). tet may be NULL: the library
+ * then locates each particle with a tet walk from a voxel seed; particles
+ * outside the mesh are flagged LOST. Resets step, counters and potential. */
+int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double *vel,
+                      const int32_t *tet_or_null);
+/* Any output pointer may be NULL. Arrays are [3*n] / [n], in id order. */
+int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_t *tet,
+                      uint32_t *flags);
+
+/* (a) P1 charge deposit of all alive particles; rho_out [n_nodes] C/m^3 (nullable). */
+int spg_gather(spg_handle *h, double *rho_out);
+/* (b) Poisson solve K phi = rho*Vdual/eps0 with Dirichlet lifting, warm started
+ * from the previous phi; then E per tet. rho_or_null: use this nodal rho
+ * instead of the last deposit. Returns SPG_E_NOT_CONVERGED at the cap. */
+int spg_solve(spg_handle *h, const double *rho_or_null, double *phi_out, int32_t *iters,
+              double *relres);
+/* (c)(d)(e) nsteps particle steps with the current E (no deposit, no solve). */
+int spg_process(spg_handle *h, int32_t nsteps, spg_stats *stats);
+/* The whole loop: per step, gather+solve when step % poisson_every == 0,
+ * re-sort when step % resort_every == 0, then process. */
+int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats);
+/* Re-sorts particles by tet now (settled/lost particles move to the end). */
+int spg_resort(spg_handle *h);
+
+int spg_get_stats(spg_handle *h, spg_stats *stats);
+int spg_get_triangle_counts(spg_handle *h, uint64_t *counts /* [n_triangles] */);
+int spg_get_potential(spg_handle *h, double *phi /* [n_nodes] */);
+/* Sets phi (Dirichlet values are kept as given) and recomputes E. */
+int spg_set_potential(spg_handle *h, const double *phi);
+int spg_get_efield(spg_handle *h, double *E /* [3*n_tets] */);
+/* Point location through the same walk as spg_set_particles. */
+int spg_locate(spg_handle *h, int64_t n, const double *pos, int32_t *tet_out);
+
+/* Checkpoint: particles, step, phi, counters. The Philox streams are keyed by
+ * (seed, particle id, step), so a restored run continues bit-identically. */
+int spg_checkpoint_size(spg_handle *h, size_t *bytes);
+int spg_checkpoint(spg_handle *h, void *buf, size_t bytes);
+int spg_restore(spg_handle *h, const void *buf, size_t bytes);
+
+int spg_synchronize(spg_handle *h);
+/* cudaStream_t of the handle, for callers that record their own events. */
+void *spg_stream(spg_handle *h);
+int spg_profile_enable(spg_handle *h, int32_t on);
+int spg_get_profile(spg_handle *h, spg_profile *prof);
+int spg_profile_reset(spg_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* START_GPU_H */

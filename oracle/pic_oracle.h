@@ -1,0 +1,73 @@
+/*
+ * pic_oracle.h -- CPU oracle of the PIC/DSMC time step. TEST INFRASTRUCTURE:
+ * only the tests, the smoke check and the benchmark's CPU-baseline leg use it,
+ * as the checker of libstart_gpu.so; the product never links it.
+ *
+ * An FP64 C++17 + OpenMP restatement of the reference's step
+ * (src/ParticleInCellEngine/ParticleDynamicsProcessor/ParticleDynamicsProcessor.cpp:161-200)
+ * with the intended physics (push applied with the containing tet's E,
+ * E = -grad(phi), P1 deposit, Poisson with eps0, symmetric Dirichlet
+ * elimination). It takes the same mesh and parameter structs as the GPU ABI.
+ * Parity is pinned by the reference's own known-answer tests for the
+ * primitives (tests/Particle/ParticleTests.cpp, tests/Geometry/
+ * SegmentTriangleIntersectionTests.cpp, boundary-condition tests); the
+ * reference has no golden vectors for the PIC loop itself.
+ */
+#ifndef PIC_ORACLE_H
+#define PIC_ORACLE_H
+
+#include "../include/start_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct spo_handle spo_handle;
+
+const char *spo_last_error(void);
+int spo_set_threads(int n);
+int spo_get_threads(void);
+
+int spo_create(const spg_mesh_desc *mesh, const spg_params *params, spo_handle **out);
+void spo_destroy(spo_handle *h);
+int spo_mesh_info(const spo_handle *h, int64_t info[6]);
+int spo_set_particles(spo_handle *h, int64_t n, const double *pos, const double *vel, const int32_t *tet_or_null);
+int spo_get_particles(spo_handle *h, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags);
+int spo_gather(spo_handle *h, double *rho_out);
+int spo_solve(spo_handle *h, const double *rho_or_null, double *phi_out, int32_t *iters, double *relres);
+int spo_process(spo_handle *h, int32_t nsteps);
+/* Processes only particles [first, first+count) for one step without
+ * advancing the step counter (bounded CPU-baseline samples). */
+int spo_process_range(spo_handle *h, int64_t first, int64_t count);
+int spo_run(spo_handle *h, int32_t nsteps);
+int spo_get_stats(spo_handle *h, spg_stats *st);
+int spo_get_triangle_counts(spo_handle *h, uint64_t *counts);
+int spo_get_potential(spo_handle *h, double *phi);
+int spo_set_potential(spo_handle *h, const double *phi);
+int spo_get_efield(spo_handle *h, double *E);
+int spo_locate(spo_handle *h, int64_t n, const double *pos, int32_t *tet_out);
+/* Stiffness in CSR after Dirichlet elimination, and the lifting vector. */
+int spo_get_matrix(spo_handle *h, int32_t *row_ptr, int32_t *col, double *val, double *lift);
+int spo_get_dual_volumes(spo_handle *h, double *dv);
+
+/* Primitives pinned by the reference's unit tests. */
+void spo_update_position(double *pos3, const double *vel3, double dt);
+/* Segment-triangle intersection: 1 and the point when they meet (a segment
+ * lying in the triangle returns its source), else 0. */
+int spo_segment_triangle(const double *s0, const double *s1, const double *a, const double *b, const double *c,
+                         double *point);
+double spo_gas_concentration(double pressure, double temperature);
+/* Collision law with given uniforms u0 (decision), u1, u2: returns 1 and the
+ * new velocity when u0 < P. model: spg_collision_model. */
+int spo_collide_with(const spg_params *p, double *vel3, double u0, double u1, double u2);
+double spo_collision_probability(const spg_params *p, const double *vel3);
+/* Barycentric map; returns det(J). */
+double spo_tet_map(const double *x0, const double *x1, const double *x2, const double *x3, double *M9);
+/* Philox4x32-10 block. */
+void spo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,996 @@
+// C ABI of libstart_gpu.so (declared in include/start_gpu.h).
+//
+// One handle = one mesh, one particle population and one CUDA stream. The
+// time loop mirrors ModelingMainDriver::startModeling
+// (src/ModelingMainDriver.cpp:132-220): per step, gather (deposit) and solve
+// when due, then process; plus the periodic re-sort that has no reference
+// counterpart (it only changes memory order).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "spg_internal.h"
+
+using namespace spg;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr int kEventPool = 8192;
+
+struct EventSeries {
+    std::vector<cudaEvent_t> start, stop;
+    int used = 0;
+    double ms = 0.0;
+    int64_t launches = 0;
+};
+
+}  // namespace
+
+struct spg_handle {
+    spg_params prm{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // mesh
+    int64_t n_nodes = 0, n_tets = 0, n_tris = 0, n_boundary_faces = 0, nnz = 0, n_dirichlet = 0;
+    double bbox_lo[3], bbox_hi[3];
+    double vox_oi[6];
+    int32_t vox_dims[3];
+    TetRec *rec = nullptr;
+    int4 *nbr = nullptr, *ftri = nullptr, *tet_nodes = nullptr;
+    double *node_xyz = nullptr;
+    int32_t *row_ptr = nullptr, *col = nullptr;
+    double *val = nullptr, *inv_diag = nullptr, *dir_value = nullptr, *lift = nullptr, *dual_vol = nullptr;
+    uint8_t *is_dir = nullptr;
+    int32_t *vox_seed = nullptr;
+    std::vector<double> phi_init;  // Dirichlet values, 0 elsewhere
+
+    // fields
+    double *node_q = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr, *r = nullptr, *z = nullptr,
+           *p = nullptr, *q = nullptr, *partials = nullptr;
+    PcgScalars *sc = nullptr;
+    int pcg_blocks = 1;
+
+    // particles
+    DevParticles P[2]{};
+    int cur = 0;
+    int64_t cap = 0, np = 0, n_active = 0, init_lost = 0;
+    unsigned int *tri_count = nullptr;
+    DevCounters *ctr = nullptr;
+    int64_t *n_alive_dev = nullptr;
+    int32_t *sort_scratch = nullptr;
+    int64_t occupied = 0;
+    bool have_particles = false;
+    bool charge_valid = false;
+
+    // loop state
+    int64_t step = 0;
+    int32_t cg_iters_last = 0, cg_solves = 0;
+    int64_t cg_iters_total = 0;
+    double cg_relres_last = 0.0;
+
+    // profiling
+    bool prof = false;
+    EventSeries ev_step, ev_dep, ev_pcg, ev_ef, ev_sort;
+    double step_bytes = 0, dep_bytes = 0, pcg_bytes = 0, sort_bytes = 0;
+    int64_t pcg_iters_prof = 0;
+    unsigned long long processed_at_reset = 0;
+    int64_t launches = 0;  // kernels launched (all phases), reset with the profile
+};
+
+namespace {
+
+int fail(spg_handle *h, int code, const std::string &msg) {
+    if (h)
+        h->err = msg;
+    else
+        g_create_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? SPG_E_OOM : SPG_E_CUDA,                 \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                         \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **ptr, size_t count) {
+    return cudaMalloc(reinterpret_cast<void **>(ptr), sizeof(T) * std::max<size_t>(count, 1));
+}
+
+template <class T>
+cudaError_t upload(T **ptr, const std::vector<T> &v, cudaStream_t s) {
+    cudaError_t e = dalloc(ptr, v.size());
+    if (e != cudaSuccess) return e;
+    if (v.empty()) return cudaSuccess;
+    e = cudaMemcpyAsync(*ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+
+void free_particles(spg_handle *h) {
+    for (auto &P : h->P) {
+        cudaFree(P.x);
+        cudaFree(P.y);
+        cudaFree(P.z);
+        cudaFree(P.vx);
+        cudaFree(P.vy);
+        cudaFree(P.vz);
+        cudaFree(P.tet);
+        cudaFree(P.idf);
+        P = DevParticles{};
+    }
+    h->cap = 0;
+}
+
+MeshDev mesh_dev(const spg_handle *h) {
+    MeshDev m;
+    m.rec = h->rec;
+    m.nbr = h->nbr;
+    m.ftri = h->ftri;
+    m.tet_nodes = h->tet_nodes;
+    m.node_xyz = h->node_xyz;
+    m.n_tets = h->n_tets;
+    m.n_nodes = h->n_nodes;
+    return m;
+}
+
+StepConst step_const(const spg_handle *h) {
+    const spg_params &p = h->prm;
+    StepConst c{};
+    c.dt = p.dt;
+    c.charge = p.charge;
+    c.mass = p.mass;
+    c.q_over_m = p.charge / p.mass;
+    c.vmin = p.min_velocity;
+    for (int k = 0; k < 3; ++k) {
+        c.lo[k] = h->bbox_lo[k];
+        c.hi[k] = h->bbox_hi[k];
+    }
+    c.model = p.collision_model;
+    c.max_cross = p.max_crossings;
+    c.gas_n = p.gas_concentration;
+    c.mass_cp = p.mass / (p.gas_mass + p.mass);
+    c.mass_ct = p.gas_mass / (p.gas_mass + p.mass);
+    c.sigma_hs = 3.14159265358979323846 * (p.hs_diameter * p.hs_diameter);
+    c.vhs_c1 = (p.vhs_dref * p.vhs_dref) / std::tgamma(5.0 / 2.0 - p.omega);
+    c.two_kT = 2.0 * p.kT_ref;
+    c.mr = p.mass * p.gas_mass / (p.mass + p.gas_mass);
+    c.expo = p.omega - 1.0 / 2.0;
+    c.inv_alpha = 1.0 / p.alpha;
+    c.seed_lo = uint32_t(p.seed);
+    c.seed_hi = uint32_t(p.seed >> 32);
+    c.step = h->step;
+    return c;
+}
+
+PcgDev pcg_dev(spg_handle *h) {
+    PcgDev d;
+    d.n = h->n_nodes;
+    d.row_ptr = h->row_ptr;
+    d.col = h->col;
+    d.val = h->val;
+    d.inv_diag = h->inv_diag;
+    d.x = h->phi;
+    d.r = h->r;
+    d.z = h->z;
+    d.p = h->p;
+    d.p2 = nullptr;
+    d.q = h->q;
+    d.partials = h->partials;
+    d.sc = h->sc;
+    d.blocks = h->pcg_blocks;
+    return d;
+}
+
+// ---- profiling helpers
+void ev_begin(spg_handle *h, EventSeries &s) {
+    if (!h->prof) return;
+    if (s.start.empty()) {
+        s.start.resize(kEventPool);
+        s.stop.resize(kEventPool);
+        for (int k = 0; k < kEventPool; ++k) {
+            cudaEventCreate(&s.start[k]);
+            cudaEventCreate(&s.stop[k]);
+        }
+    }
+    if (s.used == kEventPool) {  // resolve the pool before reuse
+        cudaEventSynchronize(s.stop[kEventPool - 1]);
+        for (int k = 0; k < kEventPool; ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, s.start[k], s.stop[k]);
+            s.ms += ms;
+        }
+        s.used = 0;
+    }
+    cudaEventRecord(s.start[s.used], h->stream);
+}
+void ev_end(spg_handle *h, EventSeries &s) {
+    if (!h->prof) return;
+    cudaEventRecord(s.stop[s.used], h->stream);
+    s.used++;
+    s.launches++;
+}
+void ev_resolve(EventSeries &s) {
+    if (s.used == 0) return;
+    cudaEventSynchronize(s.stop[s.used - 1]);
+    for (int k = 0; k < s.used; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s.start[k], s.stop[k]);
+        s.ms += ms;
+    }
+    s.used = 0;
+}
+void ev_destroy(EventSeries &s) {
+    for (auto e : s.start) cudaEventDestroy(e);
+    for (auto e : s.stop) cudaEventDestroy(e);
+    s.start.clear();
+    s.stop.clear();
+}
+
+// ---- phases
+int do_resort(spg_handle *h) {
+    if (!h->have_particles || h->np == 0) return SPG_OK;
+    ev_begin(h, h->ev_sort);
+    DevParticles &src = h->P[h->cur], &dst = h->P[1 - h->cur];
+    launch_resort(src, dst, h->n_active, h->n_tets, h->sort_scratch, h->n_alive_dev, h->stream);
+    ev_end(h, h->ev_sort);
+    h->launches += h->n_active > 0 ? 5 : 3;
+    CK(cudaGetLastError());
+    // Particles past n_active are all dead already; keep them behind the
+    // sorted range by copying the tail once (they never move again).
+    if (h->n_active < h->np) {
+        const int64_t tail = h->np - h->n_active, o = h->n_active;
+        CK(cudaMemcpyAsync(dst.x + o, src.x + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.y + o, src.y + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.z + o, src.z + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.vx + o, src.vx + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.vy + o, src.vy + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.vz + o, src.vz + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.tet + o, src.tet + o, 4 * tail, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(dst.idf + o, src.idf + o, 4 * tail, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    int64_t na = 0;
+    unsigned long long occ = 0;
+    CK(cudaMemcpyAsync(&na, h->n_alive_dev, sizeof(na), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(&occ, sort_occupied_counter(h->sort_scratch), sizeof(occ), cudaMemcpyDeviceToHost,
+                       h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->prof) h->sort_bytes += double(h->n_active) * 2.0 * 56.0 + 8.0 * double(h->n_tets + 1);
+    h->cur = 1 - h->cur;
+    h->n_active = na;
+    h->occupied = int64_t(occ);
+    return SPG_OK;
+}
+
+int do_gather(spg_handle *h) {
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "gather: no particles set");
+    CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * h->n_nodes, h->stream));
+    ev_begin(h, h->ev_dep);
+    launch_deposit64(h->P[h->cur], h->n_active, mesh_dev(h), h->prm.weight * h->prm.charge, h->node_q, h->stream);
+    ev_end(h, h->ev_dep);
+    if (h->n_active > 0) h->launches += 1;
+    CK(cudaGetLastError());
+    if (h->prof)
+        h->dep_bytes += 32.0 * double(h->n_active) + 112.0 * double(h->occupied ? h->occupied : h->n_tets) +
+                        16.0 * double(h->n_nodes);
+    h->charge_valid = true;
+    return SPG_OK;
+}
+
+int do_solve(spg_handle *h) {
+    const int64_t n = h->n_nodes;
+    launch_pcg_rhs(h->node_q, 1.0 / h->prm.epsilon0, h->lift, h->is_dir, h->dir_value, h->b, n, h->stream);
+    PcgScalars init{};
+    init.tol2 = (h->prm.cg_rtol * h->prm.cg_rtol);
+    init.max_iter = h->prm.cg_max_iter;
+    CK(cudaMemcpyAsync(h->sc, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    PcgDev d = pcg_dev(h);
+    ev_begin(h, h->ev_pcg);
+    launch_pcg_setup(d, h->b, h->stream);
+    h->launches += 2;
+    PcgScalars hs{};
+    int chunk = 4;
+    for (;;) {
+        for (int k = 0; k < chunk; ++k) launch_pcg_iteration(d, h->stream);
+        h->launches += 3 * chunk;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (hs.converged) break;
+        chunk = std::min(chunk * 2, 64);
+    }
+    ev_end(h, h->ev_pcg);
+    ev_begin(h, h->ev_ef);
+    launch_efield64(mesh_dev(h), h->rec, h->phi, h->stream);
+    ev_end(h, h->ev_ef);
+    h->launches += 1;
+    CK(cudaGetLastError());
+    h->cg_iters_last = hs.iters;
+    h->cg_iters_total += hs.iters;
+    h->cg_solves++;
+    h->cg_relres_last = hs.bb > 0.0 ? std::sqrt(hs.rr / hs.bb) : 0.0;
+    if (h->prof) {
+        h->pcg_iters_prof += hs.iters;
+        h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz) + 4.0 * double(n + 1) + 72.0 * double(n));
+    }
+    if (hs.converged == 2) {
+        std::ostringstream os;
+        os << "PCG did not converge: " << hs.iters << " iterations, relative residual " << h->cg_relres_last;
+        return fail(h, SPG_E_NOT_CONVERGED, os.str());
+    }
+    return SPG_OK;
+}
+
+int do_process(spg_handle *h) {
+    StepConst c = step_const(h);
+    ev_begin(h, h->ev_step);
+    launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->ctr, h->stream);
+    ev_end(h, h->ev_step);
+    if (h->n_active > 0) h->launches += 1;
+    CK(cudaGetLastError());
+    if (h->prof) h->step_bytes += 152.0 * double(h->occupied ? h->occupied : std::min(h->n_tets, h->n_active));
+    h->step++;
+    return SPG_OK;
+}
+
+int read_counters(spg_handle *h, DevCounters &c) {
+    CK(cudaMemcpyAsync(&c, h->ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+int fill_stats(spg_handle *h, spg_stats *st) {
+    if (!st) return SPG_OK;
+    DevCounters c{};
+    int rc = read_counters(h, c);
+    if (rc) return rc;
+    st->step = h->step;
+    st->n_particles = h->np;
+    st->n_settled = int64_t(c.settled);
+    st->n_lost = int64_t(c.lost) + h->init_lost;
+    st->n_alive = h->np - st->n_settled - st->n_lost;
+    st->particle_steps = int64_t(c.processed);
+    st->collisions = int64_t(c.collisions);
+    st->crossings = int64_t(c.crossings);
+    st->cg_iters_total = h->cg_iters_total;
+    st->cg_iters_last = h->cg_iters_last;
+    st->cg_solves = h->cg_solves;
+    st->cg_relres_last = h->cg_relres_last;
+    return SPG_OK;
+}
+
+int reset_run_state(spg_handle *h) {
+    h->step = 0;
+    h->cg_iters_last = 0;
+    h->cg_solves = 0;
+    h->cg_iters_total = 0;
+    h->cg_relres_last = 0.0;
+    h->charge_valid = false;
+    CK(cudaMemsetAsync(h->ctr, 0, sizeof(DevCounters), h->stream));
+    CK(cudaMemsetAsync(h->tri_count, 0, sizeof(unsigned int) * std::max<int64_t>(h->n_tris, 1), h->stream));
+    CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * h->n_nodes, h->stream));
+    launch_zero_efield(h->rec, h->n_tets, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+int validate_params(const spg_params *p, std::string &msg) {
+    if (!(p->dt > 0.0)) msg = "dt must be > 0";
+    else if (!(p->mass > 0.0)) msg = "mass must be > 0";
+    else if (!(p->weight > 0.0)) msg = "weight must be > 0";
+    else if (!(p->epsilon0 > 0.0)) msg = "epsilon0 must be > 0";
+    else if (p->collision_model < SPG_COLL_NONE || p->collision_model > SPG_COLL_VSS) msg = "bad collision_model";
+    else if (p->precision != SPG_FP64 && p->precision != SPG_MIXED) msg = "bad precision";
+    else if (p->collision_model != SPG_COLL_NONE && !(p->gas_mass > 0.0)) msg = "gas_mass must be > 0";
+    else if (p->collision_model != SPG_COLL_NONE && !(p->gas_concentration >= 0.0)) msg = "gas_concentration < 0";
+    else if (p->collision_model == SPG_COLL_VSS && !(p->alpha > 0.0)) msg = "alpha must be > 0";
+    else if (p->poisson_every < 1) msg = "poisson_every must be >= 1";
+    else if (p->resort_every < 0) msg = "resort_every must be >= 0";
+    else if (p->max_crossings < 1) msg = "max_crossings must be >= 1";
+    else if (p->cg_max_iter < 1) msg = "cg_max_iter must be >= 1";
+    else if (!(p->cg_rtol > 0.0)) msg = "cg_rtol must be > 0";
+    else return SPG_OK;
+    return SPG_E_INVALID;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *spg_version(void) { return "start_gb300 1.0 (sm_103a)"; }
+
+void spg_default_params(spg_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 1e-8;
+    p->charge = 1.602176565e-19;  // Constants.hpp e_charge
+    p->mass = 7.9485017e-26;      // Ti
+    p->weight = 1.0;
+    p->collision_model = SPG_COLL_NONE;
+    p->precision = SPG_FP64;
+    p->gas_mass = 6.6335209e-26;  // Ar
+    p->gas_concentration = 0.0;
+    p->hs_diameter = 3.6e-10;
+    p->vhs_dref = 4.17e-10;
+    p->omega = 0.81;
+    p->alpha = 1.40;
+    p->kT_ref = 297.0 * 1.380658e-23;  // Constants.hpp:12
+    p->epsilon0 = 8.8541878128e-12;
+    p->min_velocity = 10.0;  // Constants.hpp:50
+    p->bbox_expansion = 1.01;
+    p->seed = 0;
+    p->poisson_every = 10;
+    p->resort_every = 20;
+    p->max_crossings = 4096;
+    p->cg_max_iter = 20000;
+    p->cg_rtol = 1e-10;
+    p->device = 0;
+}
+
+const char *spg_last_error(const spg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle **out) {
+    spg_handle *h = nullptr;
+    if (!mesh || !params || !out) return fail(h, SPG_E_INVALID, "spg_create: null argument");
+    *out = nullptr;
+    std::string msg;
+    if (validate_params(params, msg)) return fail(h, SPG_E_INVALID, "spg_create: " + msg);
+    if (params->precision != SPG_FP64)
+        return fail(h, SPG_E_INVALID, "spg_create: only the FP64 form is available in this build");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(h, SPG_E_NO_DEVICE, "spg_create: no CUDA device");
+    if (params->device < 0 || params->device >= ndev) return fail(h, SPG_E_NO_DEVICE, "spg_create: bad device");
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, params->device);
+    if (prop.major * 10 + prop.minor != 103) {
+        std::ostringstream os;
+        os << "spg_create: built for sm_103a (GB300); device is sm_" << prop.major << prop.minor;
+        return fail(h, SPG_E_NO_DEVICE, os.str());
+    }
+    HostMesh hm;
+    std::string err;
+    int rc = prepare_mesh(*mesh, params->bbox_expansion, hm, err);
+    if (rc) return fail(h, rc, err);
+
+    std::unique_ptr<spg_handle> H(new (std::nothrow) spg_handle());
+    if (!H) return fail(h, SPG_E_OOM, "spg_create: host allocation failed");
+    h = H.get();
+    h->prm = *params;
+    h->device = params->device;
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->n_nodes = hm.n_nodes;
+    h->n_tets = hm.n_tets;
+    h->n_tris = hm.n_tris;
+    h->n_boundary_faces = hm.n_boundary_faces;
+    h->nnz = int64_t(hm.col.size());
+    h->n_dirichlet = hm.n_dirichlet;
+    for (int k = 0; k < 3; ++k) {
+        h->bbox_lo[k] = hm.bbox_lo[k];
+        h->bbox_hi[k] = hm.bbox_hi[k];
+        h->vox_oi[k] = hm.vox_origin[k];
+        h->vox_oi[3 + k] = hm.vox_inv[k];
+        h->vox_dims[k] = hm.vox_dims[k];
+    }
+    std::vector<double> inv_diag(hm.diag.size());
+    for (size_t i = 0; i < hm.diag.size(); ++i) inv_diag[i] = 1.0 / hm.diag[i];
+    cudaStream_t s = h->stream;
+    CK(upload(&h->rec, hm.rec, s));
+    CK(upload(reinterpret_cast<int32_t **>(&h->nbr), hm.nbr, s));
+    CK(upload(reinterpret_cast<int32_t **>(&h->ftri), hm.ftri, s));
+    CK(upload(reinterpret_cast<int32_t **>(&h->tet_nodes), hm.tet_nodes, s));
+    CK(upload(&h->node_xyz, hm.node_xyz, s));
+    CK(upload(&h->row_ptr, hm.row_ptr, s));
+    CK(upload(&h->col, hm.col, s));
+    CK(upload(&h->val, hm.val, s));
+    CK(upload(&h->inv_diag, inv_diag, s));
+    CK(upload(&h->is_dir, hm.is_dir, s));
+    CK(upload(&h->dir_value, hm.dir_value, s));
+    CK(upload(&h->lift, hm.lift, s));
+    CK(upload(&h->dual_vol, hm.dual_vol, s));
+    CK(upload(&h->vox_seed, hm.vox_seed, s));
+    h->phi_init = hm.dir_value;
+    const int64_t n = h->n_nodes;
+    CK(dalloc(&h->node_q, n));
+    CK(dalloc(&h->rho, n));
+    CK(dalloc(&h->phi, n));
+    CK(dalloc(&h->b, n));
+    CK(dalloc(&h->r, n));
+    CK(dalloc(&h->z, n));
+    CK(dalloc(&h->p, n));
+    CK(dalloc(&h->q, n));
+    h->pcg_blocks = pcg_blocks(n);
+    CK(dalloc(&h->partials, 3 * size_t(h->pcg_blocks)));
+    CK(dalloc(&h->sc, 1));
+    CK(cudaMemsetAsync(h->sc, 0, sizeof(PcgScalars), s));
+    CK(dalloc(&h->tri_count, std::max<int64_t>(h->n_tris, 1)));
+    CK(dalloc(&h->ctr, 1));
+    CK(dalloc(&h->n_alive_dev, 1));
+    CK(dalloc(&h->sort_scratch, size_t(sort_scratch_words(h->n_tets))));
+    rc = reset_run_state(h);
+    if (rc) return rc;
+    *out = H.release();
+    return SPG_OK;
+}
+
+int spg_destroy(spg_handle *h) {
+    if (!h) return SPG_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_particles(h);
+    void *ptrs[] = {h->rec,      h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
+                    h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
+                    h->node_q,   h->rho,      h->phi,      h->b,         h->r,        h->z,         h->p,
+                    h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch};
+    for (void *ptr : ptrs) cudaFree(ptr);
+    for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SPG_OK;
+}
+
+int spg_mesh_info(const spg_handle *h, int64_t info[6]) {
+    if (!h || !info) return SPG_E_INVALID;
+    info[0] = h->n_nodes;
+    info[1] = h->n_tets;
+    info[2] = h->n_tris;
+    info[3] = h->n_boundary_faces;
+    info[4] = h->nnz;
+    info[5] = h->n_dirichlet;
+    return SPG_OK;
+}
+
+int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double *vel, const int32_t *tet_or_null) {
+    if (!h) return SPG_E_INVALID;
+    if (n < 0 || n > kMaxParticles) return fail(h, SPG_E_INVALID, "set_particles: n out of range");
+    if (n > 0 && (!pos || !vel)) return fail(h, SPG_E_INVALID, "set_particles: null pos/vel");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    if (n > h->cap) {
+        free_particles(h);
+        for (auto &P : h->P) {
+            CK(dalloc(&P.x, n));
+            CK(dalloc(&P.y, n));
+            CK(dalloc(&P.z, n));
+            CK(dalloc(&P.vx, n));
+            CK(dalloc(&P.vy, n));
+            CK(dalloc(&P.vz, n));
+            CK(dalloc(&P.tet, n));
+            CK(dalloc(&P.idf, n));
+        }
+        h->cap = n;
+    }
+    h->cur = 0;
+    h->np = n;
+    h->n_active = n;
+    h->init_lost = 0;
+    h->occupied = 0;
+    if (n > 0) {
+        double *dpos = nullptr, *dvel = nullptr;
+        int32_t *dtet = nullptr;
+        unsigned long long *dlost = nullptr;
+        CK(dalloc(&dpos, 3 * n));
+        CK(dalloc(&dvel, 3 * n));
+        CK(dalloc(&dtet, n));
+        CK(dalloc(&dlost, 1));
+        CK(cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvel, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+        if (tet_or_null) {
+            std::vector<int32_t> t(tet_or_null, tet_or_null + n);
+            for (auto &v : t)
+                if (v >= h->n_tets) v = -1;
+            CK(cudaMemcpyAsync(dtet, t.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+            CK(cudaStreamSynchronize(s));
+        } else {
+            launch_locate(dpos, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings, dtet, s);
+        }
+        CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
+        launch_count_lost(dtet, n, dlost, s);
+        launch_init_particles(dpos, dvel, dtet, n, h->P[0], s);
+        CK(cudaGetLastError());
+        unsigned long long lost = 0;
+        CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        h->init_lost = int64_t(lost);
+        cudaFree(dpos);
+        cudaFree(dvel);
+        cudaFree(dtet);
+        cudaFree(dlost);
+    }
+    h->have_particles = true;
+    return reset_run_state(h);
+}
+
+int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags) {
+    if (!h) return SPG_E_INVALID;
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "get_particles: no particles set");
+    if (n != h->np) return fail(h, SPG_E_INVALID, "get_particles: n does not match the particle count");
+    if (n == 0) return SPG_OK;
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    double *dpos = nullptr, *dvel = nullptr;
+    int32_t *dtet = nullptr;
+    uint32_t *dfl = nullptr;
+    if (pos) CK(dalloc(&dpos, 3 * n));
+    if (vel) CK(dalloc(&dvel, 3 * n));
+    if (tet) CK(dalloc(&dtet, n));
+    if (flags) CK(dalloc(&dfl, n));
+    launch_gather_by_id(h->P[h->cur], n, dpos, dvel, dtet, dfl, s);
+    CK(cudaGetLastError());
+    if (pos) CK(cudaMemcpyAsync(pos, dpos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    if (vel) CK(cudaMemcpyAsync(vel, dvel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    if (tet) CK(cudaMemcpyAsync(tet, dtet, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    if (flags) CK(cudaMemcpyAsync(flags, dfl, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cudaFree(dpos);
+    cudaFree(dvel);
+    cudaFree(dtet);
+    cudaFree(dfl);
+    return SPG_OK;
+}
+
+int spg_gather(spg_handle *h, double *rho_out) {
+    if (!h) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    int rc = do_gather(h);
+    if (rc) return rc;
+    if (rho_out) {
+        launch_node_rho(h->node_q, h->dual_vol, h->rho, h->n_nodes, h->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(rho_out, h->rho, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+namespace {
+__attribute__((unused)) void node_q_from_rho_host(const std::vector<double> &rho, const std::vector<double> &dv,
+                                                  std::vector<double> &q) {
+    q.resize(rho.size());
+    for (size_t i = 0; i < rho.size(); ++i) q[i] = rho[i] * dv[i];
+}
+}  // namespace
+
+int spg_solve(spg_handle *h, const double *rho_or_null, double *phi_out, int32_t *iters, double *relres) {
+    if (!h) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    if (rho_or_null) {
+        std::vector<double> dv(h->n_nodes), q;
+        CK(cudaMemcpy(dv.data(), h->dual_vol, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost));
+        node_q_from_rho_host(std::vector<double>(rho_or_null, rho_or_null + h->n_nodes), dv, q);
+        CK(cudaMemcpyAsync(h->node_q, q.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        h->charge_valid = true;
+    }
+    int rc = do_solve(h);
+    if (iters) *iters = h->cg_iters_last;
+    if (relres) *relres = h->cg_relres_last;
+    if (rc && rc != SPG_E_NOT_CONVERGED) return rc;
+    if (phi_out) {
+        CK(cudaMemcpyAsync(phi_out, h->phi, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return rc;
+}
+
+int spg_process(spg_handle *h, int32_t nsteps, spg_stats *stats) {
+    if (!h) return SPG_E_INVALID;
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "process: no particles set");
+    if (nsteps < 0) return fail(h, SPG_E_INVALID, "process: nsteps < 0");
+    CK(cudaSetDevice(h->device));
+    for (int32_t k = 0; k < nsteps; ++k) {
+        int rc = do_process(h);
+        if (rc) return rc;
+    }
+    return fill_stats(h, stats);
+}
+
+int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
+    if (!h) return SPG_E_INVALID;
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "run: no particles set");
+    if (nsteps < 0) return fail(h, SPG_E_INVALID, "run: nsteps < 0");
+    CK(cudaSetDevice(h->device));
+    int status = SPG_OK;
+    for (int32_t k = 0; k < nsteps; ++k) {
+        int rc;
+        if (h->prm.resort_every > 0 && h->step % h->prm.resort_every == 0) {
+            rc = do_resort(h);
+            if (rc) return rc;
+        }
+        if (h->step % h->prm.poisson_every == 0) {
+            rc = do_gather(h);
+            if (rc) return rc;
+            rc = do_solve(h);
+            if (rc == SPG_E_NOT_CONVERGED)
+                status = rc;
+            else if (rc)
+                return rc;
+        }
+        rc = do_process(h);
+        if (rc) return rc;
+    }
+    int rc = fill_stats(h, stats);
+    return rc ? rc : status;
+}
+
+int spg_resort(spg_handle *h) {
+    if (!h) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    return do_resort(h);
+}
+
+int spg_get_stats(spg_handle *h, spg_stats *stats) {
+    if (!h || !stats) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    return fill_stats(h, stats);
+}
+
+int spg_get_triangle_counts(spg_handle *h, uint64_t *counts) {
+    if (!h || (!counts && h->n_tris > 0)) return SPG_E_INVALID;
+    if (h->n_tris == 0) return SPG_OK;
+    CK(cudaSetDevice(h->device));
+    std::vector<unsigned int> c(h->n_tris);
+    CK(cudaMemcpyAsync(c.data(), h->tri_count, sizeof(unsigned int) * h->n_tris, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int64_t k = 0; k < h->n_tris; ++k) counts[k] = c[k];
+    return SPG_OK;
+}
+
+int spg_get_potential(spg_handle *h, double *phi) {
+    if (!h || !phi) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync(phi, h->phi, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+int spg_set_potential(spg_handle *h, const double *phi) {
+    if (!h || !phi) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync(h->phi, phi, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+    launch_efield64(mesh_dev(h), h->rec, h->phi, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+int spg_get_efield(spg_handle *h, double *E) {
+    if (!h || !E) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    std::vector<TetRec> rec(h->n_tets);
+    CK(cudaMemcpyAsync(rec.data(), h->rec, sizeof(TetRec) * h->n_tets, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int64_t t = 0; t < h->n_tets; ++t)
+        for (int k = 0; k < 3; ++k) E[3 * t + k] = rec[t].E[k];
+    return SPG_OK;
+}
+
+int spg_locate(spg_handle *h, int64_t n, const double *pos, int32_t *tet_out) {
+    if (!h || n < 0 || (n > 0 && (!pos || !tet_out))) return SPG_E_INVALID;
+    if (n == 0) return SPG_OK;
+    CK(cudaSetDevice(h->device));
+    double *dpos = nullptr;
+    int32_t *dtet = nullptr;
+    CK(dalloc(&dpos, 3 * n));
+    CK(dalloc(&dtet, n));
+    CK(cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+    launch_locate(dpos, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings, dtet, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(tet_out, dtet, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    cudaFree(dpos);
+    cudaFree(dtet);
+    return SPG_OK;
+}
+
+// Checkpoint layout: header, 8 particle arrays (current order), phi, triangle
+// counters, device counters.
+namespace {
+struct CkptHeader {
+    uint64_t magic, version;
+    int64_t np, n_active, step, n_nodes, n_tris, init_lost, occupied;
+    int64_t cg_iters_total;
+    int32_t cg_iters_last, cg_solves;
+    double cg_relres_last;
+};
+constexpr uint64_t kMagic = 0x5350474B50543031ull;  // "SPGKPT01"
+size_t ckpt_bytes(const spg_handle *h) {
+    return sizeof(CkptHeader) + size_t(h->np) * (6 * 8 + 4 + 4) + size_t(h->n_nodes) * 8 + size_t(h->n_tris) * 4 +
+           sizeof(DevCounters);
+}
+}  // namespace
+
+int spg_checkpoint_size(spg_handle *h, size_t *bytes) {
+    if (!h || !bytes) return SPG_E_INVALID;
+    *bytes = ckpt_bytes(h);
+    return SPG_OK;
+}
+
+int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
+    if (!h || !buf) return SPG_E_INVALID;
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "checkpoint: no particles set");
+    if (bytes < ckpt_bytes(h)) return fail(h, SPG_E_INVALID, "checkpoint: buffer too small");
+    CK(cudaSetDevice(h->device));
+    CkptHeader hd{};
+    hd.magic = kMagic;
+    hd.version = 1;
+    hd.np = h->np;
+    hd.n_active = h->n_active;
+    hd.step = h->step;
+    hd.n_nodes = h->n_nodes;
+    hd.n_tris = h->n_tris;
+    hd.init_lost = h->init_lost;
+    hd.occupied = h->occupied;
+    hd.cg_iters_total = h->cg_iters_total;
+    hd.cg_iters_last = h->cg_iters_last;
+    hd.cg_solves = h->cg_solves;
+    hd.cg_relres_last = h->cg_relres_last;
+    char *o = static_cast<char *>(buf);
+    std::memcpy(o, &hd, sizeof(hd));
+    o += sizeof(hd);
+    const DevParticles &P = h->P[h->cur];
+    const int64_t n = h->np;
+    cudaStream_t s = h->stream;
+    double *darr[6] = {P.x, P.y, P.z, P.vx, P.vy, P.vz};
+    for (double *a : darr) {
+        CK(cudaMemcpyAsync(o, a, 8 * n, cudaMemcpyDeviceToHost, s));
+        o += 8 * n;
+    }
+    CK(cudaMemcpyAsync(o, P.tet, 4 * n, cudaMemcpyDeviceToHost, s));
+    o += 4 * n;
+    CK(cudaMemcpyAsync(o, P.idf, 4 * n, cudaMemcpyDeviceToHost, s));
+    o += 4 * n;
+    CK(cudaMemcpyAsync(o, h->phi, 8 * h->n_nodes, cudaMemcpyDeviceToHost, s));
+    o += 8 * h->n_nodes;
+    if (h->n_tris) CK(cudaMemcpyAsync(o, h->tri_count, 4 * h->n_tris, cudaMemcpyDeviceToHost, s));
+    o += 4 * h->n_tris;
+    CK(cudaMemcpyAsync(o, h->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
+    if (!h || !buf) return SPG_E_INVALID;
+    if (bytes < sizeof(CkptHeader)) return fail(h, SPG_E_INVALID, "restore: buffer too small");
+    CkptHeader hd;
+    std::memcpy(&hd, buf, sizeof(hd));
+    if (hd.magic != kMagic || hd.version != 1) return fail(h, SPG_E_INVALID, "restore: not a checkpoint");
+    if (hd.n_nodes != h->n_nodes || hd.n_tris != h->n_tris)
+        return fail(h, SPG_E_INVALID, "restore: checkpoint is for a different mesh");
+    if (hd.np < 0 || hd.np > kMaxParticles || hd.n_active < 0 || hd.n_active > hd.np)
+        return fail(h, SPG_E_INVALID, "restore: corrupt header");
+    CK(cudaSetDevice(h->device));
+    // allocate through set_particles with an empty upload of the right size
+    const int64_t n = hd.np;
+    if (bytes < sizeof(CkptHeader) + size_t(n) * 56 + size_t(h->n_nodes) * 8 + size_t(h->n_tris) * 4 +
+                    sizeof(DevCounters))
+        return fail(h, SPG_E_INVALID, "restore: buffer too small");
+    if (n > h->cap) {
+        free_particles(h);
+        for (auto &P : h->P) {
+            CK(dalloc(&P.x, n));
+            CK(dalloc(&P.y, n));
+            CK(dalloc(&P.z, n));
+            CK(dalloc(&P.vx, n));
+            CK(dalloc(&P.vy, n));
+            CK(dalloc(&P.vz, n));
+            CK(dalloc(&P.tet, n));
+            CK(dalloc(&P.idf, n));
+        }
+        h->cap = n;
+    }
+    h->cur = 0;
+    const char *o = static_cast<const char *>(buf) + sizeof(hd);
+    const DevParticles &P = h->P[0];
+    cudaStream_t s = h->stream;
+    double *darr[6] = {P.x, P.y, P.z, P.vx, P.vy, P.vz};
+    for (double *a : darr) {
+        CK(cudaMemcpyAsync(a, o, 8 * n, cudaMemcpyHostToDevice, s));
+        o += 8 * n;
+    }
+    CK(cudaMemcpyAsync(P.tet, o, 4 * n, cudaMemcpyHostToDevice, s));
+    o += 4 * n;
+    CK(cudaMemcpyAsync(P.idf, o, 4 * n, cudaMemcpyHostToDevice, s));
+    o += 4 * n;
+    CK(cudaMemcpyAsync(h->phi, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
+    o += 8 * h->n_nodes;
+    if (h->n_tris) CK(cudaMemcpyAsync(h->tri_count, o, 4 * h->n_tris, cudaMemcpyHostToDevice, s));
+    o += 4 * h->n_tris;
+    CK(cudaMemcpyAsync(h->ctr, o, sizeof(DevCounters), cudaMemcpyHostToDevice, s));
+    h->np = n;
+    h->n_active = hd.n_active;
+    h->step = hd.step;
+    h->init_lost = hd.init_lost;
+    h->occupied = hd.occupied;
+    h->cg_iters_total = hd.cg_iters_total;
+    h->cg_iters_last = hd.cg_iters_last;
+    h->cg_solves = hd.cg_solves;
+    h->cg_relres_last = hd.cg_relres_last;
+    h->have_particles = true;
+    launch_efield64(mesh_dev(h), h->rec, h->phi, s);
+    if (h->cg_solves == 0) launch_zero_efield(h->rec, h->n_tets, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+int spg_synchronize(spg_handle *h) {
+    if (!h) return SPG_E_INVALID;
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+void *spg_stream(spg_handle *h) { return h ? static_cast<void *>(h->stream) : nullptr; }
+
+int spg_profile_enable(spg_handle *h, int32_t on) {
+    if (!h) return SPG_E_INVALID;
+    if (on && !h->prof) {
+        h->prof = true;
+        return spg_profile_reset(h);
+    }
+    h->prof = on != 0;
+    return SPG_OK;
+}
+
+int spg_profile_reset(spg_handle *h) {
+    if (!h) return SPG_E_INVALID;
+    CK(cudaStreamSynchronize(h->stream));
+    for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) {
+        s->used = 0;
+        s->ms = 0.0;
+        s->launches = 0;
+    }
+    h->step_bytes = h->dep_bytes = h->pcg_bytes = h->sort_bytes = 0.0;
+    h->pcg_iters_prof = 0;
+    h->launches = 0;
+    DevCounters c{};
+    int rc = read_counters(h, c);
+    if (rc) return rc;
+    h->processed_at_reset = c.processed;
+    return SPG_OK;
+}
+
+int spg_get_profile(spg_handle *h, spg_profile *pr) {
+    if (!h || !pr) return SPG_E_INVALID;
+    CK(cudaStreamSynchronize(h->stream));
+    for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_resolve(*s);
+    DevCounters c{};
+    int rc = read_counters(h, c);
+    if (rc) return rc;
+    std::memset(pr, 0, sizeof(*pr));
+    pr->step_ms = h->ev_step.ms;
+    pr->step_launches = h->ev_step.launches;
+    pr->step_bytes = h->step_bytes + 112.0 * double(c.processed - h->processed_at_reset);
+    pr->deposit_ms = h->ev_dep.ms;
+    pr->deposit_launches = h->ev_dep.launches;
+    pr->deposit_bytes = h->dep_bytes;
+    pr->pcg_ms = h->ev_pcg.ms;
+    pr->pcg_solves = h->ev_pcg.launches;
+    pr->pcg_bytes = h->pcg_bytes;
+    pr->pcg_iters = h->pcg_iters_prof;
+    pr->efield_ms = h->ev_ef.ms;
+    pr->efield_launches = h->ev_ef.launches;
+    pr->sort_ms = h->ev_sort.ms;
+    pr->sort_launches = h->ev_sort.launches;
+    pr->sort_bytes = h->sort_bytes;
+    pr->kernel_launches = h->launches;
+    pr->occupied_tets = h->occupied;
+    return SPG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11), usable from host and
+// device code. The collision streams are keyed by (particle id, seed) and
+// counted by (step, draw), so a particle's draws do not depend on how
+// particles are ordered, sorted or sharded, and a restored run repeats them.
+#pragma once
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define SPG_HD __host__ __device__ __forceinline__
+#else
+#define SPG_HD inline
+#endif
+
+namespace spg {
+
+struct Philox4 {
+    uint32_t v[4];
+};
+
+SPG_HD void philox_mulhilo(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
+    const uint64_t p = uint64_t(a) * uint64_t(b);
+    hi = uint32_t(p >> 32);
+    lo = uint32_t(p);
+}
+
+SPG_HD Philox4 philox4x32_10(Philox4 c, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        philox_mulhilo(M0, c.v[0], hi0, lo0);
+        philox_mulhilo(M1, c.v[2], hi1, lo1);
+        Philox4 o;
+        o.v[0] = hi1 ^ c.v[1] ^ k0;
+        o.v[1] = lo1;
+        o.v[2] = hi0 ^ c.v[3] ^ k1;
+        o.v[3] = lo0;
+        c = o;
+        k0 += W0;
+        k1 += W1;
+    }
+    return c;
+}
+
+// 53-bit uniform double in [0, 1) from two 32-bit words.
+SPG_HD double u01_from(uint32_t a, uint32_t b) {
+    return (double(a >> 5) * 67108864.0 + double(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// Draw block `draw` of particle `id` at step `step`: four words.
+SPG_HD Philox4 collision_draw(uint64_t step, uint32_t draw, uint32_t id, uint32_t seed_lo, uint32_t seed_hi) {
+    Philox4 c;
+    c.v[0] = uint32_t(step);
+    c.v[1] = draw;
+    c.v[2] = uint32_t(step >> 32);
+    c.v[3] = seed_hi;
+    return philox4x32_10(c, id, seed_lo);
+}
+
+}  // namespace spg
