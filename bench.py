@@ -240,13 +240,22 @@ def run_gpu(args):
         ps = int(c.item())
     value = ps / (ms / 1e3)
     peak, peak_src = measured_peak()
-    step_bw = prof["step_bytes"] / (prof["step_ms"] / 1e3) / 1e9 if prof["step_ms"] > 0 else None
-    roof = {"kernel": "k_step64 (push + walk + collide + settle)", "bound": "hbm",
-            "achieved": step_bw, "peak": peak, "unit": "GB/s",
-            "frac": (step_bw / peak) if step_bw else None,
-            "traffic": args.traffic, "peak_source": peak_src,
-            "bytes_per_launch": prof["step_bytes"] / max(1, prof["step_launches"]),
-            "ms_per_launch": prof["step_ms"] / max(1, prof["step_launches"])}
+    phases = {
+        "step": ("k_step64 + k_walk_queue64 (push, move, collide, walk, settle)", prof["step_ms"],
+                 prof["step_bytes"], prof["step_launches"]),
+        "pcg": ("PCG iteration kernels (SELL-32 SpMV + dots, updates)", prof["pcg_ms"], prof["pcg_bytes"],
+                prof["pcg_iters"]),
+        "deposit": ("k_deposit64 (fixed-point P1 deposit)", prof["deposit_ms"], prof["deposit_bytes"],
+                    prof["deposit_launches"]),
+    }
+    dom = max(phases, key=lambda k: phases[k][1])
+    name, dms, dbytes, dl = phases[dom]
+    bw = dbytes / (dms / 1e3) / 1e9 if dms > 0 else None
+    roof = {"kernel": name, "phase": dom, "bound": "hbm", "achieved": bw, "peak": peak, "unit": "GB/s",
+            "frac": (bw / peak) if bw else None, "traffic": args.traffic, "peak_source": peak_src,
+            "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl)}
+    for k, (nm, ms_k, b_k, l_k) in phases.items():
+        roof[f"{k}_GBps"] = b_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
     breakdown = {k: prof[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")}
     breakdown["pcg_iters"] = prof["pcg_iters"]
     breakdown["pcg_GBps"] = prof["pcg_bytes"] / (prof["pcg_ms"] / 1e3) / 1e9 if prof["pcg_ms"] > 0 else None

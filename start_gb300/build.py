@@ -41,6 +41,7 @@ def _sources():
     return [
         ("kernels_particles.cu", common_nv + ["--fmad=false"]),
         ("kernels_pcg.cu", common_nv),
+        ("kernels_mixed.cu", common_nv),
         ("mesh_prep.cpp", common_cc + ["-fopenmp"]),
         ("capi.cpp", common_cc),
     ]

@@ -23,6 +23,13 @@ namespace {
 thread_local std::string g_create_error;
 
 constexpr int kEventPool = 8192;
+constexpr int kPcgChunk = 8;
+// Mixed form: FP32 inner PCG to 1e-4 of the outer residual (about what an
+// FP32 matrix can resolve for kappa ~ 1e4), at most this many inner
+// iterations per correction and outer refinement steps per solve.
+constexpr double kInnerRtol = 1e-4;
+constexpr int kInnerMaxIter = 2000;
+constexpr int kOuterMax = 40;
 
 struct EventSeries {
     std::vector<cudaEvent_t> start, stop;
@@ -48,6 +55,10 @@ struct spg_handle {
     int4 *nbr = nullptr, *ftri = nullptr, *tet_nodes = nullptr;
     double *node_xyz = nullptr;
     int32_t *row_ptr = nullptr, *col = nullptr;
+    int64_t *slice_ptr = nullptr;
+    int32_t *scol = nullptr;
+    double *sval = nullptr;
+    int64_t sell_entries = 0;
     double *val = nullptr, *inv_diag = nullptr, *dir_value = nullptr, *lift = nullptr, *dual_vol = nullptr;
     uint8_t *is_dir = nullptr;
     int32_t *vox_seed = nullptr;
@@ -56,8 +67,26 @@ struct spg_handle {
     // fields
     double *node_q = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr, *r = nullptr, *z = nullptr,
            *p = nullptr, *q = nullptr, *partials = nullptr;
+    double *efield = nullptr;                 // 3 per tet
+    unsigned long long *node_fix = nullptr;   // fixed-point deposit accumulators
+    int fix_bits = 40;                        // deposit quantum 2^-fix_bits of one particle's charge
     PcgScalars *sc = nullptr;
     int pcg_blocks = 1;
+    // PCG iterations are replayed as a CUDA graph of kPcgChunk iterations
+    // (3 kernels each); converged solves turn the remaining kernels into no-ops.
+    cudaGraphExec_t pcg_graph = nullptr;
+
+    // mixed form (precision == SPG_MIXED)
+    bool mixed = false;
+    double pbytes = 56.0;  // bytes per particle in HBM
+    TetRec32 *rec32 = nullptr;
+    double *cen = nullptr;  // 3 per tet
+    DevParticles32 Q[2]{};
+    float *sval32 = nullptr, *inv_diag32 = nullptr;
+    float *e32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+    double *partials32 = nullptr;
+    PcgScalars *sc32 = nullptr;
+    cudaGraphExec_t pcg32_graph = nullptr;
 
     // particles
     DevParticles P[2]{};
@@ -65,6 +94,8 @@ struct spg_handle {
     int64_t cap = 0, np = 0, n_active = 0, init_lost = 0;
     unsigned int *tri_count = nullptr;
     DevCounters *ctr = nullptr;
+    WalkItem *walkq = nullptr;       // capacity cap (particles)
+    unsigned int *walkq_n = nullptr;
     int64_t *n_alive_dev = nullptr;
     int32_t *sort_scratch = nullptr;
     int64_t occupied = 0;
@@ -131,7 +162,82 @@ void free_particles(spg_handle *h) {
         cudaFree(P.idf);
         P = DevParticles{};
     }
+    for (auto &Q : h->Q) {
+        cudaFree(Q.x);
+        cudaFree(Q.y);
+        cudaFree(Q.z);
+        cudaFree(Q.vx);
+        cudaFree(Q.vy);
+        cudaFree(Q.vz);
+        cudaFree(Q.tet);
+        cudaFree(Q.idf);
+        Q = DevParticles32{};
+    }
+    cudaFree(h->walkq);
+    h->walkq = nullptr;
     h->cap = 0;
+}
+
+MeshDev32 mesh_dev32(const spg_handle *h) {
+    MeshDev32 m;
+    m.rec = h->rec32;
+    m.rec64 = h->rec;
+    m.cen = h->cen;
+    m.nbr = h->nbr;
+    m.ftri = h->ftri;
+    m.tet_nodes = h->tet_nodes;
+    m.n_tets = h->n_tets;
+    return m;
+}
+
+PcgDev32 pcg_dev32(spg_handle *h) {
+    PcgDev32 f;
+    f.n = h->n_nodes;
+    f.slice_ptr = h->slice_ptr;
+    f.scol = h->scol;
+    f.sval = h->sval32;
+    f.inv_diag = h->inv_diag32;
+    f.e = h->e32;
+    f.r = h->r32;
+    f.z = h->z32;
+    f.p = h->p32;
+    f.q = h->q32;
+    f.partials = h->partials32;
+    f.sc = h->sc32;
+    f.blocks = h->pcg_blocks;
+    return f;
+}
+
+// Allocates both particle buffers (and the walk queue) for n particles.
+int alloc_particles(spg_handle *h, int64_t n) {
+    if (n <= h->cap) return SPG_OK;
+    free_particles(h);
+    if (h->mixed) {
+        for (auto &Q : h->Q) {
+            CK(dalloc(&Q.x, n));
+            CK(dalloc(&Q.y, n));
+            CK(dalloc(&Q.z, n));
+            CK(dalloc(&Q.vx, n));
+            CK(dalloc(&Q.vy, n));
+            CK(dalloc(&Q.vz, n));
+            CK(dalloc(&Q.tet, n));
+            CK(dalloc(&Q.idf, n));
+        }
+    } else {
+        for (auto &P : h->P) {
+            CK(dalloc(&P.x, n));
+            CK(dalloc(&P.y, n));
+            CK(dalloc(&P.z, n));
+            CK(dalloc(&P.vx, n));
+            CK(dalloc(&P.vy, n));
+            CK(dalloc(&P.vz, n));
+            CK(dalloc(&P.tet, n));
+            CK(dalloc(&P.idf, n));
+        }
+    }
+    CK(dalloc(&h->walkq, n));
+    h->cap = n;
+    return SPG_OK;
 }
 
 MeshDev mesh_dev(const spg_handle *h) {
@@ -172,7 +278,31 @@ StepConst step_const(const spg_handle *h) {
     c.seed_lo = uint32_t(p.seed);
     c.seed_hi = uint32_t(p.seed >> 32);
     c.step = h->step;
+    for (int k = 0; k < 3; ++k) {
+        c.lo_key[k] = order_key_host(c.lo[k]);
+        c.hi_key[k] = order_key_host(c.hi[k]);
+    }
+    const double two_vmin = 2.0 * std::fabs(p.min_velocity);
+    std::memcpy(&c.two_vmin_bits, &two_vmin, sizeof(two_vmin));
+    // FP32 screen of P = sigma |v| n dt: HS kp (v^2)^(1/2); VHS/VSS
+    // pi c1 (2 kT/m_r)^(w-1/2) n dt (v^2)^(1-w).
+    if (p.collision_model == SPG_COLL_HS) {
+        c.kp_f = float(c.sigma_hs * p.gas_concentration * p.dt);
+        c.pexp_f = 0.5f;
+    } else {
+        c.kp_f = float(3.14159265358979323846 * c.vhs_c1 * std::pow(c.two_kT / c.mr, c.expo) * p.gas_concentration *
+                       p.dt);
+        c.pexp_f = float(0.5 - c.expo);
+    }
     return c;
+}
+
+// Fixed-point deposit exponent: every node total stays below 2^63 even if
+// all n particles sit on one node.
+int fix_bits_for(int64_t n) {
+    int k = 52;
+    while (k > 8 && double(n + 1) * std::ldexp(1.0, k) >= 9.0e18) --k;
+    return k;
 }
 
 PcgDev pcg_dev(spg_handle *h) {
@@ -182,6 +312,9 @@ PcgDev pcg_dev(spg_handle *h) {
     d.col = h->col;
     d.val = h->val;
     d.inv_diag = h->inv_diag;
+    d.slice_ptr = h->slice_ptr;
+    d.scol = h->scol;
+    d.sval = h->sval;
     d.x = h->phi;
     d.r = h->r;
     d.z = h->z;
@@ -240,34 +373,49 @@ void ev_destroy(EventSeries &s) {
 }
 
 // ---- phases
+template <class T>
+int copy_tail(spg_handle *h, T *dst, const T *src, int64_t o, int64_t n) {
+    CK(cudaMemcpyAsync(dst + o, src + o, sizeof(T) * n, cudaMemcpyDeviceToDevice, h->stream));
+    return SPG_OK;
+}
+
 int do_resort(spg_handle *h) {
     if (!h->have_particles || h->np == 0) return SPG_OK;
     ev_begin(h, h->ev_sort);
-    DevParticles &src = h->P[h->cur], &dst = h->P[1 - h->cur];
-    launch_resort(src, dst, h->n_active, h->n_tets, h->sort_scratch, h->n_alive_dev, h->stream);
+    const int64_t tail = h->np - h->n_active, o = h->n_active;
+    int rc = SPG_OK;
+    if (h->mixed) {
+        DevParticles32 &src = h->Q[h->cur], &dst = h->Q[1 - h->cur];
+        launch_resort32(src, dst, h->n_active, h->n_tets, h->sort_scratch, h->n_alive_dev, h->stream);
+        // Particles past n_active are dead already; they keep their slots.
+        if (tail > 0)
+            for (auto pr : {std::make_pair(dst.x, src.x), std::make_pair(dst.y, src.y), std::make_pair(dst.z, src.z),
+                            std::make_pair(dst.vx, src.vx), std::make_pair(dst.vy, src.vy),
+                            std::make_pair(dst.vz, src.vz)})
+                if ((rc = copy_tail(h, pr.first, pr.second, o, tail))) return rc;
+        if (tail > 0 && ((rc = copy_tail(h, dst.tet, src.tet, o, tail)) || (rc = copy_tail(h, dst.idf, src.idf, o, tail))))
+            return rc;
+    } else {
+        DevParticles &src = h->P[h->cur], &dst = h->P[1 - h->cur];
+        launch_resort(src, dst, h->n_active, h->n_tets, h->sort_scratch, h->n_alive_dev, h->stream);
+        if (tail > 0)
+            for (auto pr : {std::make_pair(dst.x, src.x), std::make_pair(dst.y, src.y), std::make_pair(dst.z, src.z),
+                            std::make_pair(dst.vx, src.vx), std::make_pair(dst.vy, src.vy),
+                            std::make_pair(dst.vz, src.vz)})
+                if ((rc = copy_tail(h, pr.first, pr.second, o, tail))) return rc;
+        if (tail > 0 && ((rc = copy_tail(h, dst.tet, src.tet, o, tail)) || (rc = copy_tail(h, dst.idf, src.idf, o, tail))))
+            return rc;
+    }
     ev_end(h, h->ev_sort);
     h->launches += h->n_active > 0 ? 5 : 3;
     CK(cudaGetLastError());
-    // Particles past n_active are all dead already; keep them behind the
-    // sorted range by copying the tail once (they never move again).
-    if (h->n_active < h->np) {
-        const int64_t tail = h->np - h->n_active, o = h->n_active;
-        CK(cudaMemcpyAsync(dst.x + o, src.x + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.y + o, src.y + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.z + o, src.z + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.vx + o, src.vx + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.vy + o, src.vy + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.vz + o, src.vz + o, 8 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.tet + o, src.tet + o, 4 * tail, cudaMemcpyDeviceToDevice, h->stream));
-        CK(cudaMemcpyAsync(dst.idf + o, src.idf + o, 4 * tail, cudaMemcpyDeviceToDevice, h->stream));
-    }
     int64_t na = 0;
     unsigned long long occ = 0;
     CK(cudaMemcpyAsync(&na, h->n_alive_dev, sizeof(na), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(&occ, sort_occupied_counter(h->sort_scratch), sizeof(occ), cudaMemcpyDeviceToHost,
                        h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (h->prof) h->sort_bytes += double(h->n_active) * 2.0 * 56.0 + 8.0 * double(h->n_tets + 1);
+    if (h->prof) h->sort_bytes += double(h->n_active) * 2.0 * h->pbytes + 8.0 * double(h->n_tets + 1);
     h->cur = 1 - h->cur;
     h->n_active = na;
     h->occupied = int64_t(occ);
@@ -276,22 +424,57 @@ int do_resort(spg_handle *h) {
 
 int do_gather(spg_handle *h) {
     if (!h->have_particles) return fail(h, SPG_E_STATE, "gather: no particles set");
-    CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * h->n_nodes, h->stream));
+    CK(cudaMemsetAsync(h->node_fix, 0, sizeof(unsigned long long) * h->n_nodes, h->stream));
     ev_begin(h, h->ev_dep);
-    launch_deposit64(h->P[h->cur], h->n_active, mesh_dev(h), h->prm.weight * h->prm.charge, h->node_q, h->stream);
+    if (h->mixed)
+        launch_deposit32(h->Q[h->cur], h->n_active, mesh_dev32(h), h->fix_bits, h->node_fix, h->stream);
+    else
+        launch_deposit64(h->P[h->cur], h->n_active, mesh_dev(h), h->fix_bits, h->node_fix, h->stream);
     ev_end(h, h->ev_dep);
+    launch_fix_to_charge(h->node_fix, std::ldexp(h->prm.weight * h->prm.charge, -h->fix_bits), h->node_q,
+                         h->n_nodes, h->stream);
+    h->launches += 1;
     if (h->n_active > 0) h->launches += 1;
     CK(cudaGetLastError());
     if (h->prof)
-        h->dep_bytes += 32.0 * double(h->n_active) + 112.0 * double(h->occupied ? h->occupied : h->n_tets) +
+        h->dep_bytes += (h->mixed ? 20.0 : 32.0) * double(h->n_active) +
+                        (h->mixed ? 52.0 : 112.0) * double(h->occupied ? h->occupied : h->n_tets) +
                         16.0 * double(h->n_nodes);
     h->charge_valid = true;
     return SPG_OK;
 }
 
-int do_solve(spg_handle *h) {
+// E from phi for both forms (and the FP32 push increment of the mixed form).
+int update_field(spg_handle *h) {
+    ev_begin(h, h->ev_ef);
+    launch_efield64(mesh_dev(h), h->rec, h->efield, h->phi, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
+    h->launches += 1;
+    if (h->mixed) {
+        launch_push32(h->rec32, h->efield, h->n_tets, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
+        h->launches += 1;
+    }
+    ev_end(h, h->ev_ef);
+    CK(cudaGetLastError());
+    return SPG_OK;
+}
+
+int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped) {
+    int rc = update_field(h);
+    if (rc) return rc;
+    h->cg_iters_last = iters;
+    h->cg_iters_total += iters;
+    h->cg_solves++;
+    h->cg_relres_last = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+    if (capped) {
+        std::ostringstream os;
+        os << "PCG did not converge: " << iters << " iterations, relative residual " << h->cg_relres_last;
+        return fail(h, SPG_E_NOT_CONVERGED, os.str());
+    }
+    return SPG_OK;
+}
+
+int do_solve64(spg_handle *h) {
     const int64_t n = h->n_nodes;
-    launch_pcg_rhs(h->node_q, 1.0 / h->prm.epsilon0, h->lift, h->is_dir, h->dir_value, h->b, n, h->stream);
     PcgScalars init{};
     init.tol2 = (h->prm.cg_rtol * h->prm.cg_rtol);
     init.max_iter = h->prm.cg_max_iter;
@@ -299,48 +482,105 @@ int do_solve(spg_handle *h) {
     PcgDev d = pcg_dev(h);
     ev_begin(h, h->ev_pcg);
     launch_pcg_setup(d, h->b, h->stream);
-    h->launches += 2;
+    h->launches += 1;
     PcgScalars hs{};
-    int chunk = 4;
+    if (!h->pcg_graph) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < kPcgChunk; ++k) launch_pcg_iteration(d, h->stream);
+        CK(cudaStreamEndCapture(h->stream, &g));
+        CK(cudaGraphInstantiate(&h->pcg_graph, g, 0));
+        cudaGraphDestroy(g);
+    }
     for (;;) {
-        for (int k = 0; k < chunk; ++k) launch_pcg_iteration(d, h->stream);
-        h->launches += 3 * chunk;
-        CK(cudaGetLastError());
+        CK(cudaGraphLaunch(h->pcg_graph, h->stream));
+        h->launches += 3 * kPcgChunk;
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         if (hs.converged) break;
-        chunk = std::min(chunk * 2, 64);
     }
     ev_end(h, h->ev_pcg);
-    ev_begin(h, h->ev_ef);
-    launch_efield64(mesh_dev(h), h->rec, h->phi, h->stream);
-    ev_end(h, h->ev_ef);
-    h->launches += 1;
-    CK(cudaGetLastError());
-    h->cg_iters_last = hs.iters;
-    h->cg_iters_total += hs.iters;
-    h->cg_solves++;
-    h->cg_relres_last = hs.bb > 0.0 ? std::sqrt(hs.rr / hs.bb) : 0.0;
     if (h->prof) {
         h->pcg_iters_prof += hs.iters;
         h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz) + 4.0 * double(n + 1) + 72.0 * double(n));
     }
-    if (hs.converged == 2) {
-        std::ostringstream os;
-        os << "PCG did not converge: " << hs.iters << " iterations, relative residual " << h->cg_relres_last;
-        return fail(h, SPG_E_NOT_CONVERGED, os.str());
+    return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
+}
+
+// Mixed form: FP32-SpMV PCG corrections inside FP64 iterative refinement,
+// stopped on the FP64 residual ||b - A x|| <= cg_rtol ||b||.
+int do_solve_mixed(spg_handle *h) {
+    const int64_t n = h->n_nodes;
+    PcgScalars outer{}, inner{};
+    outer.tol2 = h->prm.cg_rtol * h->prm.cg_rtol;
+    inner.tol2 = kInnerRtol * kInnerRtol;
+    inner.max_iter = kInnerMaxIter;
+    CK(cudaMemcpyAsync(h->sc, &outer, sizeof(outer), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->sc32, &inner, sizeof(inner), cudaMemcpyHostToDevice, h->stream));
+    PcgDev d = pcg_dev(h);
+    PcgDev32 f = pcg_dev32(h);
+    if (!h->pcg32_graph) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < kPcgChunk; ++k) launch_pcg32_iteration(f, h->stream);
+        CK(cudaStreamEndCapture(h->stream, &g));
+        CK(cudaGraphInstantiate(&h->pcg32_graph, g, 0));
+        cudaGraphDestroy(g);
     }
-    return SPG_OK;
+    ev_begin(h, h->ev_pcg);
+    int32_t total = 0;
+    PcgScalars hs{}, hi{};
+    bool capped = true;
+    for (int outer_it = 0; outer_it <= kOuterMax; ++outer_it) {
+        launch_refine_setup(d, f, h->b, h->stream);
+        h->launches += 1;
+        CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (hs.converged) {
+            capped = false;
+            break;
+        }
+        if (outer_it == kOuterMax || total >= h->prm.cg_max_iter) break;
+        for (;;) {
+            CK(cudaGraphLaunch(h->pcg32_graph, h->stream));
+            h->launches += 3 * kPcgChunk;
+            CK(cudaMemcpyAsync(&hi, h->sc32, sizeof(hi), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (hi.converged) break;
+        }
+        total += hi.iters;
+        launch_refine_apply(h->phi, h->e32, n, h->stream);
+        h->launches += 1;
+    }
+    ev_end(h, h->ev_pcg);
+    if (h->prof) {
+        h->pcg_iters_prof += total;
+        h->pcg_bytes += double(total) * (8.0 * double(h->nnz) + 4.0 * double(n + 1) + 36.0 * double(n));
+    }
+    return finish_solve(h, total, hs.rr, hs.bb, capped);
+}
+
+int do_solve(spg_handle *h) {
+    launch_pcg_rhs(h->node_q, 1.0 / h->prm.epsilon0, h->lift, h->is_dir, h->dir_value, h->b, h->n_nodes, h->stream);
+    h->launches += 1;
+    return h->mixed ? do_solve_mixed(h) : do_solve64(h);
 }
 
 int do_process(spg_handle *h) {
     StepConst c = step_const(h);
     ev_begin(h, h->ev_step);
-    launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->ctr, h->stream);
+    if (h->mixed)
+        launch_step32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
+                      h->stream);
+    else
+        launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
+                      h->stream);
     ev_end(h, h->ev_step);
-    if (h->n_active > 0) h->launches += 1;
+    if (h->n_active > 0) h->launches += 2;  // step kernel + queued walks
     CK(cudaGetLastError());
-    if (h->prof) h->step_bytes += 152.0 * double(h->occupied ? h->occupied : std::min(h->n_tets, h->n_active));
+    if (h->prof)
+        h->step_bytes += (h->mixed ? 92.0 : 152.0) *
+                         double(h->occupied ? h->occupied : std::min(h->n_tets, h->n_active));
     h->step++;
     return SPG_OK;
 }
@@ -382,7 +622,8 @@ int reset_run_state(spg_handle *h) {
     CK(cudaMemsetAsync(h->tri_count, 0, sizeof(unsigned int) * std::max<int64_t>(h->n_tris, 1), h->stream));
     CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * h->n_nodes, h->stream));
-    launch_zero_efield(h->rec, h->n_tets, h->stream);
+    launch_zero_efield(h->rec, h->efield, h->n_tets, h->stream);
+    if (h->mixed) launch_push32(h->rec32, h->efield, h->n_tets, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return SPG_OK;
@@ -449,8 +690,6 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     *out = nullptr;
     std::string msg;
     if (validate_params(params, msg)) return fail(h, SPG_E_INVALID, "spg_create: " + msg);
-    if (params->precision != SPG_FP64)
-        return fail(h, SPG_E_INVALID, "spg_create: only the FP64 form is available in this build");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(h, SPG_E_NO_DEVICE, "spg_create: no CUDA device");
@@ -472,6 +711,8 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     h = H.get();
     h->prm = *params;
     h->device = params->device;
+    h->mixed = params->precision == SPG_MIXED;
+    h->pbytes = h->mixed ? 32.0 : 56.0;
     CK(cudaSetDevice(h->device));
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->n_nodes = hm.n_nodes;
@@ -495,6 +736,20 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(upload(reinterpret_cast<int32_t **>(&h->ftri), hm.ftri, s));
     CK(upload(reinterpret_cast<int32_t **>(&h->tet_nodes), hm.tet_nodes, s));
     CK(upload(&h->node_xyz, hm.node_xyz, s));
+    {
+        std::vector<int64_t> sp;
+        std::vector<int32_t> sc;
+        std::vector<double> sv;
+        build_sell32(hm.n_nodes, hm.row_ptr.data(), hm.col.data(), hm.val.data(), sp, sc, sv);
+        h->sell_entries = int64_t(sv.size());
+        CK(upload(&h->slice_ptr, sp, s));
+        CK(upload(&h->scol, sc, s));
+        CK(upload(&h->sval, sv, s));
+        if (h->mixed) {
+            std::vector<float> sv32(sv.begin(), sv.end());
+            CK(upload(&h->sval32, sv32, s));
+        }
+    }
     CK(upload(&h->row_ptr, hm.row_ptr, s));
     CK(upload(&h->col, hm.col, s));
     CK(upload(&h->val, hm.val, s));
@@ -505,8 +760,38 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(upload(&h->dual_vol, hm.dual_vol, s));
     CK(upload(&h->vox_seed, hm.vox_seed, s));
     h->phi_init = hm.dir_value;
+    if (h->mixed) {
+        // FP32 maps about the centroid, FP64 centroids, FP32 inner-solver arrays
+        std::vector<TetRec32> r32(hm.n_tets);
+        std::vector<double> cen(3 * hm.n_tets);
+        for (int64_t t = 0; t < hm.n_tets; ++t) {
+            for (int c = 0; c < 3; ++c) {
+                double acc = 0.0;
+                for (int k = 0; k < 4; ++k) acc += hm.node_xyz[3 * int64_t(hm.tet_nodes[4 * t + k]) + c];
+                cen[3 * t + c] = 0.25 * acc;
+            }
+            TetRec32 &q = r32[t];
+            for (int k = 0; k < 9; ++k) q.M[k] = float(hm.rec[t].M[k]);
+            for (int c = 0; c < 3; ++c) {
+                q.H[c] = 0.0f;
+                q.cen[c] = float(cen[3 * t + c]);
+            }
+            q.ezero = 1u;
+        }
+        CK(upload(&h->rec32, r32, s));
+        CK(upload(&h->cen, cen, s));
+        std::vector<float> id32(inv_diag.begin(), inv_diag.end());
+        CK(upload(&h->inv_diag32, id32, s));
+        CK(dalloc(&h->e32, hm.n_nodes));
+        CK(dalloc(&h->r32, hm.n_nodes));
+        CK(dalloc(&h->z32, hm.n_nodes));
+        CK(dalloc(&h->p32, hm.n_nodes));
+        CK(dalloc(&h->q32, hm.n_nodes));
+    }
     const int64_t n = h->n_nodes;
     CK(dalloc(&h->node_q, n));
+    CK(dalloc(&h->node_fix, n));
+    CK(dalloc(&h->efield, 3 * size_t(h->n_tets)));
     CK(dalloc(&h->rho, n));
     CK(dalloc(&h->phi, n));
     CK(dalloc(&h->b, n));
@@ -517,9 +802,13 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     h->pcg_blocks = pcg_blocks(n);
     CK(dalloc(&h->partials, 3 * size_t(h->pcg_blocks)));
     CK(dalloc(&h->sc, 1));
+    CK(dalloc(&h->partials32, 3 * size_t(pcg_blocks(hm.n_nodes))));
+    CK(dalloc(&h->sc32, 1));
+    CK(cudaMemsetAsync(h->sc32, 0, sizeof(PcgScalars), s));
     CK(cudaMemsetAsync(h->sc, 0, sizeof(PcgScalars), s));
     CK(dalloc(&h->tri_count, std::max<int64_t>(h->n_tris, 1)));
     CK(dalloc(&h->ctr, 1));
+    CK(dalloc(&h->walkq_n, 1));
     CK(dalloc(&h->n_alive_dev, 1));
     CK(dalloc(&h->sort_scratch, size_t(sort_scratch_words(h->n_tets))));
     rc = reset_run_state(h);
@@ -536,9 +825,14 @@ int spg_destroy(spg_handle *h) {
     void *ptrs[] = {h->rec,      h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
                     h->node_q,   h->rho,      h->phi,      h->b,         h->r,        h->z,         h->p,
-                    h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch};
+                    h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,
+                    h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
+                    h->p32,      h->q32,      h->partials32, h->sc32,
+                    h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch, h->walkq_n};
     for (void *ptr : ptrs) cudaFree(ptr);
     for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
+    if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
+    if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return SPG_OK;
@@ -561,19 +855,9 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
     if (n > 0 && (!pos || !vel)) return fail(h, SPG_E_INVALID, "set_particles: null pos/vel");
     CK(cudaSetDevice(h->device));
     cudaStream_t s = h->stream;
-    if (n > h->cap) {
-        free_particles(h);
-        for (auto &P : h->P) {
-            CK(dalloc(&P.x, n));
-            CK(dalloc(&P.y, n));
-            CK(dalloc(&P.z, n));
-            CK(dalloc(&P.vx, n));
-            CK(dalloc(&P.vy, n));
-            CK(dalloc(&P.vz, n));
-            CK(dalloc(&P.tet, n));
-            CK(dalloc(&P.idf, n));
-        }
-        h->cap = n;
+    {
+        const int rc = alloc_particles(h, n);
+        if (rc) return rc;
     }
     h->cur = 0;
     h->np = n;
@@ -601,7 +885,10 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
         }
         CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
         launch_count_lost(dtet, n, dlost, s);
-        launch_init_particles(dpos, dvel, dtet, n, h->P[0], s);
+        if (h->mixed)
+            launch_to_local(dpos, dvel, dtet, h->cen, n, h->Q[0], s);
+        else
+            launch_init_particles(dpos, dvel, dtet, n, h->P[0], s);
         CK(cudaGetLastError());
         unsigned long long lost = 0;
         CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
@@ -613,6 +900,7 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
         cudaFree(dlost);
     }
     h->have_particles = true;
+    h->fix_bits = fix_bits_for(n);
     return reset_run_state(h);
 }
 
@@ -630,7 +918,10 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
     if (vel) CK(dalloc(&dvel, 3 * n));
     if (tet) CK(dalloc(&dtet, n));
     if (flags) CK(dalloc(&dfl, n));
-    launch_gather_by_id(h->P[h->cur], n, dpos, dvel, dtet, dfl, s);
+    if (h->mixed)
+        launch_gather32(h->Q[h->cur], n, h->cen, dpos, dvel, dtet, dfl, s);
+    else
+        launch_gather_by_id(h->P[h->cur], n, dpos, dvel, dtet, dfl, s);
     CK(cudaGetLastError());
     if (pos) CK(cudaMemcpyAsync(pos, dpos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
     if (vel) CK(cudaMemcpyAsync(vel, dvel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
@@ -763,8 +1054,10 @@ int spg_set_potential(spg_handle *h, const double *phi) {
     if (!h || !phi) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
     CK(cudaMemcpyAsync(h->phi, phi, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
-    launch_efield64(mesh_dev(h), h->rec, h->phi, h->stream);
-    CK(cudaGetLastError());
+    {
+        const int rc = update_field(h);
+        if (rc) return rc;
+    }
     CK(cudaStreamSynchronize(h->stream));
     return SPG_OK;
 }
@@ -772,11 +1065,8 @@ int spg_set_potential(spg_handle *h, const double *phi) {
 int spg_get_efield(spg_handle *h, double *E) {
     if (!h || !E) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
-    std::vector<TetRec> rec(h->n_tets);
-    CK(cudaMemcpyAsync(rec.data(), h->rec, sizeof(TetRec) * h->n_tets, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(E, h->efield, sizeof(double) * 3 * h->n_tets, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    for (int64_t t = 0; t < h->n_tets; ++t)
-        for (int k = 0; k < 3; ++k) E[3 * t + k] = rec[t].E[k];
     return SPG_OK;
 }
 
@@ -798,7 +1088,8 @@ int spg_locate(spg_handle *h, int64_t n, const double *pos, int32_t *tet_out) {
     return SPG_OK;
 }
 
-// Checkpoint layout: header, 8 particle arrays (current order), phi, triangle
+// Checkpoint layout: header, 8 particle arrays (current order; positions and
+// velocities are 8 B in the FP64 form, 4 B in the mixed form), phi, triangle
 // counters, device counters.
 namespace {
 struct CkptHeader {
@@ -807,11 +1098,28 @@ struct CkptHeader {
     int64_t cg_iters_total;
     int32_t cg_iters_last, cg_solves;
     double cg_relres_last;
+    int32_t precision, pad;
 };
-constexpr uint64_t kMagic = 0x5350474B50543031ull;  // "SPGKPT01"
-size_t ckpt_bytes(const spg_handle *h) {
-    return sizeof(CkptHeader) + size_t(h->np) * (6 * 8 + 4 + 4) + size_t(h->n_nodes) * 8 + size_t(h->n_tris) * 4 +
+constexpr uint64_t kMagic = 0x5350474B50543032ull;  // "SPGKPT02"
+size_t particle_bytes(const spg_handle *h) { return h->mixed ? 32 : 56; }
+size_t ckpt_bytes_for(const spg_handle *h, int64_t np) {
+    return sizeof(CkptHeader) + size_t(np) * particle_bytes(h) + size_t(h->n_nodes) * 8 + size_t(h->n_tris) * 4 +
            sizeof(DevCounters);
+}
+size_t ckpt_bytes(const spg_handle *h) { return ckpt_bytes_for(h, h->np); }
+// The 8 particle arrays of buffer `which` with their element sizes.
+void particle_arrays(spg_handle *h, int which, void *ptr[8], size_t sz[8]) {
+    if (h->mixed) {
+        const DevParticles32 &Q = h->Q[which];
+        void *a[8] = {Q.x, Q.y, Q.z, Q.vx, Q.vy, Q.vz, Q.tet, Q.idf};
+        for (int k = 0; k < 8; ++k) ptr[k] = a[k];
+    } else {
+        const DevParticles &P = h->P[which];
+        void *a[8] = {P.x, P.y, P.z, P.vx, P.vy, P.vz, P.tet, P.idf};
+        for (int k = 0; k < 8; ++k) ptr[k] = a[k];
+    }
+    for (int k = 0; k < 6; ++k) sz[k] = h->mixed ? 4 : 8;
+    sz[6] = sz[7] = 4;
 }
 }  // namespace
 
@@ -828,7 +1136,7 @@ int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
     CK(cudaSetDevice(h->device));
     CkptHeader hd{};
     hd.magic = kMagic;
-    hd.version = 1;
+    hd.version = 2;
     hd.np = h->np;
     hd.n_active = h->n_active;
     hd.step = h->step;
@@ -840,21 +1148,19 @@ int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
     hd.cg_iters_last = h->cg_iters_last;
     hd.cg_solves = h->cg_solves;
     hd.cg_relres_last = h->cg_relres_last;
+    hd.precision = h->prm.precision;
     char *o = static_cast<char *>(buf);
     std::memcpy(o, &hd, sizeof(hd));
     o += sizeof(hd);
-    const DevParticles &P = h->P[h->cur];
     const int64_t n = h->np;
     cudaStream_t s = h->stream;
-    double *darr[6] = {P.x, P.y, P.z, P.vx, P.vy, P.vz};
-    for (double *a : darr) {
-        CK(cudaMemcpyAsync(o, a, 8 * n, cudaMemcpyDeviceToHost, s));
-        o += 8 * n;
+    void *arr[8];
+    size_t sz[8];
+    particle_arrays(h, h->cur, arr, sz);
+    for (int k = 0; k < 8; ++k) {
+        if (n) CK(cudaMemcpyAsync(o, arr[k], sz[k] * n, cudaMemcpyDeviceToHost, s));
+        o += sz[k] * n;
     }
-    CK(cudaMemcpyAsync(o, P.tet, 4 * n, cudaMemcpyDeviceToHost, s));
-    o += 4 * n;
-    CK(cudaMemcpyAsync(o, P.idf, 4 * n, cudaMemcpyDeviceToHost, s));
-    o += 4 * n;
     CK(cudaMemcpyAsync(o, h->phi, 8 * h->n_nodes, cudaMemcpyDeviceToHost, s));
     o += 8 * h->n_nodes;
     if (h->n_tris) CK(cudaMemcpyAsync(o, h->tri_count, 4 * h->n_tris, cudaMemcpyDeviceToHost, s));
@@ -869,44 +1175,30 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     if (bytes < sizeof(CkptHeader)) return fail(h, SPG_E_INVALID, "restore: buffer too small");
     CkptHeader hd;
     std::memcpy(&hd, buf, sizeof(hd));
-    if (hd.magic != kMagic || hd.version != 1) return fail(h, SPG_E_INVALID, "restore: not a checkpoint");
+    if (hd.magic != kMagic || hd.version != 2) return fail(h, SPG_E_INVALID, "restore: not a checkpoint");
     if (hd.n_nodes != h->n_nodes || hd.n_tris != h->n_tris)
         return fail(h, SPG_E_INVALID, "restore: checkpoint is for a different mesh");
+    if (hd.precision != h->prm.precision)
+        return fail(h, SPG_E_INVALID, "restore: checkpoint is for the other precision form");
     if (hd.np < 0 || hd.np > kMaxParticles || hd.n_active < 0 || hd.n_active > hd.np)
         return fail(h, SPG_E_INVALID, "restore: corrupt header");
-    CK(cudaSetDevice(h->device));
-    // allocate through set_particles with an empty upload of the right size
     const int64_t n = hd.np;
-    if (bytes < sizeof(CkptHeader) + size_t(n) * 56 + size_t(h->n_nodes) * 8 + size_t(h->n_tris) * 4 +
-                    sizeof(DevCounters))
-        return fail(h, SPG_E_INVALID, "restore: buffer too small");
-    if (n > h->cap) {
-        free_particles(h);
-        for (auto &P : h->P) {
-            CK(dalloc(&P.x, n));
-            CK(dalloc(&P.y, n));
-            CK(dalloc(&P.z, n));
-            CK(dalloc(&P.vx, n));
-            CK(dalloc(&P.vy, n));
-            CK(dalloc(&P.vz, n));
-            CK(dalloc(&P.tet, n));
-            CK(dalloc(&P.idf, n));
-        }
-        h->cap = n;
+    if (bytes < ckpt_bytes_for(h, n)) return fail(h, SPG_E_INVALID, "restore: buffer too small");
+    CK(cudaSetDevice(h->device));
+    {
+        const int rc = alloc_particles(h, n);
+        if (rc) return rc;
     }
     h->cur = 0;
     const char *o = static_cast<const char *>(buf) + sizeof(hd);
-    const DevParticles &P = h->P[0];
     cudaStream_t s = h->stream;
-    double *darr[6] = {P.x, P.y, P.z, P.vx, P.vy, P.vz};
-    for (double *a : darr) {
-        CK(cudaMemcpyAsync(a, o, 8 * n, cudaMemcpyHostToDevice, s));
-        o += 8 * n;
+    void *arr[8];
+    size_t sz[8];
+    particle_arrays(h, 0, arr, sz);
+    for (int k = 0; k < 8; ++k) {
+        if (n) CK(cudaMemcpyAsync(arr[k], o, sz[k] * n, cudaMemcpyHostToDevice, s));
+        o += sz[k] * n;
     }
-    CK(cudaMemcpyAsync(P.tet, o, 4 * n, cudaMemcpyHostToDevice, s));
-    o += 4 * n;
-    CK(cudaMemcpyAsync(P.idf, o, 4 * n, cudaMemcpyHostToDevice, s));
-    o += 4 * n;
     CK(cudaMemcpyAsync(h->phi, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
     o += 8 * h->n_nodes;
     if (h->n_tris) CK(cudaMemcpyAsync(h->tri_count, o, 4 * h->n_tris, cudaMemcpyHostToDevice, s));
@@ -922,8 +1214,14 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     h->cg_solves = hd.cg_solves;
     h->cg_relres_last = hd.cg_relres_last;
     h->have_particles = true;
-    launch_efield64(mesh_dev(h), h->rec, h->phi, s);
-    if (h->cg_solves == 0) launch_zero_efield(h->rec, h->n_tets, s);
+    if (h->cg_solves == 0) {
+        launch_zero_efield(h->rec, h->efield, h->n_tets, s);
+        if (h->mixed) launch_push32(h->rec32, h->efield, h->n_tets, h->prm.charge, h->prm.mass, h->prm.dt, s);
+    } else {
+        const int rc = update_field(h);
+        if (rc) return rc;
+    }
+    h->fix_bits = fix_bits_for(h->np);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     return SPG_OK;

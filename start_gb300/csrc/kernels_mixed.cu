@@ -1,0 +1,532 @@
+// Mixed-precision form of the particle step (SPG_MIXED).
+//
+// Particle state is 32 B: position in FP32 relative to the owning tet's
+// centroid, velocity in FP32, tet and id/flags. Per tet a 64-B record holds
+// the FP32 barycentric map about the centroid (lambda_{1..3} = 1/4 + M x),
+// the FP32 push increment and the centroid in FP32 (for the modelling-box
+// test). FP64 is kept where the result depends on a sign near zero or on
+// cancellation:
+//   * a barycentric coordinate within 1e-5 of zero is recomputed in FP64
+//     (the FP64 map of the plain form, x promoted to FP64);
+//   * a face crossing re-bases the position into the neighbour's frame in
+//     FP64: x' = x + (c_old - c_new), then rounds to FP32;
+//   * the deposit accumulates in 64-bit fixed point (exact).
+// Every other operation (push, move, collision, exit parameter) is FP32,
+// which on GB300 issues ~60x faster than FP64.
+#include <cmath>
+
+#include "philox.h"
+#include "spg_internal.h"
+
+namespace spg {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr float kNearZero = 1e-5f;
+
+enum { W_INSIDE = 0, W_SURFACE = 1, W_EXIT = 2, W_CAP = 3 };
+
+struct Geo32 {
+    float M[9];
+};
+
+__device__ __forceinline__ void load_geo32(const TetRec32 *__restrict__ rec, int t, Geo32 &g) {
+    const float4 *rp = reinterpret_cast<const float4 *>(rec + t);
+    const float4 a = __ldg(rp), b = __ldg(rp + 1);
+    const float c = __ldg(&rec[t].M[8]);
+    g.M[0] = a.x; g.M[1] = a.y; g.M[2] = a.z; g.M[3] = a.w;
+    g.M[4] = b.x; g.M[5] = b.y; g.M[6] = b.z; g.M[7] = b.w; g.M[8] = c;
+}
+
+__device__ __forceinline__ void bary32(const Geo32 &g, float x, float y, float z, float l[4]) {
+    l[1] = fmaf(g.M[2], z, fmaf(g.M[1], y, fmaf(g.M[0], x, 0.25f)));
+    l[2] = fmaf(g.M[5], z, fmaf(g.M[4], y, fmaf(g.M[3], x, 0.25f)));
+    l[3] = fmaf(g.M[8], z, fmaf(g.M[7], y, fmaf(g.M[6], x, 0.25f)));
+    l[0] = 1.0f - l[1] - l[2] - l[3];
+}
+
+// FP64 barycentrics of an FP32 local position (near-zero decisions).
+__device__ __noinline__ void bary64_local(const TetRec *__restrict__ rec64, int t, float x, float y, float z,
+                                         float l[4]) {
+    const double *M = rec64[t].M;
+    const double dx = x, dy = y, dz = z;
+    const double l1 = 0.25 + (M[0] * dx + M[1] * dy + M[2] * dz);
+    const double l2 = 0.25 + (M[3] * dx + M[4] * dy + M[5] * dz);
+    const double l3 = 0.25 + (M[6] * dx + M[7] * dy + M[8] * dz);
+    const double l0 = 1.0 - l1 - l2 - l3;
+    // keep only the sign information exactly; magnitudes are FP32-rounded
+    l[0] = float(l0);
+    l[1] = float(l1);
+    l[2] = float(l2);
+    l[3] = float(l3);
+    for (int k = 0; k < 4; ++k)
+        if (l[k] == 0.0f && (k == 0 ? l0 : (k == 1 ? l1 : (k == 2 ? l2 : l3))) < 0.0) l[k] = -1e-30f;
+}
+
+__device__ __forceinline__ int comp(const int4 &v, int f) {
+    return f == 0 ? v.x : (f == 1 ? v.y : (f == 2 ? v.z : v.w));
+}
+
+struct MixedArgs {
+    DevParticles32 p;
+    int64_t n;
+    const TetRec32 *rec;
+    const TetRec *rec64;
+    const double *cen;  // 3 per tet
+    const int4 *nbr, *ftri, *tet_nodes;
+    int64_t n_tets;
+};
+
+// Inside test of an end point with FP64 rescue near zero.
+__device__ __forceinline__ bool inside32(const MixedArgs &a, const Geo32 &g, int t, float x, float y, float z,
+                                         float l[4]) {
+    bary32(g, x, y, z, l);
+    const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
+    if (mn > kNearZero) return true;
+    if (mn < -kNearZero) return false;
+    bary64_local(a.rec64, t, x, y, z, l);
+    return l[0] >= 0.0f && l[1] >= 0.0f && l[2] >= 0.0f && l[3] >= 0.0f;
+}
+
+// Re-base a local position from tet a to tet b: x + (c_a - c_b) in FP64.
+__device__ __forceinline__ void rebase(const double *__restrict__ cen, int ta, int tb, float &x, float &y,
+                                       float &z) {
+    x = float(double(x) + (cen[3 * ta] - cen[3 * tb]));
+    y = float(double(y) + (cen[3 * ta + 1] - cen[3 * tb + 1]));
+    z = float(double(z) + (cen[3 * ta + 2] - cen[3 * tb + 2]));
+}
+
+struct Walk32 {
+    int tet, status, tri, crossings;
+    float hx, hy, hz;  // end (or hit) point in the final tet's frame
+};
+
+// Segment walk in local frames: p0, p1 are given in tet t's frame and are
+// re-based on every crossing. Same exit rule as the FP64 walk (smallest
+// crossing parameter among faces with lambda(p1) < 0, entry face excluded).
+__device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float p0y, float p0z, float p1x,
+                                      float p1y, float p1z, int max_cross) {
+    Walk32 o;
+    o.crossings = 0;
+    o.tri = -1;
+    int enter = -1;
+    Geo32 g;
+    load_geo32(a.rec, t, g);
+    for (;;) {
+        float l1[4];
+        if (inside32(a, g, t, p1x, p1y, p1z, l1)) {
+            o.tet = t;
+            o.status = W_INSIDE;
+            o.hx = p1x;
+            o.hy = p1y;
+            o.hz = p1z;
+            return o;
+        }
+        float l0[4];
+        bary32(g, p0x, p0y, p0z, l0);
+        int best = -1;
+        float sb = 0.0f;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            if (f == enter || !(l1[f] < 0.0f)) continue;
+            const float s = l0[f] / (l0[f] - l1[f]);
+            if (best < 0 || s < sb) {
+                best = f;
+                sb = s;
+            }
+        }
+        if (best < 0) {
+            o.tet = t;
+            o.status = W_INSIDE;
+            o.hx = p1x;
+            o.hy = p1y;
+            o.hz = p1z;
+            return o;
+        }
+        const int tri = comp(__ldg(a.ftri + t), best);
+        if (tri >= 0) {
+            o.tet = t;
+            o.status = W_SURFACE;
+            o.tri = tri;
+            o.hx = fmaf(sb, p1x - p0x, p0x);
+            o.hy = fmaf(sb, p1y - p0y, p0y);
+            o.hz = fmaf(sb, p1z - p0z, p0z);
+            return o;
+        }
+        const int nb = comp(__ldg(a.nbr + t), best);
+        if (nb < 0 || o.crossings == max_cross) {
+            o.tet = t;
+            o.status = nb < 0 ? W_EXIT : W_CAP;
+            o.hx = p1x;
+            o.hy = p1y;
+            o.hz = p1z;
+            return o;
+        }
+        o.crossings++;
+        const int tn = nb >> 2;
+        rebase(a.cen, t, tn, p0x, p0y, p0z);
+        rebase(a.cen, t, tn, p1x, p1y, p1z);
+        t = tn;
+        enter = nb & 3;
+        load_geo32(a.rec, t, g);
+    }
+}
+
+// Collision in FP32 (same Philox streams and laws as the FP64 form).
+__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, float &vx, float &vy, float &vz) {
+    const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
+    const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+    const float P = c.kp_f * exp2f(c.pexp_f * log2f(v2));
+    const float u0 = float(r.v[0] >> 8) * 5.9604644775390625e-8f;
+    if (!(u0 < P)) return false;
+    const float u1 = float(r.v[2] >> 8) * 5.9604644775390625e-8f;
+    const Philox4 r2 = collision_draw(uint64_t(c.step), 1u, id, c.seed_lo, c.seed_hi);
+    const float u2 = float(r2.v[0] >> 8) * 5.9604644775390625e-8f;
+    float xc;
+    if (c.model == SPG_COLL_HS)
+        xc = -1.0f + 2.0f * u1;
+    else if (c.model == SPG_COLL_VHS)
+        xc = u1;
+    else
+        xc = 2.0f * powf(u1, float(c.inv_alpha)) - 1.0f;
+    const float xs = sqrtf(fmaxf(0.0f, 1.0f - xc * xc));
+    float sp, cp;
+    sincosf((2.0f * kPiF) * u2, &sp, &cp);
+    const float mcp = float(c.mass_cp), mct = float(c.mass_ct);
+    const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
+    const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
+    float ex = xs * cp * mp, ey = xs * sp * mp, ez = xc * mp;
+    if (c.model == SPG_COLL_VSS && mp > 0.0f) {
+        // rotation by (beta, gamma) of the relative velocity, without the
+        // angles: cos beta = pz/|p|, sin beta >= 0; (cos, sin) gamma from (px, py)
+        const float cb = pvz / mp, sb = sqrtf(fmaxf(0.0f, 1.0f - cb * cb));
+        const float rxy = sqrtf(fmaf(pvy, pvy, pvx * pvx));
+        const float cg = rxy > 0.0f ? pvx / rxy : 1.0f, sg = rxy > 0.0f ? pvy / rxy : 0.0f;
+        const float tx = cb * ex + sb * ez, tz = -sb * ex + cb * ez;
+        ex = cg * tx - sg * ey;
+        ey = sg * tx + cg * ey;
+        ez = tz;
+    }
+    vx = fmaf(vx, mcp, ex);
+    vy = fmaf(vy, mcp, ey);
+    vz = fmaf(vz, mcp, ez);
+    return true;
+}
+
+struct WalkItem32 {
+    int32_t i;
+    float x0, y0, z0;
+};
+
+__global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkItem32 *__restrict__ wq,
+                                                unsigned int *__restrict__ wq_n, DevCounters *ctr) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    unsigned processed = 0, coll = 0, lost = 0;
+    bool want_walk = false;
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (i < a.n) {
+        uint32_t idf = a.p.idf[i];
+        if (!(idf & kDead)) {
+            processed = 1;
+            const int t = a.p.tet[i];
+            x = a.p.x[i];
+            y = a.p.y[i];
+            z = a.p.z[i];
+            float vx = a.p.vx[i], vy = a.p.vy[i], vz = a.p.vz[i];
+            const float vmin = float(c.vmin);
+            const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
+            const TetRec32 &R = a.rec[t];
+            const float gx = __ldg(&R.cen[0]) + x, gy = __ldg(&R.cen[1]) + y, gz = __ldg(&R.cen[2]) + z;
+            const bool in_box = gx >= float(c.lo[0]) && gx <= float(c.hi[0]) && gy >= float(c.lo[1]) &&
+                                gy <= float(c.hi[1]) && gz >= float(c.lo[2]) && gz <= float(c.hi[2]);
+            if (!slow && in_box) {
+                if (!__ldg(&R.ezero)) {
+                    const float hx = __ldg(&R.H[0]), hy = __ldg(&R.H[1]), hz = __ldg(&R.H[2]);
+                    vx = (vx + hx) + hx;
+                    vy = (vy + hy) + hy;
+                    vz = (vz + hz) + hz;
+                }
+                const float dt = float(c.dt);
+                const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
+                if (!(nx == x && ny == y && nz == z)) {
+                    if (c.model != SPG_COLL_NONE) coll = collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
+                    if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
+                        a.p.idf[i] = idf | kLost;
+                        lost = 1;
+                    } else {
+                        Geo32 g;
+                        load_geo32(a.rec, t, g);
+                        float l[4];
+                        bary32(g, nx, ny, nz, l);
+                        const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
+                        want_walk = !(mn > kNearZero);
+                        a.p.x[i] = nx;
+                        a.p.y[i] = ny;
+                        a.p.z[i] = nz;
+                    }
+                }
+                a.p.vx[i] = vx;
+                a.p.vy[i] = vy;
+                a.p.vz[i] = vz;
+            }
+        }
+    }
+    const unsigned ballot = __ballot_sync(kFull, want_walk);
+    if (ballot) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(ballot) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(wq_n, unsigned(__popc(ballot)));
+        base = __shfl_sync(kFull, base, leader);
+        if (want_walk) {
+            WalkItem32 &w = wq[base + __popc(ballot & ((1u << lane) - 1u))];
+            w.i = int32_t(i);
+            w.x0 = x;
+            w.y0 = y;
+            w.z0 = z;
+        }
+    }
+    const unsigned long long s0 = __reduce_add_sync(kFull, processed), s1 = __reduce_add_sync(kFull, coll);
+    const unsigned long long s2 = __reduce_add_sync(kFull, lost);
+    if ((threadIdx.x & 31) == 0) {
+        if (s0) atomicAdd(&ctr->processed, s0);
+        if (s1) atomicAdd(&ctr->collisions, s1);
+        if (s2) atomicAdd(&ctr->lost, s2);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_walk_queue32(MixedArgs a, int max_cross, const WalkItem32 *__restrict__ wq,
+                                                      const unsigned int *__restrict__ wq_n,
+                                                      unsigned int *__restrict__ tri_count, DevCounters *ctr) {
+    const unsigned nq = *wq_n;
+    unsigned cross = 0, settled = 0, lost = 0, capped = 0;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const WalkItem32 it = wq[q];
+        const int64_t i = it.i;
+        const int t = a.p.tet[i];
+        const Walk32 w = walk32(a, t, it.x0, it.y0, it.z0, a.p.x[i], a.p.y[i], a.p.z[i], max_cross);
+        cross += unsigned(w.crossings);
+        a.p.x[i] = w.hx;
+        a.p.y[i] = w.hy;
+        a.p.z[i] = w.hz;
+        const uint32_t idf = a.p.idf[i];
+        if (w.status == W_SURFACE) {
+            atomicAdd(tri_count + w.tri, 1u);
+            a.p.idf[i] = idf | kSettled;
+            settled++;
+        } else if (w.status != W_INSIDE) {
+            a.p.idf[i] = idf | kLost;
+            lost++;
+            if (w.status == W_CAP) capped++;
+        }
+        if (w.tet != t) a.p.tet[i] = w.tet;
+    }
+    const unsigned long long s0 = __reduce_add_sync(kFull, cross), s1 = __reduce_add_sync(kFull, settled);
+    const unsigned long long s2 = __reduce_add_sync(kFull, lost), s3 = __reduce_add_sync(kFull, capped);
+    if ((threadIdx.x & 31) == 0) {
+        if (s0) atomicAdd(&ctr->crossings, s0);
+        if (s1) atomicAdd(&ctr->settled, s1);
+        if (s2) atomicAdd(&ctr->lost, s2);
+        if (s3) atomicAdd(&ctr->capped, s3);
+    }
+}
+
+// round(x * 2^k) of a float with integer ops (round half away from zero).
+__device__ __forceinline__ long long fix_round32(float x, int k) {
+    const int b = __float_as_int(x);
+    const int e = (b >> 23) & 0xff;
+    if (e == 0) return 0;
+    const long long mant = (b & 0x7fffff) | 0x800000;
+    const int sh = 150 - e - k;
+    long long r;
+    if (sh <= 0)
+        r = sh < -39 ? 0 : (mant << (-sh));
+    else if (sh > 30)
+        r = 0;
+    else
+        r = (mant + (1LL << (sh - 1))) >> sh;
+    return b < 0 ? -r : r;
+}
+
+__global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned long long *__restrict__ node_fix) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int key = -1;
+    long long v[4] = {0, 0, 0, 0};
+    if (i < a.n && !(a.p.idf[i] & kDead)) {
+        key = a.p.tet[i];
+        Geo32 g;
+        load_geo32(a.rec, key, g);
+        float l[4];
+        bary32(g, a.p.x[i], a.p.y[i], a.p.z[i], l);
+        v[1] = fix_round32(l[1], k);
+        v[2] = fix_round32(l[2], k);
+        v[3] = fix_round32(l[3], k);
+        v[0] = (1LL << k) - v[1] - v[2] - v[3];
+    }
+    const int prev = __shfl_up_sync(kFull, key, 1);
+    const bool head = lane == 0 || prev != key;
+    const unsigned heads = __ballot_sync(kFull, head);
+    if (heads != 1u) {
+        const int start = 31 - __clz(heads & (kFull >> (31 - lane)));
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const long long up = __shfl_up_sync(kFull, v[q], off);
+                if (lane - off >= start) v[q] += up;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(kFull, v[q], off);
+        }
+    }
+    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+    if (tail && key >= 0) {
+        const int4 tn = __ldg(a.tet_nodes + key);
+        atomicAdd(node_fix + tn.x, (unsigned long long)v[0]);
+        atomicAdd(node_fix + tn.y, (unsigned long long)v[1]);
+        atomicAdd(node_fix + tn.z, (unsigned long long)v[2]);
+        atomicAdd(node_fix + tn.w, (unsigned long long)v[3]);
+    }
+}
+
+// Push increment in FP32 from the FP64 field of the plain form's kernel.
+__global__ void k_push32(TetRec32 *__restrict__ rec, const double *__restrict__ efield, int64_t n, double charge,
+                         double mass, double dt) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double E0 = efield[3 * t], E1 = efield[3 * t + 1], E2 = efield[3 * t + 2];
+    rec[t].H[0] = float(((charge * E0) / mass * dt) / 2.0);
+    rec[t].H[1] = float(((charge * E1) / mass * dt) / 2.0);
+    rec[t].H[2] = float(((charge * E2) / mass * dt) / 2.0);
+    rec[t].ezero = (E0 == 0.0 && E1 == 0.0 && E2 == 0.0) ? 1u : 0u;
+}
+
+// Global FP64 state -> local FP32 state (and back).
+__global__ void k_to_local(const double *__restrict__ pos, const double *__restrict__ vel,
+                           const int32_t *__restrict__ tet, const double *__restrict__ cen, int64_t n,
+                           DevParticles32 p) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t t = tet[i];
+    const int64_t tc = t < 0 ? 0 : t;
+    p.x[i] = float(pos[3 * i] - (t < 0 ? 0.0 : cen[3 * tc]));
+    p.y[i] = float(pos[3 * i + 1] - (t < 0 ? 0.0 : cen[3 * tc + 1]));
+    p.z[i] = float(pos[3 * i + 2] - (t < 0 ? 0.0 : cen[3 * tc + 2]));
+    p.vx[i] = float(vel[3 * i]);
+    p.vy[i] = float(vel[3 * i + 1]);
+    p.vz[i] = float(vel[3 * i + 2]);
+    p.tet[i] = t;
+    p.idf[i] = uint32_t(i) | (t < 0 ? kLost : 0u);
+}
+
+__global__ void k_gather32(DevParticles32 p, int64_t n, const double *__restrict__ cen, double *pos, double *vel,
+                           int32_t *tet, uint32_t *flags) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t idf = p.idf[i];
+    const int64_t id = idf & kIdMask;
+    const int32_t t = p.tet[i];
+    const int64_t tc = t < 0 ? 0 : t;
+    const double ox = t < 0 ? 0.0 : cen[3 * tc], oy = t < 0 ? 0.0 : cen[3 * tc + 1], oz = t < 0 ? 0.0 : cen[3 * tc + 2];
+    if (pos) {
+        pos[3 * id] = ox + double(p.x[i]);
+        pos[3 * id + 1] = oy + double(p.y[i]);
+        pos[3 * id + 2] = oz + double(p.z[i]);
+    }
+    if (vel) {
+        vel[3 * id] = p.vx[i];
+        vel[3 * id + 1] = p.vy[i];
+        vel[3 * id + 2] = p.vz[i];
+    }
+    if (tet) tet[id] = t;
+    if (flags) flags[id] = ((idf & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((idf & kLost) ? SPG_FLAG_LOST : 0u);
+}
+
+__global__ void k_sort_scatter32(DevParticles32 src, DevParticles32 dst, int64_t n, int n_tets,
+                                 int32_t *__restrict__ offs) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int key = i < n ? ((src.idf[i] & kDead) ? n_tets : src.tet[i]) : -1;
+    const unsigned peers = __match_any_sync(kFull, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(offs + key, __popc(peers));
+    base = __shfl_sync(kFull, base, leader);
+    if (key < 0) return;
+    const int64_t j = base + __popc(peers & ((1u << lane) - 1u));
+    dst.x[j] = src.x[i];
+    dst.y[j] = src.y[i];
+    dst.z[j] = src.z[i];
+    dst.vx[j] = src.vx[i];
+    dst.vy[j] = src.vy[i];
+    dst.vz[j] = src.vz[i];
+    dst.tet[j] = src.tet[i];
+    dst.idf[j] = src.idf[i];
+}
+
+inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1) / block); }
+
+MixedArgs make_args(const DevParticles32 &p, int64_t n, const MeshDev32 &m) {
+    MixedArgs a;
+    a.p = p;
+    a.n = n;
+    a.rec = m.rec;
+    a.rec64 = m.rec64;
+    a.cen = m.cen;
+    a.nbr = m.nbr;
+    a.ftri = m.ftri;
+    a.tet_nodes = m.tet_nodes;
+    a.n_tets = m.n_tets;
+    return a;
+}
+
+}  // namespace
+
+void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c,
+                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s) {
+    if (n <= 0) return;
+    const MixedArgs a = make_args(p, n, m);
+    cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
+    k_step32<<<grid_for(n, 256), 256, 0, s>>>(a, c, static_cast<WalkItem32 *>(wq), wq_n, ctr);
+    k_walk_queue32<<<152 * 8, 128, 0, s>>>(a, c.max_cross, static_cast<WalkItem32 *>(wq), wq_n, tri_count, ctr);
+}
+
+void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
+                      cudaStream_t s) {
+    if (n <= 0) return;
+    k_deposit32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), k, node_fix);
+}
+
+void launch_push32(TetRec32 *rec, const double *efield, int64_t n_tets, double charge, double mass, double dt,
+                   cudaStream_t s) {
+    k_push32<<<grid_for(n_tets, 256), 256, 0, s>>>(rec, efield, n_tets, charge, mass, dt);
+}
+
+void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
+                     DevParticles32 p, cudaStream_t s) {
+    if (n <= 0) return;
+    k_to_local<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, cen, n, p);
+}
+
+void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,
+                     uint32_t *flags, cudaStream_t s) {
+    if (n <= 0) return;
+    k_gather32<<<grid_for(n, 256), 256, 0, s>>>(p, n, cen, pos, vel, tet, flags);
+}
+
+void launch_resort32(const DevParticles32 &src, DevParticles32 dst, int64_t n, int64_t n_tets, int32_t *scratch,
+                     int64_t *n_alive_dev, cudaStream_t s) {
+    launch_sort_prepare(src.tet, src.idf, n, n_tets, scratch, n_alive_dev, s);
+    if (n > 0) k_sort_scatter32<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, int(n_tets), sort_offsets(scratch));
+}
+
+size_t walk_item32_bytes() { return sizeof(WalkItem32); }
+
+}  // namespace spg

@@ -4,6 +4,16 @@
 // Compiled with --fmad=false: every a*b+c stays a separate multiply and add,
 // matching the CPU oracle (built with -ffp-contract=off) bit for bit on the
 // collisionless path. Division and sqrt are IEEE (CUDA defaults for double).
+//
+// FP64 on GB300 issues at about 2 instructions per clock per SM (FP32: ~128),
+// and double<->float conversions share that pipe. The step kernel therefore
+// keeps FP64 semantics exactly while spending FP64 instructions only where the
+// result is stored: push, move and the offset from the tet origin. Every
+// yes/no decision of the reference algorithm (slow particle, inside the
+// modelling box, degenerate segment, inside the tet, collision) is taken by an
+// integer or FP32 screen with a proven error bound; when a screen cannot
+// decide, the exact FP64 expression (the oracle's) decides. The state written
+// is therefore identical to an all-FP64 evaluation.
 #include <cmath>
 #include <cstdio>
 
@@ -24,17 +34,13 @@ struct TetGeo {
     double x0[3];
 };
 
-__device__ __forceinline__ void load_geo(const TetRec *__restrict__ rec, int t, TetGeo &g, double E[3]) {
+__device__ __forceinline__ void load_geo(const TetRec *__restrict__ rec, int t, TetGeo &g) {
     const double2 *rp = reinterpret_cast<const double2 *>(rec + t);
     double2 a = __ldg(rp + 0), b = __ldg(rp + 1), c = __ldg(rp + 2), d = __ldg(rp + 3);
     double2 e = __ldg(rp + 4), f = __ldg(rp + 5);
     g.M[0] = a.x; g.M[1] = a.y; g.M[2] = b.x; g.M[3] = b.y; g.M[4] = c.x; g.M[5] = c.y;
     g.M[6] = d.x; g.M[7] = d.y; g.M[8] = e.x;
     g.x0[0] = e.y; g.x0[1] = f.x; g.x0[2] = f.y;
-    if (E) {
-        double2 h = __ldg(rp + 6), k = __ldg(rp + 7);
-        E[0] = h.x; E[1] = h.y; E[2] = k.x;
-    }
 }
 
 // Barycentric coordinates; same expression order as the oracle.
@@ -50,6 +56,53 @@ __device__ __forceinline__ int comp(const int4 &v, int f) {
     return f == 0 ? v.x : (f == 1 ? v.y : (f == 2 ? v.z : v.w));
 }
 
+// ---------------------------------------------------------------- screens
+// Float from the high word of a double (sign, exponent, top 20 mantissa
+// bits), integer ops only: |f - x| <= 2^-20 |x| for 2^-126 <= |x| < 2^128;
+// 0 below that range, +-inf above.
+__device__ __forceinline__ float hi_float(double x) {
+    const int hi = __double2hiint(x);
+    const int a = hi & 0x7fffffff;
+    const int r = a < (897 << 20) ? 0 : (a >= (1151 << 20) ? 0x7f800000 : ((a - (896 << 20)) << 3));
+    return __int_as_float(r | (hi & int(0x80000000)));
+}
+
+// Order-preserving integer key of a double (see order_key_host).
+__device__ __forceinline__ long long order_key(double x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ULL) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+// IEEE equality of two finite doubles from their bit patterns.
+__device__ __forceinline__ bool same_value(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return x == y || ((x | y) << 1) == 0;
+}
+
+// Screened inside test: true = lambda(p) >= 0 in all four coordinates for
+// certain; false = undecided (the caller evaluates the exact FP64 walk).
+// The FP32 barycentrics use d = p - x0 (the exact FP64 subtraction of the
+// oracle) and M, d truncated to 20 mantissa bits, so each product carries a
+// relative error below 2^-19 + 3*2^-24; with S_i = sum_j |M_ij d_j| the
+// FP32 value is within 2.2e-6 S_i of the FP64 one. The margin used is
+// 4e-6 S_i + 1e-30 (for terms flushed to zero), and lambda_0 = 1 - sum gets
+// the sum of the three margins plus 1e-6 for its own FP32 rounding.
+__device__ __forceinline__ bool inside_sure(const TetGeo &g, double d0, double d1, double d2) {
+    const float e0 = hi_float(d0), e1 = hi_float(d1), e2 = hi_float(d2);
+    float l[3], b[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float m0 = hi_float(g.M[3 * r]), m1 = hi_float(g.M[3 * r + 1]), m2 = hi_float(g.M[3 * r + 2]);
+        l[r] = fmaf(m2, e2, fmaf(m1, e1, m0 * e0));
+        const float s = fmaf(fabsf(m2), fabsf(e2), fmaf(fabsf(m1), fabsf(e1), fabsf(m0) * fabsf(e0)));
+        b[r] = fmaf(4e-6f, s, 1e-30f);
+    }
+    const float l0 = 1.0f - l[0] - l[1] - l[2];
+    const float b0 = b[0] + b[1] + b[2] + 1e-6f;
+    return l[0] > b[0] && l[1] > b[1] && l[2] > b[2] && l0 > b0;
+}
+
 struct WalkOut {
     int tet, status, tri, crossings;
     double s;
@@ -61,8 +114,8 @@ struct WalkOut {
 // parameter s = l0/(l0 - l1) along the segment is smallest (lowest local face
 // index on ties). A face carrying a surface triangle stops the walk there
 // (when stop_surface); a boundary face without one is an exit.
-__device__ WalkOut walk64(const MeshDev &m, int t, TetGeo g, double p0x, double p0y, double p0z, double p1x,
-                          double p1y, double p1z, int max_cross, bool stop_surface) {
+__device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double p0x, double p0y, double p0z,
+                                       double p1x, double p1y, double p1z, int max_cross, bool stop_surface) {
     WalkOut o;
     o.crossings = 0;
     o.tri = -1;
@@ -117,13 +170,13 @@ __device__ WalkOut walk64(const MeshDev &m, int t, TetGeo g, double p0x, double 
         o.crossings++;
         t = nb >> 2;
         enter = nb & 3;
-        load_geo(m.rec, t, g, nullptr);
+        load_geo(m.rec, t, g);
     }
 }
 
-// Gas collision of one particle: HSModel.cpp:6-42, VHSModel.cpp:6-52,
-// VSSModel.cpp:6-54. Stationary target; v' = m_p/(m_p+m_t) v + |m_t/(m_p+m_t) v| n.
-__device__ bool collide64(const StepConst &c, uint32_t id, double &vx, double &vy, double &vz) {
+// Collision probability exactly as the reference evaluates it:
+// HSModel.cpp:12-15, VHSModel.cpp:14-25 (and VSSModel.cpp, same formula).
+__device__ __noinline__ double probability64(const StepConst c, double vx, double vy, double vz) {
     const double vmod = sqrt(vx * vx + vy * vy + vz * vz);
     double sigma;
     if (c.model == SPG_COLL_HS) {
@@ -133,13 +186,12 @@ __device__ bool collide64(const StepConst &c, uint32_t id, double &vx, double &v
         const double d2 = c.vhs_c1 * pow(base, c.expo);
         sigma = kPi * d2;
     }
-    const double P = ((sigma * vmod) * c.gas_n) * c.dt;
-    const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
-    const double u0 = u01_from(r.v[0], r.v[1]);
-    if (!(u0 < P)) return false;
-    const double u1 = u01_from(r.v[2], r.v[3]);
-    const Philox4 r2 = collision_draw(uint64_t(c.step), 1u, id, c.seed_lo, c.seed_hi);
-    const double u2 = u01_from(r2.v[0], r2.v[1]);
+    return ((sigma * vmod) * c.gas_n) * c.dt;
+}
+
+// Post-collision velocity (HSModel.cpp:24-39, VHSModel.cpp:31-46,
+// VSSModel.cpp:32-48): stationary target; v' = m_p/(m_p+m_t) v + |m_t/(m_p+m_t) v| n.
+__device__ __noinline__ void scatter64(const StepConst c, double u1, double u2, double &vx, double &vy, double &vz) {
     double xi_cos;
     if (c.model == SPG_COLL_HS)
         xi_cos = -1.0 + 2.0 * u1;
@@ -169,80 +221,120 @@ __device__ bool collide64(const StepConst &c, uint32_t id, double &vx, double &v
     vx = ex + cmx;
     vy = ey + cmy;
     vz = ez + cmz;
+}
+
+// Gas collision decision and scattering. Draw u0 (53-bit) decides; the FP32
+// screen compares the interval of u0 known from its top 24 bits with
+// P_f (1 -+ 1e-4). P_f = kp (v^2)^pexp from 20-bit velocity components has a
+// relative error below 2e-5, so a decided screen agrees with u0 < P in FP64.
+__device__ __forceinline__ bool collide(const StepConst &c, uint32_t id, double &vx, double &vy, double &vz) {
+    const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
+    const float fx = hi_float(vx), fy = hi_float(vy), fz = hi_float(vz);
+    const float v2 = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
+    const float pf = c.kp_f * exp2f(c.pexp_f * log2f(v2));
+    const float ulo = float(r.v[0] >> 8) * 5.9604644775390625e-8f;  // 2^-24
+    const float uhi = ulo + 5.9604644775390625e-8f;
+    bool hit;
+    if (uhi < pf * (1.0f - 1e-4f))
+        hit = true;
+    else if (ulo > pf * (1.0f + 1e-4f))
+        hit = false;
+    else
+        hit = u01_from(r.v[0], r.v[1]) < probability64(c, vx, vy, vz);
+    if (!hit) return false;
+    const double u1 = u01_from(r.v[2], r.v[3]);
+    const Philox4 r2 = collision_draw(uint64_t(c.step), 1u, id, c.seed_lo, c.seed_hi);
+    scatter64(c, u1, u01_from(r2.v[0], r2.v[1]), vx, vy, vz);
     return true;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(unsigned v) { return __reduce_add_sync(kFull, v); }
 
+// Finite test from the exponent bits (no FP64 compare).
+__device__ __forceinline__ bool finite_bits(double x) {
+    return ((__double2hiint(x) >> 20) & 0x7ff) != 0x7ff;
+}
+
+// Warp-aggregated append of this lane's item to the walk queue.
+__device__ __forceinline__ void queue_walk(WalkItem *__restrict__ q, unsigned int *__restrict__ qn, bool want,
+                                           int64_t i, double x, double y, double z) {
+    const unsigned ballot = __ballot_sync(kFull, want);
+    if (!ballot) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(qn, unsigned(__popc(ballot)));
+    base = __shfl_sync(kFull, base, leader);
+    if (want) {
+        WalkItem &w = q[base + __popc(ballot & ((1u << lane) - 1u))];
+        w.i = int32_t(i);
+        w.x0 = x;
+        w.y0 = y;
+        w.z0 = z;
+    }
+}
+
 // One particle step (ParticleDynamicsProcessor.cpp:161-200 order):
 // settled? -> |v| < vmin? -> outside bbox? -> E push (Boris, B = 0) -> move ->
 // gas collision -> surface crossing along the move segment.
-__global__ void __launch_bounds__(256) k_step64(DevParticles p, int64_t n, MeshDev m, StepConst c,
-                                                unsigned int *__restrict__ tri_count, DevCounters *ctr) {
+// The new position is written for every moving particle. A particle whose
+// end point is not certainly inside its tet is appended to the walk queue
+// with its start point; k_walk_queue64 then walks it in full warps (FP64
+// instructions issue per warp on GB300, so a walk taken by a few lanes of
+// every warp would cost the whole warp its FP64 throughput).
+__global__ void __launch_bounds__(256, 4) k_step64(DevParticles p, int64_t n, MeshDev m, StepConst c,
+                                                WalkItem *__restrict__ wq, unsigned int *__restrict__ wq_n,
+                                                DevCounters *ctr) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     unsigned processed = 0, coll = 0, cross = 0, settled = 0, lost = 0, capped = 0;
+    bool want_walk = false;
+    double x = 0.0, y = 0.0, z = 0.0;
     if (i < n) {
         uint32_t idf = p.idf[i];
         if (!(idf & kDead)) {
             processed = 1;
             const int t = p.tet[i];
-            double x = p.x[i], y = p.y[i], z = p.z[i];
+            x = p.x[i];
+            y = p.y[i];
+            z = p.z[i];
             double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
-            const double vmod = sqrt(vx * vx + vy * vy + vz * vz);
-            const bool inside_box = x >= c.lo[0] && x <= c.hi[0] && y >= c.lo[1] && y <= c.hi[1] &&
-                                    z >= c.lo[2] && z <= c.hi[2];
-            if (!(vmod < c.vmin) && inside_box) {
-                TetGeo g;
-                double E[3];
-                load_geo(m.rec, t, g, E);
-                if (!(E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0)) {
+            // |v| < vmin: certainly false when some |v_k| >= 2 vmin (bit compare of
+            // non-negative doubles); otherwise the exact FP64 test.
+            const long long ax = __double_as_longlong(vx) & 0x7fffffffffffffffLL;
+            const long long ay = __double_as_longlong(vy) & 0x7fffffffffffffffLL;
+            const long long az = __double_as_longlong(vz) & 0x7fffffffffffffffLL;
+            bool slow = false;
+            if (ax < c.two_vmin_bits && ay < c.two_vmin_bits && az < c.two_vmin_bits)
+                slow = sqrt(vx * vx + vy * vy + vz * vz) < c.vmin;
+            const long long kx = order_key(x), ky = order_key(y), kz = order_key(z);
+            const bool inside_box = kx >= c.lo_key[0] && kx <= c.hi_key[0] && ky >= c.lo_key[1] &&
+                                    ky <= c.hi_key[1] && kz >= c.lo_key[2] && kz <= c.hi_key[2];
+            if (!slow && inside_box) {
+                const TetRec *rp = m.rec + t;
+                if (!__ldg(&rp->ezero)) {
                     // Particle::electroMagneticPush (Particle.cpp:196-234) with B = 0:
-                    // v- = v + a dt/2, rotation is the identity, v = v- + a dt/2.
-                    const double ax = (c.charge * E[0]) / c.mass;
-                    const double ay = (c.charge * E[1]) / c.mass;
-                    const double az = (c.charge * E[2]) / c.mass;
-                    const double hx = (ax * c.dt) / 2.0, hy = (ay * c.dt) / 2.0, hz = (az * c.dt) / 2.0;
+                    // v- = v + a dt/2, the rotation is the identity, v = v- + a dt/2.
+                    const double hx = __ldg(&rp->H[0]), hy = __ldg(&rp->H[1]), hz = __ldg(&rp->H[2]);
                     vx = (vx + hx) + hx;
                     vy = (vy + hy) + hy;
                     vz = (vz + hz) + hz;
                 }
                 // Particle::updatePosition (Particle.cpp:157-165)
                 const double nx = x + vx * c.dt, ny = y + vy * c.dt, nz = z + vz * c.dt;
-                if (!(nx == x && ny == y && nz == z)) {
+                if (!(same_value(nx, x) && same_value(ny, y) && same_value(nz, z))) {
                     const uint32_t id = idf & kIdMask;
-                    if (c.model != SPG_COLL_NONE) coll = collide64(c, id, vx, vy, vz) ? 1u : 0u;
-                    if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
+                    if (c.model != SPG_COLL_NONE) coll = collide(c, id, vx, vy, vz) ? 1u : 0u;
+                    if (!(finite_bits(nx) && finite_bits(ny) && finite_bits(nz))) {
                         idf |= kLost;
                         lost = 1;
                         p.idf[i] = idf;
                     } else {
-                        const WalkOut w = walk64(m, t, g, x, y, z, nx, ny, nz, c.max_cross, true);
-                        cross = unsigned(w.crossings);
-                        if (w.status == W_INSIDE) {
-                            x = nx;
-                            y = ny;
-                            z = nz;
-                        } else if (w.status == W_SURFACE) {
-                            x = x + w.s * (nx - x);
-                            y = y + w.s * (ny - y);
-                            z = z + w.s * (nz - z);
-                            atomicAdd(tri_count + w.tri, 1u);
-                            idf |= kSettled;
-                            settled = 1;
-                            p.idf[i] = idf;
-                        } else {
-                            x = nx;
-                            y = ny;
-                            z = nz;
-                            idf |= kLost;
-                            lost = 1;
-                            capped = w.status == W_CAP ? 1u : 0u;
-                            p.idf[i] = idf;
-                        }
-                        if (w.tet != t) p.tet[i] = w.tet;
-                        p.x[i] = x;
-                        p.y[i] = y;
-                        p.z[i] = z;
+                        TetGeo g;
+                        load_geo(m.rec, t, g);
+                        want_walk = !inside_sure(g, nx - g.x0[0], ny - g.x0[1], nz - g.x0[2]);
+                        p.x[i] = nx;
+                        p.y[i] = ny;
+                        p.z[i] = nz;
                     }
                 }
                 p.vx[i] = vx;
@@ -251,6 +343,7 @@ __global__ void __launch_bounds__(256) k_step64(DevParticles p, int64_t n, MeshD
             }
         }
     }
+    queue_walk(wq, wq_n, want_walk, i, x, y, z);
     // Block-level counter reduction, one atomic per counter per block.
     __shared__ unsigned long long sh[8][6];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -277,54 +370,136 @@ __global__ void __launch_bounds__(256) k_step64(DevParticles p, int64_t n, MeshD
     }
 }
 
-// P1 deposit: node_q[n] += w q lambda_n(x_p) for every alive particle.
-// Lanes of a warp hold consecutive (tet-sorted) particles; equal tets form
-// runs, each run is summed with a segmented shuffle scan and its last lane
-// issues the four atomics, so a warp inside one tet does 4 atomics, not 128.
-__global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, MeshDev m, double wq,
-                                                   double *__restrict__ node_q) {
+// Exact FP64 walk of the queued particles (start point from the queue, end
+// point already in the position arrays), one particle per lane.
+__global__ void __launch_bounds__(128) k_walk_queue64(DevParticles p, MeshDev m, int max_cross,
+                                                      const WalkItem *__restrict__ wq,
+                                                      const unsigned int *__restrict__ wq_n,
+                                                      unsigned int *__restrict__ tri_count, DevCounters *ctr) {
+    const unsigned nq = *wq_n;
+    unsigned cross = 0, settled = 0, lost = 0, capped = 0;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const WalkItem it = wq[q];
+        const int64_t i = it.i;
+        const int t = p.tet[i];
+        const double nx = p.x[i], ny = p.y[i], nz = p.z[i];
+        TetGeo g;
+        load_geo(m.rec, t, g);
+        const WalkOut w = walk64(m, t, g, it.x0, it.y0, it.z0, nx, ny, nz, max_cross, true);
+        cross += unsigned(w.crossings);
+        uint32_t idf = p.idf[i];
+        if (w.status == W_SURFACE) {
+            p.x[i] = it.x0 + w.s * (nx - it.x0);
+            p.y[i] = it.y0 + w.s * (ny - it.y0);
+            p.z[i] = it.z0 + w.s * (nz - it.z0);
+            atomicAdd(tri_count + w.tri, 1u);
+            p.idf[i] = idf | kSettled;
+            settled++;
+        } else if (w.status != W_INSIDE) {
+            p.idf[i] = idf | kLost;
+            lost++;
+            if (w.status == W_CAP) capped++;
+        }
+        if (w.tet != t) p.tet[i] = w.tet;
+    }
+    const unsigned long long a0 = __reduce_add_sync(kFull, cross), a1 = __reduce_add_sync(kFull, settled);
+    const unsigned long long a2 = __reduce_add_sync(kFull, lost), a3 = __reduce_add_sync(kFull, capped);
+    if ((threadIdx.x & 31) == 0) {
+        if (a0) atomicAdd(&ctr->crossings, a0);
+        if (a1) atomicAdd(&ctr->settled, a1);
+        if (a2) atomicAdd(&ctr->lost, a2);
+        if (a3) atomicAdd(&ctr->capped, a3);
+    }
+}
+
+// round(x * 2^k) for |x| < 2 and k <= 52 with integer ops only (round half
+// away from zero on the magnitude).
+__device__ __forceinline__ long long fix_round(double x, int k) {
+    const long long b = __double_as_longlong(x);
+    const int e = int((b >> 52) & 0x7ff);
+    if (e == 0) return 0;
+    const long long mant = (b & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+    const int sh = 1075 - e - k;
+    long long r;
+    if (sh <= 0)
+        r = mant << (-sh);
+    else if (sh > 62)
+        r = 0;
+    else
+        r = (mant + (1LL << (sh - 1))) >> sh;
+    return b < 0 ? -r : r;
+}
+
+// P1 deposit in fixed point: each alive particle adds round(lambda_i 2^k) for
+// i = 1..3 and 2^k minus their sum for lambda_0, so its four node shares are
+// exactly 2^k and charge is conserved exactly. Integer sums do not depend on
+// summation order, so the result is the same for any particle order, grid
+// or atomic interleaving. Lanes of a warp hold consecutive (tet-sorted)
+// particles; runs of equal tet are summed with a segmented shuffle scan and
+// the last lane of each run issues the four atomics.
+__global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, MeshDev m, int k,
+                                                   unsigned long long *__restrict__ node_fix) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     int key = -1;
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    long long v[4] = {0, 0, 0, 0};
     if (i < n && !(p.idf[i] & kDead)) {
         key = p.tet[i];
         TetGeo g;
-        load_geo(m.rec, key, g, nullptr);
-        double l[4];
-        bary(g, p.x[i], p.y[i], p.z[i], l);
-        v[0] = wq * l[0];
-        v[1] = wq * l[1];
-        v[2] = wq * l[2];
-        v[3] = wq * l[3];
+        load_geo(m.rec, key, g);
+        const double d0 = p.x[i] - g.x0[0], d1 = p.y[i] - g.x0[1], d2 = p.z[i] - g.x0[2];
+        const double l1 = g.M[0] * d0 + g.M[1] * d1 + g.M[2] * d2;
+        const double l2 = g.M[3] * d0 + g.M[4] * d1 + g.M[5] * d2;
+        const double l3 = g.M[6] * d0 + g.M[7] * d1 + g.M[8] * d2;
+        v[1] = fix_round(l1, k);
+        v[2] = fix_round(l2, k);
+        v[3] = fix_round(l3, k);
+        v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
     const int prev = __shfl_up_sync(kFull, key, 1);
     const bool head = lane == 0 || prev != key;
     const unsigned heads = __ballot_sync(kFull, head);
-    const unsigned le = kFull >> (31 - lane);
-    const int start = 31 - __clz(heads & le);
+    if (heads != 1u) {
+        const unsigned le = kFull >> (31 - lane);
+        const int start = 31 - __clz(heads & le);
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
+        for (int off = 1; off < 32; off <<= 1) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const double up = __shfl_up_sync(kFull, v[k], off);
-            if (lane - off >= start) v[k] += up;
+            for (int q = 0; q < 4; ++q) {
+                const long long up = __shfl_up_sync(kFull, v[q], off);
+                if (lane - off >= start) v[q] += up;
+            }
+        }
+    } else {  // one run covers the warp: butterfly sum, every lane holds it
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(kFull, v[q], off);
         }
     }
     const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
     if (tail && key >= 0) {
         const int4 tn = __ldg(m.tet_nodes + key);
-        atomicAdd(node_q + tn.x, v[0]);
-        atomicAdd(node_q + tn.y, v[1]);
-        atomicAdd(node_q + tn.z, v[2]);
-        atomicAdd(node_q + tn.w, v[3]);
+        atomicAdd(node_fix + tn.x, (unsigned long long)v[0]);
+        atomicAdd(node_fix + tn.y, (unsigned long long)v[1]);
+        atomicAdd(node_fix + tn.z, (unsigned long long)v[2]);
+        atomicAdd(node_fix + tn.w, (unsigned long long)v[3]);
     }
 }
 
-// E per tet: E = -sum_i phi_i grad(lambda_i) = -sum_r (phi_{r+1} - phi_0) M_r.
+__global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix, double scale,
+                                double *__restrict__ node_q, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    node_q[i] = double((long long)node_fix[i]) * scale;
+}
+
+// E per tet: E = -sum_i phi_i grad(lambda_i) = -sum_r (phi_{r+1} - phi_0) M_r
 // (VolumetricMesh::computeElectricFields, VolumetricMesh.cpp:382-411, with the
-// sign and scale of E = -grad(phi).)
-__global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, const double *__restrict__ phi) {
+// sign and scale of E = -grad(phi)), plus the push increment
+// H = ((q E / m) dt) / 2, the operations of Particle::electroMagneticPush.
+__global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, double *__restrict__ efield,
+                           const double *__restrict__ phi, double charge, double mass, double dt) {
     const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= m.n_tets) return;
     const int4 tn = __ldg(m.tet_nodes + t);
@@ -334,9 +509,32 @@ __global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, const double *__
     double E[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
-    r.E[0] = E[0];
-    r.E[1] = E[1];
-    r.E[2] = E[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        efield[3 * t + k] = E[k];
+        const double a = (charge * E[k]) / mass;
+        r.H[k] = (a * dt) / 2.0;
+    }
+    r.ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
+}
+
+__global__ void k_zero_efield(TetRec *__restrict__ rec, double *__restrict__ efield, int64_t n) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    rec[t].H[0] = 0.0;
+    rec[t].H[1] = 0.0;
+    rec[t].H[2] = 0.0;
+    rec[t].ezero = 1u;
+    efield[3 * t] = 0.0;
+    efield[3 * t + 1] = 0.0;
+    efield[3 * t + 2] = 0.0;
+}
+
+__global__ void k_count_lost(const int32_t *__restrict__ tet, int64_t n, unsigned long long *out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const unsigned v = (i < n && tet[i] < 0) ? 1u : 0u;
+    const unsigned s = __reduce_add_sync(kFull, v);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, (unsigned long long)s);
 }
 
 // Point location: walk from the centroid of the voxel's seed tet to p.
@@ -346,7 +544,7 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t n, MeshDev m, c
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
-    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) {
+    if (!(finite_bits(px) && finite_bits(py) && finite_bits(pz))) {
         tet_out[i] = -1;
         return;
     }
@@ -361,7 +559,7 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t n, MeshDev m, c
         c[k] = 0.25 * (((m.node_xyz[3 * tn.x + k] + m.node_xyz[3 * tn.y + k]) + m.node_xyz[3 * tn.z + k]) +
                        m.node_xyz[3 * tn.w + k]);
     TetGeo g;
-    load_geo(m.rec, seed, g, nullptr);
+    load_geo(m.rec, seed, g);
     const WalkOut w = walk64(m, seed, g, c[0], c[1], c[2], px, py, pz, max_cross, false);
     tet_out[i] = w.status == W_INSIDE ? w.tet : -1;
 }
@@ -411,9 +609,10 @@ __device__ __forceinline__ int sort_key(const DevParticles &p, int64_t i, int n_
     return (p.idf[i] & kDead) ? n_tets : p.tet[i];
 }
 
-__global__ void k_sort_hist(DevParticles p, int64_t n, int n_tets, int32_t *__restrict__ cnt) {
+__global__ void k_sort_hist(const int32_t *__restrict__ tet, const uint32_t *__restrict__ idf, int64_t n, int n_tets,
+                            int32_t *__restrict__ cnt) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int key = i < n ? sort_key(p, i, n_tets) : -1;
+    const int key = i < n ? ((idf[i] & kDead) ? n_tets : tet[i]) : -1;
     const unsigned peers = __match_any_sync(kFull, key);
     const int lane = threadIdx.x & 31;
     if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(cnt + key, __popc(peers));
@@ -437,7 +636,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile(int32_t *__restrict_
         v[k] = run;
         run += x;
     }
-    // exclusive scan of per-thread runs across the block
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int32_t incl = run;
 #pragma unroll
@@ -541,19 +739,36 @@ inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1)
 }  // namespace
 
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c, unsigned int *tri_count,
-                   DevCounters *ctr, cudaStream_t s) {
+                   WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s) {
     if (n <= 0) return;
-    k_step64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, c, tri_count, ctr);
+    cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
+    k_step64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, c, wq, wq_n, ctr);
+    k_walk_queue64<<<152 * 8, 128, 0, s>>>(p, m, c.max_cross, wq, wq_n, tri_count, ctr);
 }
 
-void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, double wq, double *node_q,
+void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,
                       cudaStream_t s) {
     if (n <= 0) return;
-    k_deposit64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, wq, node_q);
+    k_deposit64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, k, node_fix);
 }
 
-void launch_efield64(const MeshDev &m, TetRec *rec, const double *phi, cudaStream_t s) {
-    k_efield64<<<grid_for(m.n_tets, 256), 256, 0, s>>>(m, rec, phi);
+void launch_fix_to_charge(const unsigned long long *node_fix, double scale, double *node_q, int64_t n,
+                          cudaStream_t s) {
+    k_fix_to_charge<<<grid_for(n, 256), 256, 0, s>>>(node_fix, scale, node_q, n);
+}
+
+void launch_efield64(const MeshDev &m, TetRec *rec, double *efield, const double *phi, double charge, double mass,
+                     double dt, cudaStream_t s) {
+    k_efield64<<<grid_for(m.n_tets, 256), 256, 0, s>>>(m, rec, efield, phi, charge, mass, dt);
+}
+
+void launch_zero_efield(TetRec *rec, double *efield, int64_t n_tets, cudaStream_t s) {
+    k_zero_efield<<<grid_for(n_tets, 256), 256, 0, s>>>(rec, efield, n_tets);
+}
+
+void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_count_lost<<<grid_for(n, 256), 256, 0, s>>>(tet, n, out);
 }
 
 void launch_locate(const double *pos, int64_t n, const MeshDev &m, const int32_t *vox_seed,
@@ -586,47 +801,27 @@ unsigned long long *sort_occupied_counter(int32_t *scratch) {
     return reinterpret_cast<unsigned long long *>(scratch);
 }
 
-void launch_resort(const DevParticles &src, DevParticles dst, int64_t n, int64_t n_tets, int32_t *scratch,
-                   int64_t *n_alive_dev, cudaStream_t s) {
+int32_t *sort_offsets(int32_t *scratch) { return scratch + 2; }
+
+void launch_sort_prepare(const int32_t *tet, const uint32_t *idf, int64_t n, int64_t n_tets, int32_t *scratch,
+                         int64_t *n_alive_dev, cudaStream_t s) {
     const int64_t len = n_tets + 1;
     const int64_t nb = (len + kScanTile - 1) / kScanTile;
     unsigned long long *occupied = sort_occupied_counter(scratch);
-    int32_t *cnt = scratch + 2;
+    int32_t *cnt = sort_offsets(scratch);
     int32_t *sums = cnt + len;
     cudaMemsetAsync(cnt, 0, sizeof(int32_t) * len, s);
     cudaMemsetAsync(occupied, 0, sizeof(unsigned long long), s);
-    if (n > 0) k_sort_hist<<<grid_for(n, 256), 256, 0, s>>>(src, n, int(n_tets), cnt);
+    if (n > 0) k_sort_hist<<<grid_for(n, 256), 256, 0, s>>>(tet, idf, n, int(n_tets), cnt);
     k_scan_tile<<<unsigned(nb), kScanThreads, 0, s>>>(cnt, len, int(n_tets), sums, occupied);
     k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
     k_scan_add<<<grid_for(len, 256), 256, 0, s>>>(cnt, len, sums, int(n_tets), n_alive_dev);
-    if (n > 0) k_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, int(n_tets), cnt);
 }
 
-}  // namespace spg
-
-namespace spg {
-namespace {
-__global__ void k_zero_efield(TetRec *__restrict__ rec, int64_t n) {
-    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    rec[t].E[0] = 0.0;
-    rec[t].E[1] = 0.0;
-    rec[t].E[2] = 0.0;
-}
-__global__ void k_count_lost(const int32_t *__restrict__ tet, int64_t n, unsigned long long *out) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const unsigned v = (i < n && tet[i] < 0) ? 1u : 0u;
-    const unsigned s = __reduce_add_sync(0xffffffffu, v);
-    if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, (unsigned long long)s);
-}
-}  // namespace
-
-void launch_zero_efield(TetRec *rec, int64_t n_tets, cudaStream_t s) {
-    k_zero_efield<<<unsigned((n_tets + 255) / 256), 256, 0, s>>>(rec, n_tets);
+void launch_resort(const DevParticles &src, DevParticles dst, int64_t n, int64_t n_tets, int32_t *scratch,
+                   int64_t *n_alive_dev, cudaStream_t s) {
+    launch_sort_prepare(src.tet, src.idf, n, n_tets, scratch, n_alive_dev, s);
+    if (n > 0) k_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, int(n_tets), sort_offsets(scratch));
 }
 
-void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, cudaStream_t s) {
-    if (n <= 0) return;
-    k_count_lost<<<unsigned((n + 255) / 256), 256, 0, s>>>(tet, n, out);
-}
 }  // namespace spg

@@ -20,14 +20,18 @@ constexpr uint32_t kLost = 1u << 29;
 constexpr uint32_t kDead = kSettled | kLost;
 constexpr int64_t kMaxParticles = int64_t(kIdMask) + 1;
 
-// Per-tet record read by the push and the walk: barycentric map and E.
-// lambda_{1..3}(p) = M * (p - x0), lambda_0 = 1 - lambda_1 - lambda_2 - lambda_3.
-// Row r of M is grad(lambda_{r+1}); E = -sum_i phi_i grad(lambda_i).
+// Per-tet record read by the push and the walk: barycentric map and the
+// push increment. lambda_{1..3}(p) = M * (p - x0), lambda_0 = 1 - sum.
+// Row r of M is grad(lambda_{r+1}). H = ((q E / m) dt) / 2 per component is
+// the Boris half-step velocity increment for B = 0, computed once per tet
+// after each solve with the same operations the per-particle formula uses;
+// ezero = 1 when E is exactly zero (the reference then skips the push).
 struct alignas(128) TetRec {
     double M[9];
     double x0[3];
-    double E[3];
-    double pad;
+    double H[3];
+    uint32_t ezero;
+    uint32_t pad;
 };
 static_assert(sizeof(TetRec) == 128, "TetRec must be one 128-byte line");
 
@@ -60,6 +64,16 @@ struct HostMesh {
     std::vector<int32_t> vox_seed;
 };
 
+// Order-preserving map of a double to int64: a < b <=> key(a) < key(b) for
+// non-NaN values, with -0 and +0 mapped to the same key.
+inline long long order_key_host(double x) {
+    long long b;
+    static_assert(sizeof(b) == sizeof(x), "");
+    __builtin_memcpy(&b, &x, sizeof(b));
+    if (b == (long long)0x8000000000000000ULL) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
 // Returns SPG_OK or SPG_E_BAD_MESH / SPG_E_INVALID with a message in err.
 int prepare_mesh(const spg_mesh_desc &desc, double bbox_expansion, HostMesh &out, std::string &err);
 
@@ -87,6 +101,12 @@ struct StepConst {
     double dt, q_over_m, charge, mass;
     double vmin;
     double lo[3], hi[3];
+    // order-preserving integer keys of lo/hi (exact bbox test without FP64 compares)
+    long long lo_key[3], hi_key[3];
+    // bit pattern of 2*vmin: |v_k| above it means |v| >= vmin for certain
+    long long two_vmin_bits;
+    // FP32 screen of the collision probability: P ~= kp * (v^2)^pexp
+    float kp_f, pexp_f;
     int32_t model;
     int32_t max_cross;
     // collisions
@@ -109,16 +129,30 @@ struct MeshDev {
     int64_t n_tets, n_nodes;
 };
 
+// A particle whose move needs the exact tet walk: its index and start point.
+struct WalkItem {
+    int32_t i;
+    int32_t pad;
+    double x0, y0, z0;
+};
+
 // Kernel launchers (kernels_particles.cu).
+// Step kernel plus the exact walk of the queued particles (wq holds up to n items).
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c,
-                   unsigned int *tri_count, DevCounters *ctr, cudaStream_t s);
-void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, double wq, double *node_q,
+                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s);
+// Fixed-point P1 deposit: node_fix[n] += round(lambda_n * 2^k) per alive
+// particle (lambda_0 takes the remainder so each particle adds exactly 2^k).
+void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,
                       cudaStream_t s);
-void launch_efield64(const MeshDev &m, TetRec *rec, const double *phi, cudaStream_t s);
+// node_q = node_fix * scale
+void launch_fix_to_charge(const unsigned long long *node_fix, double scale, double *node_q, int64_t n,
+                          cudaStream_t s);
+void launch_efield64(const MeshDev &m, TetRec *rec, double *efield, const double *phi, double charge, double mass,
+                     double dt, cudaStream_t s);
 void launch_locate(const double *pos, int64_t n, const MeshDev &m, const int32_t *vox_seed,
                    const double *vox_origin_inv, const int32_t *vox_dims, int max_cross,
                    int32_t *tet_out, cudaStream_t s);
-void launch_zero_efield(TetRec *rec, int64_t n_tets, cudaStream_t s);
+void launch_zero_efield(TetRec *rec, double *efield, int64_t n_tets, cudaStream_t s);
 void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, cudaStream_t s);
 void launch_init_particles(const double *pos, const double *vel, const int32_t *tet, int64_t n,
                            DevParticles p, cudaStream_t s);
@@ -131,6 +165,53 @@ int64_t sort_scratch_words(int64_t n_tets);
 unsigned long long *sort_occupied_counter(int32_t *scratch);
 void launch_resort(const DevParticles &src, DevParticles dst, int64_t n, int64_t n_tets, int32_t *scratch,
                    int64_t *n_alive_dev, cudaStream_t s);
+// Histogram + exclusive scan of the sort keys; sort_offsets(scratch) then
+// holds the first slot of every key (tets, then n_tets for dead particles).
+void launch_sort_prepare(const int32_t *tet, const uint32_t *idf, int64_t n, int64_t n_tets, int32_t *scratch,
+                         int64_t *n_alive_dev, cudaStream_t s);
+int32_t *sort_offsets(int32_t *scratch);
+
+// ---------------------------------------------------------- mixed precision
+// Per-tet record of the mixed form (64 B): FP32 barycentric map about the
+// centroid, lambda_{1..3} = 1/4 + M (x - c); FP32 push increment; FP32
+// centroid (modelling-box test only); E-null flag.
+struct alignas(64) TetRec32 {
+    float M[9];
+    float H[3];
+    float cen[3];
+    uint32_t ezero;
+};
+static_assert(sizeof(TetRec32) == 64, "TetRec32 must be 64 bytes");
+
+// 32 B per particle: position relative to the owning tet's centroid.
+struct DevParticles32 {
+    float *x, *y, *z, *vx, *vy, *vz;
+    int32_t *tet;
+    uint32_t *idf;
+};
+
+struct MeshDev32 {
+    const TetRec32 *rec;
+    const TetRec *rec64;  // FP64 map for near-zero barycentric tests
+    const double *cen;    // FP64 centroids, 3 per tet
+    const int4 *nbr, *ftri, *tet_nodes;
+    int64_t n_tets;
+};
+
+// kernels_mixed.cu
+void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c,
+                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s);
+void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
+                      cudaStream_t s);
+void launch_push32(TetRec32 *rec, const double *efield, int64_t n_tets, double charge, double mass, double dt,
+                   cudaStream_t s);
+void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
+                     DevParticles32 p, cudaStream_t s);
+void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,
+                     uint32_t *flags, cudaStream_t s);
+void launch_resort32(const DevParticles32 &src, DevParticles32 dst, int64_t n, int64_t n_tets, int32_t *scratch,
+                     int64_t *n_alive_dev, cudaStream_t s);
+size_t walk_item32_bytes();
 
 // PCG (kernels_pcg.cu).
 // tol2 is set to rtol^2 by the host and scaled by ||b||^2 in the setup kernel.
@@ -144,12 +225,33 @@ struct PcgDev {
     int64_t n;
     const int32_t *row_ptr, *col;
     const double *val, *inv_diag;
+    const int64_t *slice_ptr;  // SELL-32: n_slices + 1 offsets
+    const int32_t *scol;
+    const double *sval;
     double *x, *r, *z, *p, *p2, *q;
     double *partials;  // 3 doubles per block
     PcgScalars *sc;
     int blocks;
 };
+struct PcgDev32 {
+    int64_t n;
+    const int64_t *slice_ptr;
+    const int32_t *scol;
+    const float *sval;
+    const float *inv_diag;
+    float *e, *r, *z, *p, *q;
+    double *partials;  // 3 doubles per block (separate from the FP64 solver's)
+    PcgScalars *sc;
+    int blocks;
+};
 int pcg_blocks(int64_t n);
+// Mixed-precision solve pieces (kernels_pcg.cu).
+void launch_refine_setup(const PcgDev &d, const PcgDev32 &f, const double *b, cudaStream_t s);
+void launch_pcg32_iteration(PcgDev32 &f, cudaStream_t s);
+void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s);
+// CSR -> SELL-32 (slices of 32 rows, column-major, zero padding).
+void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val,
+                  std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
                     const double *dir_value, double *b, int64_t n, cudaStream_t s);

@@ -1,0 +1,133 @@
+"""Mixed-precision form (FP32 tet-local state, FP32 push, FP32-SpMV PCG in
+FP64 refinement) against the FP64 oracle.
+
+Bars (from the benchmark configuration of the mixed form):
+  * L1 error of the surface-deposition histogram over triangles <= 1 %;
+  * landing-position RMS error and nodal potential max error reported and
+    bounded (1e-6 of the box size, 1e-6 of max |phi|);
+  * the FP64 refinement reaches a 1e-10 relative residual.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _w0(n=10000, steps=200, collisions=False, **kw):
+    from start_gb300.workloads import workload0
+
+    w = workload0(n_particles=n, collisions=collisions, steps=steps)
+    w.params.update(kw)
+    return w
+
+
+def _pair(w):
+    import oracle
+    from start_gb300 import StartPIC
+
+    g = StartPIC(w.mesh, dict(w.params, precision=1))
+    o = oracle.Oracle(w.mesh, w.params)
+    for e in (g, o):
+        e.set_particles(w.pos, w.vel)
+    return g, o
+
+
+def test_mixed_roundtrip_state(built):
+    """Global -> tet-local FP32 -> global keeps positions to FP32 resolution
+    of the local offset and every tet id."""
+    w = _w0(n=5000)
+    g, o = _pair(w)
+    pg, po = g.particles(), o.particles()
+    assert np.array_equal(pg["tet"], po["tet"])
+    assert np.max(np.abs(pg["pos"] - w.pos)) <= 1e-9  # |x - c| < 1 cm, FP32 ulp < 1e-9 m
+    assert np.max(np.abs(pg["vel"] - w.vel) / np.abs(w.vel).max()) <= 1e-7
+
+
+def test_mixed_solve_reaches_1e10(built):
+    w = _w0(n=20000, cg_rtol=1e-10)
+    g, o = _pair(w)
+    for e in (g, o):
+        e.gather(want_rho=False)
+    pg, itg, rrg = g.solve()
+    po, ito, rro = o.solve()
+    assert rrg <= 1e-10
+    assert np.max(np.abs(pg - po)) <= 1e-6 * np.max(np.abs(po))
+
+
+def test_mixed_deposit_close_to_fp64(built):
+    w = _w0(n=20000)
+    g, o = _pair(w)
+    rg, ro = g.gather(), o.gather()
+    assert np.max(np.abs(rg - ro)) <= 1e-6 * np.max(np.abs(ro))
+    total = w.params["weight"] * w.params["charge"] * len(w.pos)
+    assert abs(np.dot(rg, o.dual_volumes()) - total) <= 1e-12 * total  # exact fixed-point conservation
+
+
+def test_mixed_vs_fp64_collisionless_run(built):
+    w = _w0(n=10000, steps=200)
+    g, o = _pair(w)
+    sg, so = g.run(w.steps), o.run(w.steps)
+    cg, co = g.triangle_counts().astype(float), o.triangle_counts().astype(float)
+    l1 = np.abs(cg - co).sum() / co.sum()
+    assert l1 <= 0.01, l1
+    pg, po = g.particles(), o.particles()
+    both = (pg["flags"] == 1) & (po["flags"] == 1)
+    assert both.mean() > 0.95
+    rms = np.sqrt(np.mean(np.sum((pg["pos"][both] - po["pos"][both]) ** 2, axis=1)))
+    assert rms <= 1e-6 * 0.1, rms
+    phg, pho = g.potential(), o.potential()
+    assert np.max(np.abs(phg - pho)) <= 1e-6 * np.max(np.abs(pho))
+    assert abs(sg["particle_steps"] - so["particle_steps"]) <= 0.01 * so["particle_steps"]
+
+
+def test_mixed_with_collisions_histogram(built):
+    from scipy import stats
+
+    w = _w0(n=10000, steps=200, collisions=True)
+    w.params["gas_concentration"] *= 200.0
+    g, o = _pair(w)
+    sg, so = g.run(w.steps), o.run(w.steps)
+    assert abs(sg["collisions"] - so["collisions"]) <= 0.05 * so["collisions"]
+    cen = w.mesh.triangle_centroids()
+    ij = np.floor(cen / 0.025).astype(int).clip(0, 3)
+    key = w.mesh.tri_tag * 100 + (ij * np.array([16, 4, 1])).sum(1)
+    _, inv = np.unique(key, return_inverse=True)
+    a = np.bincount(inv, weights=g.triangle_counts().astype(float))
+    b = np.bincount(inv, weights=o.triangle_counts().astype(float))
+    keep = (a + b) > 0
+    a, b = a[keep], b[keep]
+    k1, k2 = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    chi2 = np.sum((k1 * a - k2 * b) ** 2 / (a + b))
+    assert stats.chi2.sf(chi2, len(a) - 1) > 0.01
+
+
+def test_mixed_checkpoint_restore_is_exact(built):
+    from start_gb300 import StartPIC
+
+    w = _w0(n=5000, steps=80, collisions=True)
+    g = StartPIC(w.mesh, dict(w.params, precision=1))
+    g.set_particles(w.pos, w.vel)
+    g.run(40)
+    blob = g.checkpoint()
+    g.run(40)
+    a = g.particles()
+    g.restore(blob)
+    g.run(40)
+    b = g.particles()
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["tet"], b["tet"])
+
+
+def test_mixed_resort_invariance(built):
+    from start_gb300 import StartPIC
+
+    res = []
+    for every in (0, 3):
+        w = _w0(n=6000, steps=60)
+        w.params["resort_every"] = every
+        g = StartPIC(w.mesh, dict(w.params, precision=1))
+        g.set_particles(w.pos, w.vel)
+        g.run(60)
+        res.append((g.particles(), g.triangle_counts()))
+    (pa, ca), (pb, cb) = res
+    assert np.array_equal(pa["tet"], pb["tet"]) and np.array_equal(ca, cb)
+    assert np.array_equal(pa["pos"], pb["pos"])
