@@ -230,6 +230,7 @@ def run_gpu(args):
     st1 = eng.stats()
     prof = eng.profile()
     eng.profile_enable(False)
+    counts_fp64 = eng.triangle_counts()  # after W + K steps, for the mixed-form L1 comparison
     ps = st1["particle_steps"] - st0["particle_steps"]
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -297,6 +298,44 @@ def run_gpu(args):
                "sample": f"{min(args.cpu_sample, len(w.pos))} of {len(w.pos)} particles, {args.cpu_steps} "
                          f"full-loop steps on the full mesh (one warm PCG solve)", "timed_s": info["timed_s"]}
     eng.close()
+
+    mixed = None
+    if not args.no_mixed:
+        # The mixed-precision form on the same inputs and steps (BASELINE
+        # configuration 2): throughput and the L1 error of its surface
+        # histogram against the FP64 form after the same W + K steps.
+        wm = build_workload(args)
+        wm.params["device"] = local
+        wm.params["precision"] = 1
+        em = StartPIC(wm.mesh, wm.params)
+        em.set_particles(wm.pos, wm.vel)
+        sm_ = torch.cuda.ExternalStream(em.stream_ptr(), device=local)
+        em.run(args.warmup)
+        em.synchronize()
+        em.profile_enable(True)
+        m0 = em.stats()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(sm_)
+        em.run(args.steps, raise_on_nonconvergence=False)
+        e1.record(sm_)
+        e1.synchronize()
+        mms = e0.elapsed_time(e1)
+        m1 = em.stats()
+        mp = em.profile()
+        cm = em.triangle_counts().astype(float)
+        cf = counts_fp64.astype(float)
+        mval = (m1["particle_steps"] - m0["particle_steps"]) / (mms / 1e3)
+        mixed = {"value": mval, "unit": UNIT, "ms_per_step": mms / args.steps, "speedup_vs_fp64": mval / value,
+                 "l1_hist_error_vs_fp64": float(np.abs(cm - cf).sum() / max(cf.sum(), 1.0)),
+                 "settled_fp64": int(cf.sum()), "settled_mixed": int(cm.sum()),
+                 "breakdown_ms": {k: mp[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")},
+                 "pcg_iters": mp["pcg_iters"],
+                 "step_GBps": mp["step_bytes"] / (mp["step_ms"] / 1e3) / 1e9 if mp["step_ms"] > 0 else None,
+                 "pcg_GBps": mp["pcg_bytes"] / (mp["pcg_ms"] / 1e3) / 1e9 if mp["pcg_ms"] > 0 else None,
+                 "gpu_launches": mp["kernel_launches"], "dtype": "f32 state/push/SpMV, f64 refinement + sums"}
+        em.close()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -304,7 +343,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded workload generator)", "config": config_dict(args, w),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown,
+            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown, "mixed": mixed,
             "alive_particles": {"start": st0["n_alive"], "end": st1["n_alive"]},
             "cg_iters_last": st1["cg_iters_last"],
         }
@@ -327,6 +366,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the step kernel, if captured")
     args = ap.parse_args()

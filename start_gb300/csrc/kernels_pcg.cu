@@ -232,11 +232,14 @@ __device__ __forceinline__ float warp_sumf(float v) {
     return v;
 }
 
-// FP64 block reduction of FP32 warp partials (lane 0 of each warp holds one).
+// FP64 block reduction of FP32 per-thread partials: each warp sums in FP32
+// (the total lands in lane 0), only lane 0 passes it on, and everything from
+// there on is FP64.
 __device__ bool block_reduce2_w(float a, float b, double *partials, PcgScalars *sc, double tot[2]) {
     a = warp_sumf(a);
     b = warp_sumf(b);
-    return block_reduce2(double(a), double(b), partials, sc, tot);
+    const bool lead = (threadIdx.x & 31) == 0;
+    return block_reduce2(lead ? double(a) : 0.0, lead ? double(b) : 0.0, partials, sc, tot);
 }
 
 // Outer step: r = b - A x in FP64, rr = r.r, bb = b.b; start the inner solve:
@@ -351,9 +354,12 @@ __global__ void k_refine_apply(double *__restrict__ x, const float *__restrict__
 
 }  // namespace
 
+// Four 256-thread blocks per SM: each thread then handles several rows, so
+// the FP64 shuffle reductions of the dot products (which issue per warp at
+// the FP64 rate) are amortised over several rows.
 int pcg_blocks(int64_t n) {
     const int64_t want = (n + kThreads - 1) / kThreads;
-    return int(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
+    return int(want < 152 * 4 ? (want < 1 ? 1 : want) : 152 * 4);
 }
 
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,

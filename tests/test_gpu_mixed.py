@@ -52,6 +52,8 @@ def test_mixed_solve_reaches_1e10(built):
     po, ito, rro = o.solve()
     assert rrg <= 1e-10
     assert np.max(np.abs(pg - po)) <= 1e-6 * np.max(np.abs(po))
+    # FP32 corrections converge like FP64 CG (kappa * eps32 << 1 per refinement)
+    assert itg <= 2 * ito + 50, (itg, ito)
 
 
 def test_mixed_deposit_close_to_fp64(built):
