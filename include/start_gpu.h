@@ -200,6 +200,33 @@ int spg_profile_enable(spg_handle *h, int32_t on);
 int spg_get_profile(spg_handle *h, spg_profile *prof);
 int spg_profile_reset(spg_handle *h);
 
+/* Jacobi-preconditioned CG on a caller-provided CSR matrix that allocates
+ * nothing. It has no counterpart in the reference: it exists for callers that
+ * must not call cudaMalloc/cudaFree. That covers a program whose device memory
+ * is all owned by its own pool (a PyTorch caching allocator, a fixed arena),
+ * and a loop that must not take the device synchronisation an allocation can
+ * imply.
+ *
+ * row_ptr [n+1], col [nnz], val [nnz], b [n] and x [n] are DEVICE pointers the
+ * caller allocated; x holds the initial guess and receives the solution. The
+ * stop rule is the one spg_solve uses: ||b - A x||_2 <= rtol ||b||_2, or
+ * max_iter iterations (SPG_E_NOT_CONVERGED, x keeps the last iterate).
+ * stream is a cudaStream_t, or NULL for the default stream.
+ *
+ * Limit: n <= 131072 rows. Larger n returns SPG_E_INVALID without touching
+ * the GPU. The working vectors live in one static device array of about
+ * 5.3 MB that every GPU loading the library keeps until the process exits.
+ * All calls on a device share it. Calls that overlap on the GPU (several
+ * streams, several host threads) race on it and must be serialised by the
+ * caller. Each call resets the parts that must start at zero.
+ *
+ * The first call on each device looks up the array's device address with
+ * that device current. Make that first call before any stream capture. Error
+ * messages: spg_last_error(NULL) on the calling thread. */
+int spg_pcg_solve_noalloc(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val,
+                          const double *b, double *x, double rtol, int32_t max_iter, void *stream,
+                          int32_t *iters, double *relres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,8 @@ SIGNATURES = {
     "spg_profile_enable": (C.c_int, [_H, C.c_int32]),
     "spg_get_profile": (C.c_int, [_H, C.POINTER(Profile)]),
     "spg_profile_reset": (C.c_int, [_H]),
+    "spg_pcg_solve_noalloc": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_double, C.c_int32, C.c_void_p, _pi32, _pd]),
 }
 
 _lib = None

@@ -42,6 +42,7 @@ def _sources():
         ("kernels_particles.cu", common_nv + ["--fmad=false"]),
         ("kernels_pcg.cu", common_nv),
         ("kernels_mixed.cu", common_nv),
+        ("noalloc.cu", common_nv),
         ("mesh_prep.cpp", common_cc + ["-fopenmp"]),
         ("capi.cpp", common_cc),
     ]

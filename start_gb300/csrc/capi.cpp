@@ -40,6 +40,10 @@ struct EventSeries {
 
 }  // namespace
 
+namespace spg {
+void set_thread_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace spg
+
 struct spg_handle {
     spg_params prm{};
     int device = 0;

@@ -74,6 +74,9 @@ inline long long order_key_host(double x) {
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
+// Message returned by spg_last_error(NULL) on the calling thread.
+void set_thread_error(const std::string &msg);
+
 // Returns SPG_OK or SPG_E_BAD_MESH / SPG_E_INVALID with a message in err.
 int prepare_mesh(const spg_mesh_desc &desc, double bbox_expansion, HostMesh &out, std::string &err);
 
