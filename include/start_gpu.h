@@ -193,6 +193,26 @@ int spg_checkpoint_size(spg_handle *h, size_t *bytes);
 int spg_checkpoint(spg_handle *h, void *buf, size_t bytes);
 int spg_restore(spg_handle *h, const void *buf, size_t bytes);
 
+/* Dirichlet values: g [n_nodes], read at the Dirichlet nodes of the mesh.
+ * Updates the lifting of the right-hand side; the next spg_solve uses them.
+ * (The reference sets them once from its config, MatrixBoundaryConditionsManager.) */
+int spg_set_dirichlet(spg_handle *h, const double *g);
+
+/* Gradient of a smoothed landing objective through the particle steps (FP64
+ * form; collisions none/HS/VHS with their events and random numbers held
+ * fixed). spg_grad_forward runs nsteps particle steps in the current field
+ * (no deposit or solve), keeping the particle state every checkpoint_every
+ * steps and where each particle lands, and returns
+ *   J = (1/N) sum over the N particles that landed of exp(-|r - target|^2 / (2 sigma^2)).
+ * spg_grad_backward recomputes each checkpoint window, runs the adjoint of
+ * push, move and frozen collisions, one adjoint CG on the stiffness matrix,
+ * and returns dJ/dg at the Dirichlet nodes (0 elsewhere) and, if non-NULL,
+ * dJ/d(initial position) and dJ/d(initial velocity) per particle [3n, id order].
+ * N is held constant. Tet crossings are piecewise constant and carry no gradient. */
+int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, const double target[3], double sigma,
+                     double *J, int64_t *n_landed);
+int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_dv0, int32_t *adj_cg_iters);
+
 int spg_synchronize(spg_handle *h);
 /* cudaStream_t of the handle, for callers that record their own events. */
 void *spg_stream(spg_handle *h);

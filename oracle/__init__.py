@@ -59,6 +59,9 @@ def load(path: str | Path | None = None):
         "spo_locate": (C.c_int, [_H, C.c_int64, _pd, _pi32]),
         "spo_get_matrix": (C.c_int, [_H, _pi32, _pi32, _pd, _pd]),
         "spo_get_dual_volumes": (C.c_int, [_H, _pd]),
+        "spo_set_dirichlet": (C.c_int, [_H, _pd]),
+        "spo_grad": (C.c_int, [_H, C.c_int32, _pd, C.c_double, _pd, C.POINTER(C.c_int64), _pd, _pd, _pd]),
+        "spo_grad_freeze": (C.c_int, [_H, C.c_int]),
         "spo_update_position": (None, [_pd, _pd, C.c_double]),
         "spo_segment_triangle": (C.c_int, [_pd, _pd, _pd, _pd, _pd, _pd]),
         "spo_gas_concentration": (C.c_double, [C.c_double, C.c_double]),
@@ -234,6 +237,27 @@ class Oracle:
         self.lib.spo_get_matrix(self.h, _ptr(rp, C.c_int32), _ptr(ci, C.c_int32), _ptr(av, C.c_double),
                                 _ptr(lift, C.c_double))
         return rp, ci, av, lift
+
+    def set_dirichlet(self, g):
+        g = np.ascontiguousarray(g, np.float64)
+        self.lib.spo_set_dirichlet(self.h, _ptr(g, C.c_double))
+
+    def grad(self, nsteps, target, sigma):
+        """FP64 reference gradient: (J, n_landed, dJ/dg, dJ/dx0, dJ/dv0)."""
+        t = np.ascontiguousarray(target, np.float64)
+        J, nl = C.c_double(), C.c_int64()
+        dg = np.zeros(self.n_nodes)
+        dx = np.zeros((self.n_particles, 3))
+        dv = np.zeros((self.n_particles, 3))
+        rc = self.lib.spo_grad(self.h, int(nsteps), _ptr(t, C.c_double), float(sigma), C.byref(J), C.byref(nl),
+                               _ptr(dg, C.c_double), _ptr(dx, C.c_double), _ptr(dv, C.c_double))
+        if rc:
+            raise RuntimeError(self.lib.spo_last_error().decode())
+        return J.value, nl.value, dg, dx, dv
+
+    def grad_freeze(self, mode):
+        """0 off, 1 record the field cells of the next grad(), 2 replay them."""
+        self.lib.spo_grad_freeze(self.h, int(mode))
 
     def dual_volumes(self):
         dv = np.empty(self.n_nodes)

@@ -133,6 +133,7 @@ struct spo_handle {
     // stiffness after symmetric Dirichlet elimination
     std::vector<int32_t> rp, ci;
     std::vector<double> av, diag, lift, gval;
+    std::vector<std::map<int32_t, double>> elim;  // free row -> (Dirichlet col -> K_fd)
     std::vector<uint8_t> isd;
     double lo[3], hi[3];
     // location grid (tet bounding boxes)
@@ -154,6 +155,9 @@ struct spo_handle {
     int32_t cg_iters_last = 0, cg_solves = 0;
     double cg_relres_last = 0.0;
     bool have_E = false;
+    // field-cell freezing for spo_grad (0 off, 1 record, 2 replay)
+    int freeze = 0;
+    std::vector<int32_t> frozen;
 };
 
 namespace {
@@ -167,6 +171,7 @@ struct Walk {
     int32_t tri;
     int crossings;
     double s;
+    int face;  // exit face of the final tet when the walk stops on a surface
 };
 
 // The segment p0 -> p1 from tet t: stop when lambda(p1) >= 0 in all four
@@ -174,7 +179,7 @@ struct Walk {
 // lambda(p1) < 0 and the smallest crossing parameter l0/(l0 - l1), the
 // lowest face index winning ties.
 Walk walk(const spo_handle &h, int32_t t, const double p0[3], const double p1[3], int max_cross, bool stop_surface) {
-    Walk w{t, W_IN, -1, 0, 1.0};
+    Walk w{t, W_IN, -1, 0, 1.0, -1};
     int enter = -1;
     for (;;) {
         const Tet &T = h.tet[t];
@@ -208,6 +213,7 @@ Walk walk(const spo_handle &h, int32_t t, const double p0[3], const double p1[3]
             w.status = W_SURF;
             w.tri = tri;
             w.s = sb;
+            w.face = best;
             return w;
         }
         const int32_t nb = h.nbr_t[4 * int64_t(t) + best];
@@ -296,7 +302,7 @@ struct StepOut {
     int processed, coll, cross, settled, lost;
 };
 
-StepOut step_particle(spo_handle &h, const CollConst &cc, int64_t i) {
+StepOut step_particle(spo_handle &h, const CollConst &cc, int64_t i, int32_t ecell = -1) {
     StepOut o{0, 0, 0, 0, 0};
     if (h.fl[i] & (FLAG_SETTLED | FLAG_LOST)) return o;  // 1. settled
     o.processed = 1;
@@ -308,7 +314,7 @@ StepOut step_particle(spo_handle &h, const CollConst &cc, int64_t i) {
                         x[2] >= h.lo[2] && x[2] <= h.hi[2];
     if (!inside) return o;  // 3. outside the modelling space
     const int32_t t = h.pt[i];
-    const Tet &T = h.tet[t];
+    const Tet &T = h.tet[ecell >= 0 ? ecell : t];
     // 4. push: a = qE/m; v- = v + a dt/2; (rotation = identity for B = 0); v = v+ + a dt/2
     if (!(T.E[0] == 0.0 && T.E[1] == 0.0 && T.E[2] == 0.0)) {
         for (int k = 0; k < 3; ++k) {
@@ -638,6 +644,7 @@ int spo_create(const spg_mesh_desc *d, const spg_params *prm, spo_handle **out) 
     h->rp.assign(h->Nn + 1, 0);
     std::vector<std::map<int32_t, double>> rows(h->Nn);
     h->lift.assign(h->Nn, 0.0);
+    h->elim.assign(h->Nn, {});
     h->diag.assign(h->Nn, 1.0);
 #pragma omp parallel for schedule(dynamic, 512)
     for (int64_t i = 0; i < h->Nn; ++i) {
@@ -660,10 +667,12 @@ int spo_create(const spg_mesh_desc *d, const spg_params *prm, spo_handle **out) 
             for (int b = 0; b < 4; ++b) {
                 const double kab = h->vol[t] * (G[a][0] * G[b][0] + G[a][1] * G[b][1] + G[a][2] * G[b][2]);
                 const int32_t j = h->tn[4 * t + b];
-                if (h->isd[j])
+                if (h->isd[j]) {
                     lift += kab * h->gval[j];
-                else
+                    h->elim[i][j] += kab;
+                } else {
                     rows[i][j] += kab;
+                }
             }
         }
         h->lift[i] = lift;
@@ -895,6 +904,193 @@ int spo_get_matrix(spo_handle *h, int32_t *row_ptr, int32_t *col, double *val, d
 
 int spo_get_dual_volumes(spo_handle *h, double *dv) {
     std::copy(h->dual.begin(), h->dual.end(), dv);
+    return SPG_OK;
+}
+
+int spo_set_dirichlet(spo_handle *h, const double *g) {
+    for (int64_t i = 0; i < h->Nn; ++i)
+        if (h->isd[i]) {
+            h->gval[i] = g[i];
+            h->phi[i] = g[i];
+        }
+    for (int64_t i = 0; i < h->Nn; ++i) {
+        double s = 0.0;
+        for (const auto &e : h->elim[i]) s += e.second * h->gval[e.first];
+        h->lift[i] = s;
+    }
+    return SPG_OK;
+}
+
+// FP64 reference gradient of J = (1/N) sum_landed exp(-|r - t|^2/(2 s^2)):
+// the forward keeps every particle's full history (tet and velocity at the
+// start of each step), then the backward recursion of the particle adjoint,
+// dJ/dE -> dJ/dphi, one adjoint PCG and the transpose of the lifting.
+int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, double *J, int64_t *n_landed,
+             double *dJ_dg, double *dJ_dx0, double *dJ_dv0) {
+    const spg_params &p = h->prm;
+    if (p.collision_model == SPG_COLL_VSS) return fail(SPG_E_INVALID, "VSS has no adjoint");
+    const int64_t n = h->np;
+    std::vector<int32_t> htet(size_t(nsteps) * n);
+    std::vector<double> hv(size_t(nsteps) * n * 3);
+    std::vector<int32_t> land_step(n, -1), land_tet(n, -1), land_face(n, -1);
+    std::vector<double> land_s(n, 0.0);
+    const CollConst cc = coll_const(p);
+    const int64_t step0 = h->step;
+    const bool replay = h->freeze == 2 && h->frozen.size() == htet.size();
+    for (int32_t k = 0; k < nsteps; ++k) {
+        for (int64_t i = 0; i < n; ++i) {
+            const size_t o = size_t(k) * n + i;
+            const int32_t ec = replay && h->frozen[o] >= 0 ? h->frozen[o] : h->pt[i];
+            htet[o] = (h->fl[i] & (FLAG_SETTLED | FLAG_LOST)) ? -1 : ec;
+            for (int c = 0; c < 3; ++c) hv[3 * o + c] = h->v[3 * i + c];
+        }
+        // one step, remembering where a settle happened
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t i = 0; i < n; ++i) {
+            const uint32_t before = h->fl[i];
+            const int32_t t0 = h->pt[i];
+            double x0[3] = {h->x[3 * i], h->x[3 * i + 1], h->x[3 * i + 2]};
+            const int32_t ec = htet[size_t(k) * n + i];
+            step_particle(*h, cc, i, ec);
+            if (!(before & FLAG_SETTLED) && (h->fl[i] & FLAG_SETTLED)) {
+                // recompute the hit fraction and face of the settling walk
+                const Tet &T = h->tet[ec];
+                double vp[3];
+                for (int c = 0; c < 3; ++c) {
+                    const double a = (p.charge * T.E[c]) / p.mass;
+                    const double half = (a * p.dt) / 2.0;
+                    vp[c] = (T.E[0] == 0.0 && T.E[1] == 0.0 && T.E[2] == 0.0) ? hv[3 * (size_t(k) * n + i) + c]
+                                                                              : (hv[3 * (size_t(k) * n + i) + c] + half) + half;
+                }
+                const double p1[3] = {x0[0] + vp[0] * p.dt, x0[1] + vp[1] * p.dt, x0[2] + vp[2] * p.dt};
+                const Walk w = walk(*h, t0, x0, p1, p.max_crossings, true);
+                land_step[i] = k;
+                land_tet[i] = w.tet;
+                land_face[i] = w.face;
+                land_s[i] = w.s;
+            }
+        }
+        h->step++;
+    }
+    if (h->freeze == 1) h->frozen = htet;
+    // objective
+    const double inv2 = 1.0 / (2.0 * sigma * sigma);
+    double sum = 0.0;
+    int64_t cnt = 0;
+    std::vector<double> gr(3 * n, 0.0);
+    for (int64_t i = 0; i < n; ++i)
+        if (land_step[i] >= 0) {
+            const double dx = h->x[3 * i] - target[0], dy = h->x[3 * i + 1] - target[1], dz = h->x[3 * i + 2] - target[2];
+            const double g = std::exp(-(dx * dx + dy * dy + dz * dz) * inv2);
+            sum += g;
+            cnt++;
+            gr[3 * i] = -2.0 * inv2 * g * dx;
+            gr[3 * i + 1] = -2.0 * inv2 * g * dy;
+            gr[3 * i + 2] = -2.0 * inv2 * g * dz;
+        }
+    if (J) *J = cnt ? sum / double(cnt) : 0.0;
+    if (n_landed) *n_landed = cnt;
+    if (!cnt) return SPG_OK;
+    for (double &v : gr) v /= double(cnt);
+    // particle adjoint
+    std::vector<double> gE(3 * h->Nt, 0.0), ax(3 * n, 0.0), av(3 * n, 0.0);
+    const double cq = p.charge / p.mass * p.dt;
+    for (int64_t i = 0; i < n; ++i) {
+        const int N = land_step[i];
+        if (N < 0) continue;
+        double A[3] = {0, 0, 0}, V[3] = {0, 0, 0};
+        for (int k = N; k >= 0; --k) {
+            const size_t o = size_t(k) * n + i;
+            const int t = htet[o];
+            if (t < 0) continue;
+            const double *v = &hv[3 * o];
+            if (std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) < p.min_velocity) continue;
+            const Tet &T = h->tet[t];
+            double va[3];
+            const bool ez = T.E[0] == 0.0 && T.E[1] == 0.0 && T.E[2] == 0.0;
+            for (int c = 0; c < 3; ++c) {
+                const double a = (p.charge * T.E[c]) / p.mass;
+                const double half = (a * p.dt) / 2.0;
+                va[c] = ez ? v[c] : (v[c] + half) + half;
+            }
+            double b[3];
+            if (k == N) {
+                const Tet &TL = h->tet[land_tet[i]];
+                double nn[3];
+                const int f = land_face[i];
+                for (int c = 0; c < 3; ++c)
+                    nn[c] = f == 0 ? -(TL.M[c] + TL.M[3 + c] + TL.M[6 + c]) : TL.M[3 * (f - 1) + c];
+                const double nv = nn[0] * va[0] + nn[1] * va[1] + nn[2] * va[2];
+                const double *g = &gr[3 * i];
+                const double vg = (va[0] * g[0] + va[1] * g[1] + va[2] * g[2]) / nv;
+                for (int c = 0; c < 3; ++c) {
+                    A[c] = g[c] - nn[c] * vg;
+                    b[c] = land_s[i] * p.dt * A[c];
+                }
+            } else {
+                if (p.collision_model != SPG_COLL_NONE) {
+                    uint32_t r[4];
+                    draws(uint64_t(step0 + k), 0u, uint32_t(i), p.seed, r);
+                    if (u01(r[0], r[1]) < probability(p, cc, va)) {
+                        const double u1 = u01(r[2], r[3]);
+                        uint32_t r2[4];
+                        draws(uint64_t(step0 + k), 1u, uint32_t(i), p.seed, r2);
+                        const double u2 = u01(r2[0], r2[1]);
+                        const double xc = p.collision_model == SPG_COLL_HS ? -1.0 + 2.0 * u1 : u1;
+                        const double xs = std::sqrt(1.0 - xc * xc), ph = (2.0 * PI) * u2;
+                        const double nh[3] = {xs * std::cos(ph), xs * std::sin(ph), xc};
+                        const double vm = std::sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
+                        const double na = (nh[0] * V[0] + nh[1] * V[1] + nh[2] * V[2]) * cc.mass_ct / vm;
+                        for (int c = 0; c < 3; ++c) V[c] = cc.mass_cp * V[c] + na * va[c];
+                    }
+                }
+                for (int c = 0; c < 3; ++c) b[c] = V[c] + p.dt * A[c];
+            }
+            for (int c = 0; c < 3; ++c) {
+                gE[3 * t + c] += cq * b[c];
+                V[c] = b[c];
+            }
+        }
+        for (int c = 0; c < 3; ++c) {
+            ax[3 * i + c] = A[c];
+            av[3 * i + c] = V[c];
+        }
+    }
+    // dJ/dphi
+    std::vector<double> lam(h->Nn, 0.0);
+    for (int64_t t = 0; t < h->Nt; ++t) {
+        const double *a = &gE[3 * t];
+        const Tet &T = h->tet[t];
+        const double m0 = T.M[0] * a[0] + T.M[1] * a[1] + T.M[2] * a[2];
+        const double m1 = T.M[3] * a[0] + T.M[4] * a[1] + T.M[5] * a[2];
+        const double m2 = T.M[6] * a[0] + T.M[7] * a[1] + T.M[8] * a[2];
+        const int32_t *nd = &h->tn[4 * t];
+        lam[nd[0]] += m0 + m1 + m2;
+        lam[nd[1]] -= m0;
+        lam[nd[2]] -= m1;
+        lam[nd[3]] -= m2;
+    }
+    // adjoint CG: K mu = lam on free nodes (the Dirichlet rows are identity, rhs 0)
+    std::vector<double> b(h->Nn), saved_phi = h->phi;
+    for (int64_t i = 0; i < h->Nn; ++i) b[i] = h->isd[i] ? 0.0 : lam[i];
+    std::fill(h->phi.begin(), h->phi.end(), 0.0);
+    int32_t it = 0;
+    double rr = 0.0;
+    const int rc = pcg(*h, b, &it, &rr);
+    std::vector<double> mu = h->phi;
+    h->phi = saved_phi;
+    if (rc) return fail(rc, "adjoint PCG did not converge");
+    for (int64_t i = 0; i < h->Nn; ++i) dJ_dg[i] = h->isd[i] ? lam[i] : 0.0;
+    for (int64_t f = 0; f < h->Nn; ++f)
+        for (const auto &e : h->elim[f]) dJ_dg[e.first] -= e.second * mu[f];
+    if (dJ_dx0) std::copy(ax.begin(), ax.end(), dJ_dx0);
+    if (dJ_dv0) std::copy(av.begin(), av.end(), dJ_dv0);
+    return SPG_OK;
+}
+
+int spo_grad_freeze(spo_handle *h, int mode) {
+    h->freeze = mode;
+    if (mode == 0) h->frozen.clear();
     return SPG_OK;
 }
 

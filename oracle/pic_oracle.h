@@ -50,6 +50,21 @@ int spo_locate(spo_handle *h, int64_t n, const double *pos, int32_t *tet_out);
 int spo_get_matrix(spo_handle *h, int32_t *row_ptr, int32_t *col, double *val, double *lift);
 int spo_get_dual_volumes(spo_handle *h, double *dv);
 
+/* Dirichlet values (g [n_nodes] read at the Dirichlet nodes). */
+int spo_set_dirichlet(spo_handle *h, const double *g);
+/* FP64 reference gradient of J = (1/N) sum over landed particles of
+ * exp(-|r - target|^2 / (2 sigma^2)) after nsteps steps in the current field:
+ * full histories, particle adjoint, one adjoint PCG, lifting transpose.
+ * dJ_dg [n_nodes]; dJ_dx0, dJ_dv0 [3n] nullable. */
+int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, double *J, int64_t *n_landed,
+             double *dJ_dg, double *dJ_dx0, double *dJ_dv0);
+
+/* Field-cell freezing for spo_grad, for finite differences of the map the
+ * pathwise adjoint differentiates: mode 1 records the cell whose E pushes each
+ * particle at each step of the next spo_grad, mode 2 pushes with the recorded
+ * cells in later calls (the walk, landing and collisions stay live), 0 off. */
+int spo_grad_freeze(spo_handle *h, int mode);
+
 /* Primitives pinned by the reference's unit tests. */
 void spo_update_position(double *pos3, const double *vel3, double dt);
 /* Segment-triangle intersection: 1 and the point when they meet (a segment

@@ -112,7 +112,10 @@ SIGNATURES = {
     "spg_profile_enable": (C.c_int, [_H, C.c_int32]),
     "spg_get_profile": (C.c_int, [_H, C.POINTER(Profile)]),
     "spg_profile_reset": (C.c_int, [_H]),
-    "spg_pcg_solve_noalloc": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+    "spg_set_dirichlet": (C.c_int, [_H, _pd]),
+    "spg_grad_forward": (C.c_int, [_H, C.c_int32, C.c_int32, _pd, C.c_double, _pd, C.POINTER(C.c_int64)]),
+    "spg_grad_backward": (C.c_int, [_H, _pd, _pd, _pd, _pi32]),
+    "spg_pcg_solve_noalloc":(C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_double, C.c_int32, C.c_void_p, _pi32, _pd]),
 }
 

@@ -43,6 +43,7 @@ def _sources():
         ("kernels_pcg.cu", common_nv),
         ("kernels_mixed.cu", common_nv),
         ("noalloc.cu", common_nv),
+        ("kernels_adjoint.cu", common_nv + ["--fmad=false"]),
         ("mesh_prep.cpp", common_cc + ["-fopenmp"]),
         ("capi.cpp", common_cc),
     ]

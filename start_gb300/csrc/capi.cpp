@@ -119,6 +119,28 @@ struct spg_handle {
     int64_t pcg_iters_prof = 0;
     unsigned long long processed_at_reset = 0;
     int64_t launches = 0;  // kernels launched (all phases), reset with the profile
+
+    // Dirichlet data for spg_set_dirichlet and the adjoint of the lifting:
+    // eliminated couplings K_fd as CSR over free rows.
+    int64_t n_elim = 0;
+    int64_t *elim_rp = nullptr;
+    int32_t *elim_row = nullptr, *elim_col = nullptr;
+    double *elim_val = nullptr;
+    uint8_t *is_dir_host = nullptr;
+
+    // gradient state (spg_grad_forward / spg_grad_backward)
+    std::vector<DevParticles> ckpt;   // particle state at steps 0, ce, 2 ce, ...
+    int32_t grad_steps = 0, grad_every = 0;
+    int64_t grad_step0 = 0;
+    LandRec *land = nullptr;
+    double *gr = nullptr, *adj_x = nullptr, *adj_v = nullptr, *gE = nullptr, *lam = nullptr, *mu = nullptr,
+           *dJdg = nullptr, *sums = nullptr;
+    AdjHist hist{};
+    unsigned int *tri_scratch = nullptr;
+    DevCounters *ctr_scratch = nullptr;
+    int64_t ckpt_cap = 0, land_cap = 0, hist_cap = 0;  // particles (x window steps for hist) allocated
+    double grad_inv_n = 0.0;                            // 1 / landed count of the last forward
+    bool grad_ready = false;
 };
 
 namespace {
@@ -754,6 +776,16 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
             CK(upload(&h->sval32, sv32, s));
         }
     }
+    {
+        std::vector<int64_t> erp(hm.n_nodes + 1, 0);
+        for (int32_t r : hm.elim_row) erp[r + 1]++;
+        for (int64_t i = 0; i < hm.n_nodes; ++i) erp[i + 1] += erp[i];
+        h->n_elim = int64_t(hm.elim_val.size());
+        CK(upload(&h->elim_rp, erp, s));
+        CK(upload(&h->elim_row, hm.elim_row, s));
+        CK(upload(&h->elim_col, hm.elim_col, s));
+        CK(upload(&h->elim_val, hm.elim_val, s));
+    }
     CK(upload(&h->row_ptr, hm.row_ptr, s));
     CK(upload(&h->col, hm.col, s));
     CK(upload(&h->val, hm.val, s));
@@ -832,11 +864,18 @@ int spg_destroy(spg_handle *h) {
                     h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
+                    h->elim_rp,  h->elim_row, h->elim_col, h->elim_val, h->land, h->gr, h->adj_x, h->adj_v,
+                    h->gE,       h->lam,      h->mu,       h->dJdg,    h->sums, h->hist.tet, h->hist.vx,
+                    h->hist.vy,  h->hist.vz,  h->tri_scratch, h->ctr_scratch,
                     h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch, h->walkq_n};
     for (void *ptr : ptrs) cudaFree(ptr);
     for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
     if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
     if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
+    for (auto &P : h->ckpt)
+        for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
+                        (void *)P.tet, (void *)P.idf})
+            cudaFree(q);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return SPG_OK;
@@ -1227,6 +1266,227 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     }
     h->fix_bits = fix_bits_for(h->np);
     CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- gradient
+namespace {
+
+template <class T>
+int ensure(spg_handle *h, T **ptr, size_t count) {
+    if (*ptr) return SPG_OK;
+    CK(dalloc(ptr, count));
+    return SPG_OK;
+}
+
+int copy_particles(spg_handle *h, const DevParticles &dst, const DevParticles &src, int64_t n) {
+    if (n == 0) return SPG_OK;
+    cudaStream_t s = h->stream;
+    CK(cudaMemcpyAsync(dst.x, src.x, 8 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.y, src.y, 8 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.z, src.z, 8 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.vx, src.vx, 8 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.vy, src.vy, 8 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.vz, src.vz, 8 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.tet, src.tet, 4 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.idf, src.idf, 4 * n, cudaMemcpyDeviceToDevice, s));
+    return SPG_OK;
+}
+
+void free_particle_set(std::vector<DevParticles> &v) {
+    for (auto &P : v)
+        for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
+                        (void *)P.tet, (void *)P.idf})
+            cudaFree(q);
+    v.clear();
+}
+
+int alloc_dev_particles(spg_handle *h, DevParticles &P, int64_t n) {
+    CK(dalloc(&P.x, n));
+    CK(dalloc(&P.y, n));
+    CK(dalloc(&P.z, n));
+    CK(dalloc(&P.vx, n));
+    CK(dalloc(&P.vy, n));
+    CK(dalloc(&P.vz, n));
+    CK(dalloc(&P.tet, n));
+    CK(dalloc(&P.idf, n));
+    return SPG_OK;
+}
+
+// Solves K x = b (b, x device vectors of n_nodes) with the FP64 PCG of spg_solve.
+int solve_into(spg_handle *h, double *b, double *x, int32_t *iters) {
+    PcgScalars init{};
+    init.tol2 = h->prm.cg_rtol * h->prm.cg_rtol;
+    init.max_iter = h->prm.cg_max_iter;
+    CK(cudaMemcpyAsync(h->sc, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    PcgDev d = pcg_dev(h);
+    d.x = x;
+    launch_pcg_setup(d, b, h->stream);
+    PcgScalars hs{};
+    for (int chunk = 0;; ++chunk) {
+        for (int k = 0; k < kPcgChunk; ++k) launch_pcg_iteration(d, h->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (hs.converged) break;
+    }
+    if (iters) *iters = hs.iters;
+    if (hs.converged == 2) return fail(h, SPG_E_NOT_CONVERGED, "adjoint PCG did not converge");
+    return SPG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int spg_set_dirichlet(spg_handle *h, const double *g) {
+    if (!h || !g) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    double *dg = nullptr;
+    CK(dalloc(&dg, h->n_nodes));
+    CK(cudaMemcpyAsync(dg, g, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+    launch_set_dirichlet(h->is_dir, dg, h->dir_value, h->phi, h->n_nodes, h->stream);
+    launch_lift(h->elim_rp, h->elim_col, h->elim_val, h->dir_value, h->lift, h->n_nodes, h->stream);
+    CK(cudaGetLastError());
+    std::vector<uint8_t> isd(h->n_nodes);
+    CK(cudaMemcpyAsync(isd.data(), h->is_dir, h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int64_t i = 0; i < h->n_nodes; ++i)
+        if (isd[i]) h->phi_init[i] = g[i];
+    cudaFree(dg);
+    return SPG_OK;
+}
+
+int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, const double target[3], double sigma,
+                     double *J, int64_t *n_landed) {
+    if (!h || !target || !(sigma > 0.0) || nsteps < 1 || checkpoint_every < 1)
+        return fail(h, SPG_E_INVALID, "grad_forward: bad arguments");
+    if (h->mixed) return fail(h, SPG_E_INVALID, "grad_forward: the adjoint is available in the FP64 form");
+    if (h->prm.collision_model == SPG_COLL_VSS)
+        return fail(h, SPG_E_INVALID, "grad_forward: VSS scattering has no adjoint here (HS, VHS or none)");
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "grad_forward: no particles set");
+    CK(cudaSetDevice(h->device));
+    const int64_t n = h->np;
+    int rc;
+    const int nck = (nsteps + checkpoint_every - 1) / checkpoint_every;
+    h->grad_ready = false;
+    if (int(h->ckpt.size()) < nck || n > h->ckpt_cap) {
+        free_particle_set(h->ckpt);
+        h->ckpt_cap = 0;
+        h->ckpt.assign(nck, DevParticles{});
+        for (auto &P : h->ckpt)
+            if ((rc = alloc_dev_particles(h, P, std::max<int64_t>(n, 1)))) return rc;
+        h->ckpt_cap = std::max<int64_t>(n, 1);
+    }
+    if (n > h->land_cap) {
+        for (void *q : {(void *)h->land, (void *)h->gr, (void *)h->adj_x, (void *)h->adj_v}) cudaFree(q);
+        h->land = nullptr;
+        h->gr = h->adj_x = h->adj_v = nullptr;
+        h->land_cap = 0;
+        const int64_t m = std::max<int64_t>(n, 1);
+        CK(dalloc(&h->land, m));
+        CK(dalloc(&h->gr, 3 * m));
+        CK(dalloc(&h->adj_x, 3 * m));
+        CK(dalloc(&h->adj_v, 3 * m));
+        h->land_cap = m;
+    }
+    if ((rc = ensure(h, &h->sums, 2)) || (rc = ensure(h, &h->gE, 3 * size_t(h->n_tets))) ||
+        (rc = ensure(h, &h->lam, h->n_nodes)) || (rc = ensure(h, &h->mu, h->n_nodes)) ||
+        (rc = ensure(h, &h->dJdg, h->n_nodes)) || (rc = ensure(h, &h->tri_scratch, std::max<int64_t>(h->n_tris, 1))) ||
+        (rc = ensure(h, &h->ctr_scratch, 1)))
+        return rc;
+    CK(cudaMemsetAsync(h->land, 0xff, sizeof(LandRec) * std::max<int64_t>(n, 1), h->stream));
+    h->grad_steps = nsteps;
+    h->grad_every = checkpoint_every;
+    h->grad_step0 = h->step;
+    for (int k = 0; k < nsteps; ++k) {
+        if (k % checkpoint_every == 0)
+            if ((rc = copy_particles(h, h->ckpt[k / checkpoint_every], h->P[h->cur], n))) return rc;
+        StepConst c = step_const(h);
+        launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
+                      h->stream, h->land);
+        CK(cudaGetLastError());
+        h->step++;
+    }
+    CK(cudaMemsetAsync(h->sums, 0, 2 * sizeof(double), h->stream));
+    launch_objective(h->P[h->cur], n, h->land, target, sigma, h->gr, h->sums, h->stream);
+    CK(cudaGetLastError());
+    double sums[2];
+    CK(cudaMemcpyAsync(sums, h->sums, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (J) *J = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+    if (n_landed) *n_landed = int64_t(sums[1]);
+    // J = sum g / N_landed with N_landed held fixed: dJ/dr = (dg/dr) / N
+    h->grad_inv_n = sums[1] > 0.0 ? 1.0 / sums[1] : 0.0;
+    h->grad_ready = sums[1] > 0.0;
+    return SPG_OK;
+}
+
+int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_dv0, int32_t *adj_iters) {
+    if (!h || !dJ_dg) return fail(h, SPG_E_INVALID, "grad_backward: dJ_dg is required");
+    if (!h->grad_ready) return fail(h, SPG_E_STATE, "grad_backward: run spg_grad_forward first (with landings)");
+    CK(cudaSetDevice(h->device));
+    const int64_t n = h->np;
+    const int W = h->grad_every;
+    cudaStream_t s = h->stream;
+    int rc;
+    const int64_t hneed = int64_t(W) * std::max<int64_t>(n, 1);
+    if (hneed > h->hist_cap) {
+        for (void *q : {(void *)h->hist.tet, (void *)h->hist.vx, (void *)h->hist.vy, (void *)h->hist.vz}) cudaFree(q);
+        h->hist = AdjHist{};
+        h->hist_cap = 0;
+        CK(dalloc(&h->hist.tet, hneed));
+        CK(dalloc(&h->hist.vx, hneed));
+        CK(dalloc(&h->hist.vy, hneed));
+        CK(dalloc(&h->hist.vz, hneed));
+        h->hist_cap = hneed;
+    }
+    CK(cudaMemsetAsync(h->adj_x, 0, sizeof(double) * 3 * n, s));
+    CK(cudaMemsetAsync(h->adj_v, 0, sizeof(double) * 3 * n, s));
+    CK(cudaMemsetAsync(h->gE, 0, sizeof(double) * 3 * h->n_tets, s));
+    DevParticles &work = h->P[1 - h->cur];
+    const int nck = (h->grad_steps + W - 1) / W;
+    for (int w = nck - 1; w >= 0; --w) {
+        const int k0 = w * W, k1 = std::min(h->grad_steps, k0 + W);
+        if ((rc = copy_particles(h, work, h->ckpt[w], n))) return rc;
+        CK(cudaMemsetAsync(h->ctr_scratch, 0, sizeof(DevCounters), s));
+        for (int k = k0; k < k1; ++k) {
+            launch_record(work, n, h->hist, k - k0, s);
+            StepConst c = step_const(h);
+            c.step = h->grad_step0 + k;
+            launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
+        }
+        StepConst c = step_const(h);
+        c.step = h->grad_step0;  // absolute step of k = 0 (landing steps and Philox counters are absolute)
+        launch_backward(work, n, h->hist, k0, k1, h->rec, h->land, h->gr, h->grad_inv_n, h->adj_x, h->adj_v, h->gE,
+                        c, s);
+        CK(cudaGetLastError());
+    }
+    CK(cudaMemsetAsync(h->lam, 0, sizeof(double) * h->n_nodes, s));
+    launch_gE_to_nodes(h->tet_nodes, h->rec, h->gE, h->n_tets, h->lam, s);
+    launch_adj_rhs(h->lam, h->is_dir, h->b, h->mu, h->n_nodes, s);
+    CK(cudaGetLastError());
+    int32_t it = 0;
+    if ((rc = solve_into(h, h->b, h->mu, &it))) return rc;
+    if (adj_iters) *adj_iters = it;
+    launch_dirichlet_grad(h->lam, h->is_dir, h->elim_row, h->elim_col, h->elim_val, h->n_elim, h->mu, h->dJdg,
+                          h->n_nodes, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dJ_dg, h->dJdg, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost, s));
+    if (dJ_dx0 || dJ_dv0) {
+        double *dx = nullptr, *dv = nullptr;
+        if (dJ_dx0) CK(dalloc(&dx, 3 * n));
+        if (dJ_dv0) CK(dalloc(&dv, 3 * n));
+        launch_gather_adj(h->P[h->cur], n, h->adj_x, h->adj_v, dx, dv, s);
+        if (dJ_dx0) CK(cudaMemcpyAsync(dJ_dx0, dx, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+        if (dJ_dv0) CK(cudaMemcpyAsync(dJ_dv0, dv, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        cudaFree(dx);
+        cudaFree(dv);
+    }
     CK(cudaStreamSynchronize(s));
     return SPG_OK;
 }

@@ -104,7 +104,7 @@ __device__ __forceinline__ bool inside_sure(const TetGeo &g, double d0, double d
 }
 
 struct WalkOut {
-    int tet, status, tri, crossings;
+    int tet, status, tri, crossings, face;
     double s;
 };
 
@@ -119,6 +119,7 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
     WalkOut o;
     o.crossings = 0;
     o.tri = -1;
+    o.face = -1;
     o.s = 1.0;
     int enter = -1;
     for (;;) {
@@ -152,6 +153,7 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
             o.tet = t;
             o.status = W_SURFACE;
             o.tri = tri;
+            o.face = best;
             o.s = sb;
             return o;
         }
@@ -372,10 +374,13 @@ __global__ void __launch_bounds__(256, 4) k_step64(DevParticles p, int64_t n, Me
 
 // Exact FP64 walk of the queued particles (start point from the queue, end
 // point already in the position arrays), one particle per lane.
+// With land != nullptr, a particle that settles also records the step, the
+// exit face of its final tet and the hit fraction of the segment (adjoint).
 __global__ void __launch_bounds__(128) k_walk_queue64(DevParticles p, MeshDev m, int max_cross,
                                                       const WalkItem *__restrict__ wq,
                                                       const unsigned int *__restrict__ wq_n,
-                                                      unsigned int *__restrict__ tri_count, DevCounters *ctr) {
+                                                      unsigned int *__restrict__ tri_count, DevCounters *ctr,
+                                                      LandRec *__restrict__ land, int64_t step) {
     const unsigned nq = *wq_n;
     unsigned cross = 0, settled = 0, lost = 0, capped = 0;
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
@@ -395,6 +400,12 @@ __global__ void __launch_bounds__(128) k_walk_queue64(DevParticles p, MeshDev m,
             atomicAdd(tri_count + w.tri, 1u);
             p.idf[i] = idf | kSettled;
             settled++;
+            if (land) {
+                land[i].step = int32_t(step);
+                land[i].face = w.face;
+                land[i].tet = w.tet;
+                land[i].s = w.s;
+            }
         } else if (w.status != W_INSIDE) {
             p.idf[i] = idf | kLost;
             lost++;
@@ -739,11 +750,11 @@ inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1)
 }  // namespace
 
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c, unsigned int *tri_count,
-                   WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s) {
+                   WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s, LandRec *land) {
     if (n <= 0) return;
     cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
     k_step64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, c, wq, wq_n, ctr);
-    k_walk_queue64<<<152 * 8, 128, 0, s>>>(p, m, c.max_cross, wq, wq_n, tri_count, ctr);
+    k_walk_queue64<<<152 * 8, 128, 0, s>>>(p, m, c.max_cross, wq, wq_n, tri_count, ctr, land, c.step);
 }
 
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,

@@ -84,13 +84,26 @@ __device__ bool block_reduce2(double a, double b, double *partials, PcgScalars *
 // warp), each slice padded to its longest row and stored column-major, so
 // lane l of a warp reads entry j of its row at slice_ptr[s] + 32 j + l and a
 // warp's 32 loads of one j are contiguous. Padding entries have value 0.
+// Four entries per trip with their loads issued before the FMAs and two
+// accumulators, so each thread keeps several gathers in flight.
 __device__ __forceinline__ double spmv_row(const PcgDev &d, const double *__restrict__ x, int64_t i) {
     const int64_t s = i >> 5;
-    const int64_t k0 = __ldg(d.slice_ptr + s) + (i & 31);
+    int64_t k = __ldg(d.slice_ptr + s) + (i & 31);
     const int64_t k1 = __ldg(d.slice_ptr + s + 1);
-    double acc = 0.0;
-    for (int64_t k = k0; k < k1; k += 32) acc = fma(__ldg(d.sval + k), __ldg(x + __ldg(d.scol + k)), acc);
-    return acc;
+    double a0 = 0.0, a1 = 0.0;
+    for (; k + 96 < k1; k += 128) {
+        const int32_t c0 = __ldg(d.scol + k), c1 = __ldg(d.scol + k + 32);
+        const int32_t c2 = __ldg(d.scol + k + 64), c3 = __ldg(d.scol + k + 96);
+        const double v0 = __ldg(d.sval + k), v1 = __ldg(d.sval + k + 32);
+        const double v2 = __ldg(d.sval + k + 64), v3 = __ldg(d.sval + k + 96);
+        const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+        a0 = fma(v0, x0, a0);
+        a1 = fma(v1, x1, a1);
+        a0 = fma(v2, x2, a0);
+        a1 = fma(v3, x3, a1);
+    }
+    for (; k < k1; k += 32) a0 = fma(__ldg(d.sval + k), __ldg(x + __ldg(d.scol + k)), a0);
+    return a0 + a1;
 }
 
 __global__ void k_rhs(const double *__restrict__ node_q, double inv_eps0, const double *__restrict__ lift,
@@ -219,11 +232,22 @@ __global__ void __launch_bounds__(kThreads) k_pupdate(PcgDev d) {
 
 __device__ __forceinline__ float spmv_row32(const PcgDev32 &d, const float *__restrict__ x, int64_t i) {
     const int64_t s = i >> 5;
-    const int64_t k0 = __ldg(d.slice_ptr + s) + (i & 31);
+    int64_t k = __ldg(d.slice_ptr + s) + (i & 31);
     const int64_t k1 = __ldg(d.slice_ptr + s + 1);
-    float acc = 0.0f;
-    for (int64_t k = k0; k < k1; k += 32) acc = fmaf(__ldg(d.sval + k), __ldg(x + __ldg(d.scol + k)), acc);
-    return acc;
+    float a0 = 0.0f, a1 = 0.0f;
+    for (; k + 96 < k1; k += 128) {
+        const int32_t c0 = __ldg(d.scol + k), c1 = __ldg(d.scol + k + 32);
+        const int32_t c2 = __ldg(d.scol + k + 64), c3 = __ldg(d.scol + k + 96);
+        const float v0 = __ldg(d.sval + k), v1 = __ldg(d.sval + k + 32);
+        const float v2 = __ldg(d.sval + k + 64), v3 = __ldg(d.sval + k + 96);
+        const float x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+        a0 = fmaf(v0, x0, a0);
+        a1 = fmaf(v1, x1, a1);
+        a0 = fmaf(v2, x2, a0);
+        a1 = fmaf(v3, x3, a1);
+    }
+    for (; k < k1; k += 32) a0 = fmaf(__ldg(d.sval + k), __ldg(x + __ldg(d.scol + k)), a0);
+    return a0 + a1;
 }
 
 __device__ __forceinline__ float warp_sumf(float v) {

@@ -267,6 +267,7 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
     m.val.assign(nnz, 0.0);
     m.diag.assign(Nn, 1.0);
     m.lift.assign(Nn, 0.0);
+    std::vector<std::vector<std::pair<int32_t, double>>> elim(Nn);  // free row -> (Dirichlet col, K)
 #pragma omp parallel for schedule(dynamic, 1024)
     for (int64_t i = 0; i < Nn; ++i) {
         int32_t *c0 = &m.col[m.row_ptr[i]];
@@ -308,6 +309,14 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
                 const int32_t j = tn[b];
                 if (m.is_dir[j]) {
                     lift += kab * m.dir_value[j];
+                    auto &e = elim[i];
+                    auto it = std::find_if(e.begin(), e.end(), [j](const std::pair<int32_t, double> &x) {
+                        return x.first == j;
+                    });
+                    if (it == e.end())
+                        e.emplace_back(j, kab);
+                    else
+                        it->second += kab;
                 } else {
                     const int32_t *pos = std::lower_bound(c0, c0 + len, j);
                     v0[pos - c0] += kab;
@@ -317,6 +326,20 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
         m.lift[i] = lift;
         for (int32_t k = 0; k < len; ++k)
             if (c0[k] == i) m.diag[i] = v0[k];
+    }
+
+    // Eliminated couplings K_fd (free row f, Dirichlet column d): the lifting
+    // vector for new Dirichlet values and the adjoint of the lifting.
+    m.elim_row.clear();
+    m.elim_col.clear();
+    m.elim_val.clear();
+    for (int64_t i = 0; i < Nn; ++i) {
+        std::sort(elim[i].begin(), elim[i].end());
+        for (const auto &e : elim[i]) {
+            m.elim_row.push_back(int32_t(i));
+            m.elim_col.push_back(e.first);
+            m.elim_val.push_back(e.second);
+        }
     }
 
     // 7. Expanded global bounding box of the surface triangles

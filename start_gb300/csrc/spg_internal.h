@@ -56,6 +56,8 @@ struct HostMesh {
     std::vector<uint8_t> is_dir;
     std::vector<double> dir_value;  // Nn (0 on free nodes)
     std::vector<double> lift;       // Nn: sum_{j in D} K_ij g_j on free rows, 0 on D rows
+    std::vector<int32_t> elim_row, elim_col;  // eliminated couplings K_fd, f free, d Dirichlet
+    std::vector<double> elim_val;
     // Reference global bounding box test (SurfaceMesh.cpp:104-134), expanded.
     double bbox_lo[3] = {0, 0, 0}, bbox_hi[3] = {0, 0, 0};
     // Voxel seed grid for point location.
@@ -139,10 +141,49 @@ struct WalkItem {
     double x0, y0, z0;
 };
 
+// Landing record of a settled particle (adjoint of the landing point): step
+// of the crossing, exit face of the final tet, hit fraction s of the move
+// segment; step = -1 while the particle has not landed.
+struct LandRec {
+    int32_t step;
+    int32_t face;
+    int32_t tet;  // tet whose face was crossed
+    int32_t pad;
+    double s;
+};
+
+// Per-step record of a checkpoint window (adjoint recompute): tet (-1 when
+// the particle is dead) and velocity at the start of each step, [k][i].
+struct AdjHist {
+    int32_t *tet;
+    double *vx, *vy, *vz;
+};
+
+// kernels_adjoint.cu
+void launch_record(const DevParticles &p, int64_t n, const AdjHist &h, int k, cudaStream_t s);
+void launch_objective(const DevParticles &p, int64_t n, const LandRec *land, const double *target, double sigma,
+                      double *gr, double *sums, cudaStream_t s);
+void launch_backward(const DevParticles &p, int64_t n, const AdjHist &h, int k0, int k1, const TetRec *rec,
+                     const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
+                     const StepConst &c, cudaStream_t s);
+void launch_gE_to_nodes(const int4 *tet_nodes, const TetRec *rec, const double *gE, int64_t nt, double *lam,
+                        cudaStream_t s);
+void launch_adj_rhs(const double *lam, const uint8_t *is_dir, double *b, double *x, int64_t nn, cudaStream_t s);
+void launch_dirichlet_grad(const double *lam, const uint8_t *is_dir, const int32_t *er, const int32_t *ec,
+                           const double *ev, int64_t ne, const double *mu, double *out, int64_t nn, cudaStream_t s);
+void launch_lift(const int64_t *erp, const int32_t *ec, const double *ev, const double *g, double *lift, int64_t nn,
+                 cudaStream_t s);
+void launch_set_dirichlet(const uint8_t *is_dir, const double *g, double *dir_value, double *phi, int64_t nn,
+                          cudaStream_t s);
+void launch_gather_adj(const DevParticles &p, int64_t n, const double *ax, const double *av, double *dx, double *dv,
+                       cudaStream_t s);
+
 // Kernel launchers (kernels_particles.cu).
-// Step kernel plus the exact walk of the queued particles (wq holds up to n items).
+// Step kernel plus the exact walk of the queued particles (wq holds up to n
+// items); land (nullable) receives the landing records.
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c,
-                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s);
+                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
+                   LandRec *land = nullptr);
 // Fixed-point P1 deposit: node_fix[n] += round(lambda_n * 2^k) per alive
 // particle (lambda_0 takes the remainder so each particle adds exactly 2^k).
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,

@@ -224,6 +224,30 @@ class StartPIC:
         buf = C.create_string_buffer(blob, len(blob))
         self._check(self.lib.spg_restore(self.h, buf, len(blob)))
 
+    def set_dirichlet(self, g):
+        """Dirichlet values g [n_nodes] (read at the Dirichlet nodes)."""
+        g = np.ascontiguousarray(g, np.float64)
+        self._check(self.lib.spg_set_dirichlet(self.h, N.as_ptr(g, C.c_double)))
+
+    def grad_forward(self, nsteps, target, sigma, checkpoint_every=32):
+        """Particle steps with landing records and checkpoints; returns (J, n_landed)."""
+        t = np.ascontiguousarray(target, np.float64)
+        J, nl = C.c_double(), C.c_int64()
+        self._check(self.lib.spg_grad_forward(self.h, int(nsteps), int(checkpoint_every), N.as_ptr(t, C.c_double),
+                                              float(sigma), C.byref(J), C.byref(nl)))
+        return J.value, nl.value
+
+    def grad_backward(self, particles=True):
+        """Adjoint pass; returns dJ/dg [n_nodes], dJ/dx0 [n,3], dJ/dv0 [n,3], adjoint CG iterations."""
+        g = np.zeros(self.n_nodes)
+        dx = np.zeros((self.n_particles, 3)) if particles else None
+        dv = np.zeros((self.n_particles, 3)) if particles else None
+        it = C.c_int32()
+        self._check(self.lib.spg_grad_backward(self.h, N.as_ptr(g, C.c_double),
+                                               N.as_ptr(dx, C.c_double) if particles else None,
+                                               N.as_ptr(dv, C.c_double) if particles else None, C.byref(it)))
+        return g, dx, dv, it.value
+
     def synchronize(self):
         self._check(self.lib.spg_synchronize(self.h))
 

@@ -1,0 +1,105 @@
+"""GPU adjoint of the landing objective against the FP64 oracle gradient.
+
+The oracle gradient is itself checked against central finite differences of
+the same map (tests/test_oracle_adjoint.py). Problem: the 100 mm cube at
+h = 4 mm, top electrode at +500 V turning the 1 eV Ti+ ions back onto z = 0
+within 400 steps, argon at 1 Pa / 300 K, target the centre of the bottom face,
+sigma = 10 mm, checkpoints every 32 steps.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+V0 = np.array([0.0, 0.0, 0.0, 0.0, 0.0, 500.0])
+A0 = np.deg2rad(30.0)
+
+
+def _gpu_problem(n, collisions=False, steps=400):
+    from start_gb300.adjoint import LandingProblem
+
+    p = LandingProblem(n_particles=n, steps=steps, collisions=collisions, cg_rtol=1e-13)
+    p.target = np.array([0.05, 0.05, 0.0])
+    return p
+
+
+@pytest.mark.parametrize("collisions", [False, True], ids=["collisionless", "hs"])
+def test_gradient_matches_oracle(built, collisions):
+    import oracle as O
+
+    p = _gpu_problem(3000, collisions)
+    J = p.forward(V0, A0)
+    nl = p._last[2]
+    dJ_dg, dJ_dx, dJ_dv, iters = p.engine.grad_backward(particles=True)
+    assert iters > 0
+
+    o = O.Oracle(p.mesh, p.params)
+    o.set_dirichlet(p.dirichlet_values(V0))
+    x0, v0, dx0, dv0 = p.initial_state(A0)
+    o.set_particles(x0, v0)
+    o.solve(np.zeros(p.mesh.n_nodes))
+    Jo, nlo, dgo, dxo, dvo = o.grad(p.steps, p.target, p.sigma)
+
+    assert nl == nlo and nl >= 2700
+    assert abs(J - Jo) <= 1e-10 * Jo
+    # collisionless runs share every tet of every step with the oracle; with
+    # collisions the GPU's sin/cos differ from the host's in the last bit
+    tol = 1e-8 if not collisions else 1e-6
+    dV, dVo = p.face_sums(dJ_dg), p.face_sums(dgo)
+    assert np.max(np.abs(dV - dVo)) <= tol * np.max(np.abs(dVo)), (dV, dVo)
+    assert np.max(np.abs(dJ_dg - dgo)) <= tol * np.max(np.abs(dgo))
+    for a, b in ((dJ_dx, dxo), (dJ_dv, dvo)):
+        err = np.abs(a - b).max(axis=1)
+        bad = err > tol * np.abs(b).max()
+        assert bad.sum() <= (0 if not collisions else 3), np.nonzero(bad)[0][:10]
+    da = float(np.sum(dJ_dx * dx0) + np.sum(dJ_dv * dv0))
+    dao = float(np.sum(dxo * dx0) + np.sum(dvo * dv0))
+    assert abs(da - dao) <= tol * abs(dao)
+    o.close()
+    p.close()
+
+
+def test_checkpoint_interval_does_not_change_gradient(built):
+    """Recompute from checkpoints every 32 steps gives the same gradient as
+    keeping one window per step (bit-identical forward replay)."""
+    p = _gpu_problem(2000, collisions=True)
+    p.forward(V0, A0)
+    g32 = p.engine.grad_backward(particles=True)
+    p.every = 7
+    p.forward(V0, A0)
+    g7 = p.engine.grad_backward(particles=True)
+    for a, b in zip(g32[:3], g7[:3]):
+        assert np.array_equal(a, b)
+    p.close()
+
+
+def test_autograd_function(built):
+    import torch
+
+    from start_gb300.adjoint import landing_objective
+
+    p = _gpu_problem(5000)
+    f = landing_objective()
+    params = torch.tensor(np.concatenate([V0, [A0]]), dtype=torch.float64, requires_grad=True)
+    J = f.apply(params, p)
+    J.backward()
+    dV, dalpha, _ = p.backward()
+    assert np.allclose(params.grad.numpy(), np.concatenate([dV, [dalpha]]), rtol=1e-12, atol=0)
+    p.close()
+
+
+def test_gradient_cost_vs_forward(built):
+    """At 1e6 particles the gradient pass (checkpoint recompute + particle
+    adjoint + one adjoint CG) costs at most 4x one forward pass."""
+    import time
+
+    p = _gpu_problem(1_000_000, collisions=True, steps=300)
+    p.forward(V0, A0)
+    p.backward()  # warm up allocations
+    t0 = time.perf_counter()
+    p.forward(V0, A0)
+    t1 = time.perf_counter()
+    p.backward()
+    t2 = time.perf_counter()
+    assert (t2 - t1) <= 4.0 * (t1 - t0), (t1 - t0, t2 - t1)
+    p.close()

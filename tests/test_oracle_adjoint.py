@@ -1,0 +1,73 @@
+"""The FP64 reference gradient of the oracle (CPU only).
+
+The oracle's adjoint (particle recursion, frozen collisions, E transpose,
+adjoint CG, lifting transpose) is checked against central finite differences
+of the map it differentiates: the step with collision events, random numbers
+and the cell whose E pushes each particle at each step held fixed. The GPU
+gradient is then checked against this oracle gradient (tests/test_gpu_adjoint.py).
+
+Problem: the 100 mm cube at h = 4 mm, top electrode at +500 V turning the
+1 eV Ti+ ions back onto z = 0 within 400 steps, argon at 1 Pa / 300 K
+(hard spheres, about 0.3 collisions per ion), target the centre of the bottom
+face, sigma = 10 mm; h = 1e-3 V and 1e-4 rad. Denser gas makes some frozen
+collision decisions flip under the perturbation (u0 < P(v) with v moved), and
+central differences then carry those jumps.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from start_gb300.adjoint import LandingSetup
+
+V0 = np.array([0.0, 0.0, 0.0, 0.0, 0.0, 500.0])
+A0 = np.deg2rad(30.0)
+
+
+class OracleLanding(LandingSetup):
+    def __init__(self, n, collisions, gas_scale=1.0):
+        super().__init__(n_particles=n, steps=400, collisions=collisions, gas_scale=gas_scale, cg_rtol=1e-13)
+        self.target = np.array([0.05, 0.05, 0.0])
+        self.o = O.Oracle(self.mesh, self.params)
+
+    def run(self, V, alpha):
+        self.o.set_dirichlet(self.dirichlet_values(V))
+        x0, v0, dx0, dv0 = self.initial_state(alpha)
+        self.o.set_particles(x0, v0)
+        self.o.solve(np.zeros(self.mesh.n_nodes))
+        J, nl, dg, dx, dv = self.o.grad(self.steps, self.target, self.sigma)
+        da = float(np.sum(dx * dx0) + np.sum(dv * dv0))
+        return J, nl, self.face_sums(dg), da
+
+
+@pytest.fixture(scope="module", params=[False, True], ids=["collisionless", "hs"])
+def landing(request, built):
+    prob = OracleLanding(3000, request.param)
+    prob.o.grad_freeze(1)
+    base = prob.run(V0, A0)
+    prob.o.grad_freeze(2)
+    yield prob, base
+    prob.o.close()
+
+
+def test_pathwise_gradient_matches_central_differences(landing):
+    prob, (J, nl, dV, da) = landing
+    assert nl >= 2700 and 0.05 < J < 1.0
+    scale = np.max(np.abs(dV))
+    h = 1e-3
+    for f in (4, 5, 0):
+        Vp, Vm = V0.copy(), V0.copy()
+        Vp[f] += h
+        Vm[f] -= h
+        rp, rm = prob.run(Vp, A0), prob.run(Vm, A0)
+        assert rp[1] == rm[1] == nl
+        fd = (rp[0] - rm[0]) / (2 * h)
+        assert abs(dV[f] - fd) <= 1e-4 * scale, (f, dV[f], fd)
+    ha = 1e-4
+    fda = (prob.run(V0, A0 + ha)[0] - prob.run(V0, A0 - ha)[0]) / (2 * ha)
+    assert abs(da - fda) <= 1e-4 * abs(fda), (da, fda)
+
+
+def test_gradient_is_gauge_invariant(landing):
+    """Raising every electrode by the same amount leaves E unchanged."""
+    prob, (J, nl, dV, da) = landing
+    assert abs(dV.sum()) <= 1e-9 * np.abs(dV).sum()
