@@ -34,7 +34,7 @@ sys.path.insert(0, str(ROOT))
 
 import numpy as np  # noqa: E402
 
-METRIC = "particle-steps/s"
+METRIC = "particle-steps/s @1e7 ptcl: mixed vs FP64 GPU at \u22641% deposit L1; grad/fwd cost"
 UNIT = "particle-steps/s"
 
 
@@ -128,13 +128,15 @@ def build_workload(args):
     cells = args.cells
     w = workload1(n_particles=args.particles, cells=cells, seed=0, steps=args.warmup + args.steps)
     w.params["precision"] = 1 if args.precision == "mixed" else 0
+    w.params["preconditioner"] = 1 if args.precond == "amg" else 0
     return w
 
 
-def cpu_sample(w, n_sample, steps, threads=None):
+def cpu_sample(w, n_sample, steps, warmup=0, threads=None):
     """Times the CPU oracle on the first n_sample particles of the workload:
-    one untimed deposit + cold solve, then `steps` steps of the full loop
-    (warm-started solve at the first, as in steady state)."""
+    one untimed deposit + cold solve and `warmup` untimed steps, then `steps`
+    timed steps of the full loop (deposit + warm PCG every poisson_every
+    steps, push/walk/collide/settle every step), as the GPU arm does."""
     import oracle
 
     if threads:
@@ -143,8 +145,8 @@ def cpu_sample(w, n_sample, steps, threads=None):
     o = oracle.Oracle(w.mesh, w.params)
     t_setup = time.perf_counter() - t0
     o.set_particles(w.pos[:n_sample], w.vel[:n_sample])
-    o.gather(want_rho=False)
-    o.solve(want_phi=False, raise_on_nonconvergence=False)
+    if warmup > 0:
+        o.run(warmup, raise_on_nonconvergence=False)
     s0 = o.stats()["particle_steps"]
     t0 = time.perf_counter()
     o.run(steps, raise_on_nonconvergence=False)
@@ -154,28 +156,27 @@ def cpu_sample(w, n_sample, steps, threads=None):
     return (s1 - s0) / dt, dict(setup_s=t_setup, timed_s=dt, particle_steps=s1 - s0, threads=oracle.get_threads())
 
 
+def cpu_sample_desc(w, n_sample, steps, warmup):
+    who = "all" if n_sample >= len(w.pos) else f"{n_sample} of"
+    return (f"{who} {len(w.pos)} particles on the full mesh, {warmup} untimed + {steps} timed full-loop steps "
+            f"(deposit + warm PCG every {w.params['poisson_every']} steps, push/walk/collide/settle every step)")
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
     w = build_workload(args)
-    n_sample = min(args.cpu_sample, len(w.pos))
-    vals = []
-    info = {}
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_sample(w, n_sample, 1)
-    for _ in range(max(1, min(args.steps, 3))):
-        v, info = cpu_sample(w, n_sample, args.cpu_steps)
-        vals.append(v)
-    v = float(np.median(vals))
+    n_sample = min(args.cpu_sample or len(w.pos), len(w.pos))
+    steps = args.cpu_steps or args.steps
+    v, info = cpu_sample(w, n_sample, steps, args.warmup)
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded workload generator)",
+        "warmup": args.warmup, "ms_per_step": 1e3 * info["timed_s"] / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded workload generator)",
         "config": config_dict(args, w),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": info.get("threads"), "kind": "port",
-                         "sample": f"{n_sample} of {len(w.pos)} particles, {args.cpu_steps} full-loop steps "
-                                   f"(deposit + warm PCG + push/walk/collide/settle) on the full mesh"},
+                         "sample": cpu_sample_desc(w, n_sample, steps, args.warmup), "timed_s": info["timed_s"]},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference itself needs CGAL/Trilinos/Gmsh (absent); the timed CPU path is the FP64 "
                 "OpenMP oracle port of its step",
@@ -184,11 +185,61 @@ def run_reference(args):
     return 0
 
 
+def grad_leg(args, local):
+    """Gradient of the smoothed landing objective (the 100 mm electrode cube at
+    h = 4 mm, 1e6 Ti+, 300 steps, argon 1 Pa HS with collision events frozen,
+    checkpoints every 32 steps): cost of forward + backward against one plain
+    forward pass (set particles, electrode solve, 300 particle steps)."""
+    import torch
+
+    from start_gb300.adjoint import LandingProblem
+
+    V = np.array([0.0, 0.0, 0.0, 0.0, 0.0, 500.0])
+    a0 = np.deg2rad(30.0)
+    lp = LandingProblem(n_particles=args.grad_particles, steps=300, collisions=True)
+    lp.target = np.array([0.05, 0.05, 0.0])
+    e = lp.engine
+
+    def plain_forward():
+        e.set_dirichlet(lp.dirichlet_values(V))
+        x0, v0, _, _ = lp.initial_state(a0)
+        e.set_particles(x0, v0)
+        e.solve(np.zeros(lp.mesh.n_nodes))
+        e.process(lp.steps)
+        e.synchronize()
+
+    def timed(f, reps=3):
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = f()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3, out
+
+    plain_forward()
+    lp.forward(V, a0)
+    lp.backward()  # warm-up (allocations, graphs)
+    t_plain, _ = timed(plain_forward)
+    t_fwd, J = timed(lambda: lp.forward(V, a0))
+    t_bwd, (dV, da, iters) = timed(lp.backward)
+    out = {"workload": "cube100mm_h4mm_1e6ptcl_grad", "n_particles": int(args.grad_particles), "steps": 300,
+           "checkpoint_every": lp.every, "electrodes_V": V.tolist(), "half_angle_deg": 30.0,
+           "target": lp.target.tolist(), "sigma_m": lp.sigma, "J": J, "n_landed": int(lp._last[2]),
+           "dJ_dV": dV.tolist(), "dJ_dalpha": da, "adjoint_cg_iters": iters,
+           "plain_forward_ms": t_plain, "grad_forward_ms": t_fwd, "backward_ms": t_bwd,
+           "cost_ratio": (t_fwd + t_bwd) / t_plain, "timing": "host wall clock, median of 3, synchronised"}
+    lp.close()
+    return out
+
+
 def config_dict(args, w):
     return {"workload": w.name, "n_particles": int(len(w.pos)), "n_tets": int(w.mesh.n_tets),
             "n_nodes": int(w.mesh.n_nodes), "n_triangles": int(w.mesh.n_triangles),
             "collision_model": "VHS", "poisson_every": w.params["poisson_every"],
             "resort_every": w.params["resort_every"], "dt": w.params["dt"], "precision": args.precision,
+            "preconditioner": args.precond,
             "l2_policy": "inputs larger than L2 (particles 560 MB, mesh ~1.4 GB)",
             "timed_steps_start_at": args.warmup}
 
@@ -230,7 +281,9 @@ def run_gpu(args):
     st1 = eng.stats()
     prof = eng.profile()
     eng.profile_enable(False)
-    counts_fp64 = eng.triangle_counts()  # after W + K steps, for the mixed-form L1 comparison
+    counts_fp64 = eng.triangle_counts()  # after W + K steps, for the mixed-form comparison
+    state_fp64 = eng.particles() if not args.no_mixed else None
+    phi_fp64 = eng.potential() if not args.no_mixed else None
     ps = st1["particle_steps"] - st0["particle_steps"]
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -291,13 +344,14 @@ def run_gpu(args):
                "seconds": t_e2e, "note": "job-level: upload, K steps from step 0 (cold first Poisson solve), "
                                          "per-step stats read, download; host wall clock"}
 
+    eng.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, info = cpu_sample(w, min(args.cpu_sample, len(w.pos)), args.cpu_steps)
+        n_sample = min(args.cpu_sample or len(w.pos), len(w.pos))
+        steps = args.cpu_steps or args.steps
+        v, info = cpu_sample(w, n_sample, steps, args.warmup)
         cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
-               "sample": f"{min(args.cpu_sample, len(w.pos))} of {len(w.pos)} particles, {args.cpu_steps} "
-                         f"full-loop steps on the full mesh (one warm PCG solve)", "timed_s": info["timed_s"]}
-    eng.close()
+               "sample": cpu_sample_desc(w, n_sample, steps, args.warmup), "timed_s": info["timed_s"]}
 
     mixed = None
     if not args.no_mixed:
@@ -326,9 +380,17 @@ def run_gpu(args):
         mp = em.profile()
         cm = em.triangle_counts().astype(float)
         cf = counts_fp64.astype(float)
+        sm_state = em.particles()
+        phi_m = em.potential()
+        both = ((sm_state["flags"] & 1) != 0) & ((state_fp64["flags"] & 1) != 0)
+        d = sm_state["pos"][both] - state_fp64["pos"][both]
+        land_rms = float(np.sqrt(np.mean(np.sum(d * d, axis=1)))) if both.any() else None
+        phi_err = float(np.max(np.abs(phi_m - phi_fp64)) / max(np.max(np.abs(phi_fp64)), 1e-300))
         mval = (m1["particle_steps"] - m0["particle_steps"]) / (mms / 1e3)
         mixed = {"value": mval, "unit": UNIT, "ms_per_step": mms / args.steps, "speedup_vs_fp64": mval / value,
                  "l1_hist_error_vs_fp64": float(np.abs(cm - cf).sum() / max(cf.sum(), 1.0)),
+                 "landing_rms_m_vs_fp64": land_rms, "landed_in_both": int(both.sum()),
+                 "phi_max_rel_error_vs_fp64": phi_err,
                  "settled_fp64": int(cf.sum()), "settled_mixed": int(cm.sum()),
                  "breakdown_ms": {k: mp[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")},
                  "pcg_iters": mp["pcg_iters"],
@@ -336,6 +398,9 @@ def run_gpu(args):
                  "pcg_GBps": mp["pcg_bytes"] / (mp["pcg_ms"] / 1e3) / 1e9 if mp["pcg_ms"] > 0 else None,
                  "gpu_launches": mp["kernel_launches"], "dtype": "f32 state/push/SpMV, f64 refinement + sums"}
         em.close()
+    grad = None
+    if not args.no_grad and rank == 0:
+        grad = grad_leg(args, local)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -343,7 +408,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded workload generator)", "config": config_dict(args, w),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown, "mixed": mixed,
+            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown, "mixed": mixed, "grad": grad,
             "alive_particles": {"start": st0["n_alive"], "end": st1["n_alive"]},
             "cg_iters_last": st1["cg_iters_last"],
         }
@@ -362,8 +427,12 @@ def main():
     ap.add_argument("--particles", type=int, default=10_000_000)
     ap.add_argument("--cells", type=int, default=100)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--cpu-sample", type=int, default=1_000_000)
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "amg"],
+                    help="Poisson PCG preconditioner of the FP64 form")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU sample (0: all)")
+    ap.add_argument("--cpu-steps", type=int, default=0, help="timed CPU steps (0: --steps)")
+    ap.add_argument("--no-grad", action="store_true", help="skip the gradient leg")
+    ap.add_argument("--grad-particles", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")

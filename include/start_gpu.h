@@ -69,6 +69,15 @@ typedef enum spg_precision {
     SPG_MIXED = 1  /* FP32 tet-local state and push; FP32-SpMV PCG in FP64 refinement */
 } spg_precision;
 
+/* Preconditioner of the Poisson PCG. The reference preconditions Belos CG
+ * with MueLu (src/FiniteElementMethod/Solvers/MatrixEquationSolver.cpp:359-427),
+ * whose default is smoothed aggregation with Chebyshev smoothing. */
+typedef enum spg_preconditioner {
+    SPG_PRECOND_JACOBI = 0, /* diagonal scaling */
+    SPG_PRECOND_AMG = 1     /* smoothed-aggregation AMG V-cycle, degree-2 Jacobi-Chebyshev smoothing
+                               (FP64 form; the mixed form keeps Jacobi in its FP32 inner solve) */
+} spg_preconditioner;
+
 /* Particle flag bits returned by spg_get_particles. */
 #define SPG_FLAG_SETTLED 1u /* crossed a surface triangle; position = hit point */
 #define SPG_FLAG_LOST 2u    /* left the mesh through a face with no triangle, or walk cap */
@@ -110,7 +119,7 @@ typedef struct spg_params {
     int32_t cg_max_iter;      /* PCG iteration cap */
     double cg_rtol;           /* PCG stop: ||r||_2 <= cg_rtol * ||b||_2 */
     int32_t device;           /* CUDA device ordinal */
-    int32_t reserved0;
+    int32_t preconditioner;   /* spg_preconditioner: PCG preconditioner of the Poisson solve */
 } spg_params;
 
 typedef struct spg_stats {

@@ -97,7 +97,7 @@ def params_struct(params):
                     gas_mass=6.6335209e-26, gas_concentration=0.0, hs_diameter=3.6e-10, vhs_dref=4.17e-10,
                     omega=0.81, alpha=1.40, kT_ref=297.0 * 1.380658e-23, epsilon0=8.8541878128e-12,
                     min_velocity=10.0, bbox_expansion=1.01, seed=0, poisson_every=10, resort_every=20,
-                    max_crossings=4096, cg_max_iter=20000, cg_rtol=1e-10, device=0)
+                    max_crossings=4096, cg_max_iter=20000, cg_rtol=1e-10, device=0, preconditioner=0)
     defaults.update(dict(params))
     for k, v in defaults.items():
         setattr(p, k, v)

@@ -24,6 +24,7 @@ SPG_E_STATE = -8
 
 SPG_COLL_NONE, SPG_COLL_HS, SPG_COLL_VHS, SPG_COLL_VSS = 0, 1, 2, 3
 SPG_FP64, SPG_MIXED = 0, 1
+SPG_PRECOND_JACOBI, SPG_PRECOND_AMG = 0, 1
 SPG_FLAG_SETTLED, SPG_FLAG_LOST = 1, 2
 
 _pd = C.POINTER(C.c_double)
@@ -49,7 +50,7 @@ class Params(C.Structure):
         ("bbox_expansion", C.c_double), ("seed", C.c_uint64),
         ("poisson_every", C.c_int32), ("resort_every", C.c_int32),
         ("max_crossings", C.c_int32), ("cg_max_iter", C.c_int32), ("cg_rtol", C.c_double),
-        ("device", C.c_int32), ("reserved0", C.c_int32),
+        ("device", C.c_int32), ("preconditioner", C.c_int32),
     ]
 
     def as_dict(self):

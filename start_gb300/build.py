@@ -44,7 +44,9 @@ def _sources():
         ("kernels_mixed.cu", common_nv),
         ("noalloc.cu", common_nv),
         ("kernels_adjoint.cu", common_nv + ["--fmad=false"]),
+        ("kernels_amg.cu", common_nv),
         ("mesh_prep.cpp", common_cc + ["-fopenmp"]),
+        ("amg_setup.cpp", common_cc + ["-O3", "-fopenmp"]),
         ("capi.cpp", common_cc),
     ]
 
@@ -67,7 +69,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     """Build (if needed) and return the path of libstart_gpu.so."""
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + [PKG.parent / "include" / "start_gpu.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "start_gpu.h"]
     jobs, objs = [], []
     for src, flags in _sources():
         obj = BUILD / (src + ".o")

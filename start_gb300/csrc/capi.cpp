@@ -76,9 +76,17 @@ struct spg_handle {
     int fix_bits = 40;                        // deposit quantum 2^-fix_bits of one particle's charge
     PcgScalars *sc = nullptr;
     int pcg_blocks = 1;
+    PcgGrid grid64, grid32;
     // PCG iterations are replayed as a CUDA graph of kPcgChunk iterations
     // (3 kernels each); converged solves turn the remaining kernels into no-ops.
     cudaGraphExec_t pcg_graph = nullptr;
+    // AMG preconditioner (prm.preconditioner == SPG_PRECOND_AMG)
+    bool amg = false;
+    AmgDev amgd{};
+    std::vector<void *> amg_alloc;
+    std::vector<int64_t> amg_rows, amg_nnz;
+    int amg_launches = 0;         // kernel launches of one V-cycle
+    double amg_bytes = 0.0;       // algorithmic bytes of one V-cycle
 
     // mixed form (precision == SPG_MIXED)
     bool mixed = false;
@@ -230,9 +238,115 @@ PcgDev32 pcg_dev32(spg_handle *h) {
     f.q = h->q32;
     f.partials = h->partials32;
     f.sc = h->sc32;
-    f.blocks = h->pcg_blocks;
+    f.grid = h->grid32;
     return f;
 }
+
+// Builds the AMG hierarchy on the host and uploads it: every operator as
+// SELL-32 (level 0 uses the solver's matrix), D^-1, the Chebyshev constants
+// and the work vectors of each level, the dense inverse of the coarsest.
+int setup_amg(spg_handle *h, const HostMesh &hm) {
+    AmgHost ah;
+    std::string err;
+    int rc = amg_setup(hm.n_nodes, hm.row_ptr.data(), hm.col.data(), hm.val.data(), ah, err);
+    if (rc) return fail(h, rc, err);
+    const int L = int(ah.levels.size());
+    if (L > kAmgMaxLevels) return fail(h, SPG_E_INVALID, "amg: too many levels");
+    cudaStream_t s = h->stream;
+    auto keep = [&](void *p) { h->amg_alloc.push_back(p); };
+    auto up_sell = [&](const AmgCsr &M, DevSell &D) -> int {
+        std::vector<int64_t> sp;
+        std::vector<int32_t> sc;
+        std::vector<double> sv;
+        build_sell32(M.n, M.rp.data(), M.ci.data(), M.v.data(), sp, sc, sv);
+        int64_t *dsp = nullptr;
+        int32_t *dsc = nullptr;
+        double *dsv = nullptr;
+        CK(upload(&dsp, sp, s));
+        keep(dsp);
+        CK(upload(&dsc, sc, s));
+        keep(dsc);
+        CK(upload(&dsv, sv, s));
+        keep(dsv);
+        D.n = M.n;
+        D.slice_ptr = dsp;
+        D.scol = dsc;
+        D.sval = dsv;
+        return SPG_OK;
+    };
+    auto vec = [&](double **p, int64_t n) -> int {
+        CK(dalloc(p, std::max<int64_t>(n, 1)));
+        keep(*p);
+        return SPG_OK;
+    };
+    AmgDev &a = h->amgd;
+    a.levels = L;
+    h->amg_launches = 0;
+    h->amg_bytes = 0.0;
+    for (int l = 0; l < L; ++l) {
+        const AmgLevelHost &H = ah.levels[l];
+        AmgLevelDev &D = a.lev[l];
+        D.n = H.A.n;
+        h->amg_rows.push_back(H.A.n);
+        h->amg_nnz.push_back(int64_t(H.A.ci.size()));
+        if (l == 0) {
+            D.A.n = hm.n_nodes;
+            D.A.slice_ptr = h->slice_ptr;
+            D.A.scol = h->scol;
+            D.A.sval = h->sval;
+        } else if ((rc = up_sell(H.A, D.A))) {
+            return rc;
+        }
+        if (l < L - 1) {
+            if ((rc = up_sell(H.P, D.P)) || (rc = up_sell(H.R, D.R))) return rc;
+            double *dv = nullptr;
+            CK(upload(&dv, H.dinv, s));
+            keep(dv);
+            D.dinv = dv;
+            if ((rc = vec(&D.x[1], D.n)) || (rc = vec(&D.r, D.n)) || (rc = vec(&D.d, D.n))) return rc;
+            const double hi = H.lam, lo = H.lam / 30.0;
+            const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
+            const double sigma = theta / delta, rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
+            D.inv_theta = 1.0 / theta;
+            D.cheb_a = rho1 * rho0;
+            D.cheb_b = 2.0 * rho1 / delta;
+            const double nnzA = double(H.A.ci.size()), n = double(D.n);
+            const double nnzP = double(H.P.ci.size()), nc = double(H.P.m);
+            // cheb0 32n; 3 Chebyshev steps (12 nnz + 48 n); residual (12 nnz + 24 n);
+            // restriction (12 nnz(P) + 8 n + 8 nc); prolongation (12 nnz(P) + 16 n + 8 nc)
+            h->amg_bytes += 32.0 * n + 3.0 * (12.0 * nnzA + 48.0 * n) + (12.0 * nnzA + 24.0 * n) +
+                            2.0 * (12.0 * nnzP + 8.0 * nc) + 24.0 * n;
+            h->amg_launches += 7;
+        }
+        if (l > 0 && (rc = vec(&D.b, D.n))) return rc;
+        if (l > 0 && (rc = vec(&D.x[0], D.n))) return rc;
+    }
+    a.nc = ah.nc;
+    double *inv = nullptr;
+    CK(upload(&inv, ah.coarse_inv, s));
+    keep(inv);
+    a.coarse_inv = inv;
+    h->amg_launches += 1;
+    h->amg_bytes += 8.0 * double(ah.nc) * double(ah.nc + 2);
+    h->amg = true;
+    return SPG_OK;
+}
+
+// PCG setup and one iteration with the handle's preconditioner.
+void pcg_setup_any(spg_handle *h, const PcgDev &d, const double *b) {
+    if (h->amg)
+        launch_pcg_setup_amg(d, h->amgd, b, h->stream);
+    else
+        launch_pcg_setup(d, b, h->stream);
+}
+void pcg_iteration_any(spg_handle *h, PcgDev &d) {
+    if (h->amg)
+        launch_pcg_iteration_amg(d, h->amgd, h->stream);
+    else
+        launch_pcg_iteration(d, h->stream);
+}
+int pcg_iter_launches(const spg_handle *h) { return h->amg ? 4 + h->amg_launches : 3; }
+int pcg_chunk(const spg_handle *h) { return h->amg ? 2 : kPcgChunk; }
 
 // Allocates both particle buffers (and the walk queue) for n particles.
 int alloc_particles(spg_handle *h, int64_t n) {
@@ -349,7 +463,7 @@ PcgDev pcg_dev(spg_handle *h) {
     d.q = h->q;
     d.partials = h->partials;
     d.sc = h->sc;
-    d.blocks = h->pcg_blocks;
+    d.grid = h->grid64;
     return d;
 }
 
@@ -507,20 +621,21 @@ int do_solve64(spg_handle *h) {
     CK(cudaMemcpyAsync(h->sc, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     PcgDev d = pcg_dev(h);
     ev_begin(h, h->ev_pcg);
-    launch_pcg_setup(d, h->b, h->stream);
-    h->launches += 1;
+    pcg_setup_any(h, d, h->b);
+    h->launches += h->amg ? 2 + h->amg_launches : 1;
     PcgScalars hs{};
+    const int chunk = pcg_chunk(h);
     if (!h->pcg_graph) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < kPcgChunk; ++k) launch_pcg_iteration(d, h->stream);
+        for (int k = 0; k < chunk; ++k) pcg_iteration_any(h, d);
         CK(cudaStreamEndCapture(h->stream, &g));
         CK(cudaGraphInstantiate(&h->pcg_graph, g, 0));
         cudaGraphDestroy(g);
     }
     for (;;) {
         CK(cudaGraphLaunch(h->pcg_graph, h->stream));
-        h->launches += 3 * kPcgChunk;
+        h->launches += pcg_iter_launches(h) * chunk;
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         if (hs.converged) break;
@@ -528,7 +643,10 @@ int do_solve64(spg_handle *h) {
     ev_end(h, h->ev_pcg);
     if (h->prof) {
         h->pcg_iters_prof += hs.iters;
-        h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz) + 4.0 * double(n + 1) + 72.0 * double(n));
+        if (h->amg)  // spmv_dot 12 nnz + 24 n, update 48 n, V-cycle, r.z 16 n, p update 24 n
+            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz) + 112.0 * double(n) + h->amg_bytes);
+        else
+            h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz) + 4.0 * double(n + 1) + 72.0 * double(n));
     }
     return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
 }
@@ -662,6 +780,7 @@ int validate_params(const spg_params *p, std::string &msg) {
     else if (!(p->epsilon0 > 0.0)) msg = "epsilon0 must be > 0";
     else if (p->collision_model < SPG_COLL_NONE || p->collision_model > SPG_COLL_VSS) msg = "bad collision_model";
     else if (p->precision != SPG_FP64 && p->precision != SPG_MIXED) msg = "bad precision";
+    else if (p->preconditioner != SPG_PRECOND_JACOBI && p->preconditioner != SPG_PRECOND_AMG) msg = "bad preconditioner";
     else if (p->collision_model != SPG_COLL_NONE && !(p->gas_mass > 0.0)) msg = "gas_mass must be > 0";
     else if (p->collision_model != SPG_COLL_NONE && !(p->gas_concentration >= 0.0)) msg = "gas_concentration < 0";
     else if (p->collision_model == SPG_COLL_VSS && !(p->alpha > 0.0)) msg = "alpha must be > 0";
@@ -706,6 +825,7 @@ void spg_default_params(spg_params *p) {
     p->cg_max_iter = 20000;
     p->cg_rtol = 1e-10;
     p->device = 0;
+    p->preconditioner = SPG_PRECOND_JACOBI;
 }
 
 const char *spg_last_error(const spg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
@@ -776,6 +896,10 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
             CK(upload(&h->sval32, sv32, s));
         }
     }
+    if (h->prm.preconditioner == SPG_PRECOND_AMG && !h->mixed) {  // the mixed inner solve stays Jacobi
+        int rc = setup_amg(h, hm);
+        if (rc) return rc;
+    }
     {
         std::vector<int64_t> erp(hm.n_nodes + 1, 0);
         for (int32_t r : hm.elim_row) erp[r + 1]++;
@@ -836,9 +960,12 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(dalloc(&h->p, n));
     CK(dalloc(&h->q, n));
     h->pcg_blocks = pcg_blocks(n);
+    h->grid64 = pcg_grid64(n);
+    h->grid32 = pcg_grid32(n);
+    CK(cudaGetLastError());
     CK(dalloc(&h->partials, 3 * size_t(h->pcg_blocks)));
     CK(dalloc(&h->sc, 1));
-    CK(dalloc(&h->partials32, 3 * size_t(pcg_blocks(hm.n_nodes))));
+    CK(dalloc(&h->partials32, 3 * size_t(h->pcg_blocks)));
     CK(dalloc(&h->sc32, 1));
     CK(cudaMemsetAsync(h->sc32, 0, sizeof(PcgScalars), s));
     CK(cudaMemsetAsync(h->sc, 0, sizeof(PcgScalars), s));
@@ -870,6 +997,7 @@ int spg_destroy(spg_handle *h) {
                     h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch, h->walkq_n};
     for (void *ptr : ptrs) cudaFree(ptr);
     for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
+    for (void *ptr : h->amg_alloc) cudaFree(ptr);
     if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
     if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
     for (auto &P : h->ckpt)
@@ -1324,10 +1452,10 @@ int solve_into(spg_handle *h, double *b, double *x, int32_t *iters) {
     CK(cudaMemcpyAsync(h->sc, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     PcgDev d = pcg_dev(h);
     d.x = x;
-    launch_pcg_setup(d, b, h->stream);
+    pcg_setup_any(h, d, b);
     PcgScalars hs{};
     for (int chunk = 0;; ++chunk) {
-        for (int k = 0; k < kPcgChunk; ++k) launch_pcg_iteration(d, h->stream);
+        for (int k = 0; k < pcg_chunk(h); ++k) pcg_iteration_any(h, d);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));

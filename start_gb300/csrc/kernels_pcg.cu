@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "sell.cuh"
 #include "spg_internal.h"
 
 namespace spg {
@@ -28,25 +29,33 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 // Block sum of two values into partials[2*blockIdx.x + {0,1}]; returns true in
 // thread 0 of the last block to finish, whose totals are then in tot[0..1].
-__device__ bool block_reduce2(double a, double b, double *partials, PcgScalars *sc, double tot[2]) {
-    __shared__ double sa[kThreads / 32], sb[kThreads / 32];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    a = warp_sum(a);
-    b = warp_sum(b);
-    if (lane == 0) {
-        sa[wid] = a;
-        sb[wid] = b;
-    }
+// FP64 adds issue per warp at the FP64 rate, so the block sum runs in warp 0
+// only: the 256 per-thread values go through shared memory, lane l adds the
+// eight values l, l+32, ..., l+224 in that order and a five-level shuffle
+// tree finishes (a fixed order, so the sums are deterministic for a grid).
+__device__ __forceinline__ void block_sum2(double &a, double &b) {
+    __shared__ double sa[kThreads], sb[kThreads];
+    sa[threadIdx.x] = a;
+    sb[threadIdx.x] = b;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double ta = 0.0, tb = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) {
-            ta += sa[w];
-            tb += sb[w];
+    if (threadIdx.x < 32) {
+        double ta = sa[threadIdx.x], tb = sb[threadIdx.x];
+#pragma unroll
+        for (int w = 1; w < kThreads / 32; ++w) {
+            ta += sa[threadIdx.x + 32 * w];
+            tb += sb[threadIdx.x + 32 * w];
         }
-        partials[2 * blockIdx.x] = ta;
-        partials[2 * blockIdx.x + 1] = tb;
+        a = warp_sum(ta);
+        b = warp_sum(tb);
+    }
+}
+
+__device__ bool block_reduce2(double a, double b, double *partials, PcgScalars *sc, double tot[2]) {
+    __shared__ bool last;
+    block_sum2(a, b);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = a;
+        partials[2 * blockIdx.x + 1] = b;
         __threadfence();
         const unsigned ticket = atomicInc(&sc->ticket, gridDim.x - 1);
         last = ticket == gridDim.x - 1;
@@ -60,50 +69,16 @@ __device__ bool block_reduce2(double a, double b, double *partials, PcgScalars *
         ta += __ldcg(partials + 2 * k);
         tb += __ldcg(partials + 2 * k + 1);
     }
-    ta = warp_sum(ta);
-    tb = warp_sum(tb);
-    __syncthreads();
-    if (lane == 0) {
-        sa[wid] = ta;
-        sb[wid] = tb;
-    }
-    __syncthreads();
+    __syncthreads();  // the shared buffers of block_sum2 are reused
+    block_sum2(ta, tb);
     if (threadIdx.x != 0) return false;
-    ta = 0.0;
-    tb = 0.0;
-    for (int w = 0; w < kThreads / 32; ++w) {
-        ta += sa[w];
-        tb += sb[w];
-    }
     tot[0] = ta;
     tot[1] = tb;
     return true;
 }
 
-// Row i of A x in SELL-32 storage: rows are grouped in slices of 32 (one
-// warp), each slice padded to its longest row and stored column-major, so
-// lane l of a warp reads entry j of its row at slice_ptr[s] + 32 j + l and a
-// warp's 32 loads of one j are contiguous. Padding entries have value 0.
-// Four entries per trip with their loads issued before the FMAs and two
-// accumulators, so each thread keeps several gathers in flight.
 __device__ __forceinline__ double spmv_row(const PcgDev &d, const double *__restrict__ x, int64_t i) {
-    const int64_t s = i >> 5;
-    int64_t k = __ldg(d.slice_ptr + s) + (i & 31);
-    const int64_t k1 = __ldg(d.slice_ptr + s + 1);
-    double a0 = 0.0, a1 = 0.0;
-    for (; k + 96 < k1; k += 128) {
-        const int32_t c0 = __ldg(d.scol + k), c1 = __ldg(d.scol + k + 32);
-        const int32_t c2 = __ldg(d.scol + k + 64), c3 = __ldg(d.scol + k + 96);
-        const double v0 = __ldg(d.sval + k), v1 = __ldg(d.sval + k + 32);
-        const double v2 = __ldg(d.sval + k + 64), v3 = __ldg(d.sval + k + 96);
-        const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-        a0 = fma(v0, x0, a0);
-        a1 = fma(v1, x1, a1);
-        a0 = fma(v2, x2, a0);
-        a1 = fma(v3, x3, a1);
-    }
-    for (; k < k1; k += 32) a0 = fma(__ldg(d.sval + k), __ldg(x + __ldg(d.scol + k)), a0);
-    return a0 + a1;
+    return spmv_row_sell<double>(d.slice_ptr, d.scol, d.sval, x, i);
 }
 
 __global__ void k_rhs(const double *__restrict__ node_q, double inv_eps0, const double *__restrict__ lift,
@@ -224,6 +199,71 @@ __global__ void __launch_bounds__(kThreads) k_pupdate(PcgDev d) {
         d.p[i] = d.z[i] + beta * d.p[i];
 }
 
+// ------------------------------------------------- PCG with the AMG V-cycle
+// r = b - A x; bb = b.b, rr = r.r (z = M^-1 r follows as a V-cycle)
+__global__ void __launch_bounds__(kThreads) k_setup_amg(PcgDev d, const double *__restrict__ b) {
+    double bb = 0.0, rr = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
+        const double bi = b[i];
+        const double ri = bi - spmv_row(d, d.x, i);
+        d.r[i] = ri;
+        bb += bi * bi;
+        rr += ri * ri;
+    }
+    double tot[2];
+    if (block_reduce2(rr, bb, d.partials, d.sc, tot)) {
+        PcgScalars *sc = d.sc;
+        sc->rr = tot[0];
+        sc->bb = tot[1];
+        sc->tol2 = sc->tol2 * tot[1];  // rtol^2 -> rtol^2 ||b||^2
+        sc->iters = 0;
+        sc->converged = (tot[0] <= sc->tol2 || tot[1] == 0.0) ? 1 : 0;
+        sc->alpha = 0.0;
+        sc->beta = 0.0;
+        sc->rz = 0.0;
+    }
+}
+
+// x += alpha p; r -= alpha q; rr = r.r and the stop test
+__global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d) {
+    if (d.sc->converged) return;
+    const double alpha = d.sc->alpha;
+    double rr = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
+        d.x[i] += alpha * d.p[i];
+        const double ri = d.r[i] - alpha * d.q[i];
+        d.r[i] = ri;
+        rr += ri * ri;
+    }
+    double tot[2];
+    if (block_reduce2(rr, 0.0, d.partials, d.sc, tot)) {
+        PcgScalars *sc = d.sc;
+        sc->iters += 1;
+        sc->rr = tot[0];
+        if (tot[0] <= sc->tol2)
+            sc->converged = 1;
+        else if (sc->iters >= sc->max_iter)
+            sc->converged = 2;
+    }
+}
+
+// rz' = r.z (z from the V-cycle); first: p = z; else beta = rz'/rz
+__global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, int first) {
+    if (d.sc->converged) return;
+    double rz = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
+        const double zi = d.z[i];
+        rz += d.r[i] * zi;
+        if (first) d.p[i] = zi;
+    }
+    double tot[2];
+    if (block_reduce2(rz, 0.0, d.partials, d.sc, tot)) {
+        PcgScalars *sc = d.sc;
+        if (!first) sc->beta = tot[0] / sc->rz;
+        sc->rz = tot[0];
+    }
+}
+
 // ------------------------------------------------- mixed precision (SPG_MIXED)
 // FP32 SpMV PCG for the correction e in A e = r, inside FP64 iterative
 // refinement x <- x + e on r = b - A x (FP64 SpMV). Dot products are FP64:
@@ -231,23 +271,7 @@ __global__ void __launch_bounds__(kThreads) k_pupdate(PcgDev d) {
 // further accumulation is FP64.
 
 __device__ __forceinline__ float spmv_row32(const PcgDev32 &d, const float *__restrict__ x, int64_t i) {
-    const int64_t s = i >> 5;
-    int64_t k = __ldg(d.slice_ptr + s) + (i & 31);
-    const int64_t k1 = __ldg(d.slice_ptr + s + 1);
-    float a0 = 0.0f, a1 = 0.0f;
-    for (; k + 96 < k1; k += 128) {
-        const int32_t c0 = __ldg(d.scol + k), c1 = __ldg(d.scol + k + 32);
-        const int32_t c2 = __ldg(d.scol + k + 64), c3 = __ldg(d.scol + k + 96);
-        const float v0 = __ldg(d.sval + k), v1 = __ldg(d.sval + k + 32);
-        const float v2 = __ldg(d.sval + k + 64), v3 = __ldg(d.sval + k + 96);
-        const float x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-        a0 = fmaf(v0, x0, a0);
-        a1 = fmaf(v1, x1, a1);
-        a0 = fmaf(v2, x2, a0);
-        a1 = fmaf(v3, x3, a1);
-    }
-    for (; k < k1; k += 32) a0 = fmaf(__ldg(d.sval + k), __ldg(x + __ldg(d.scol + k)), a0);
-    return a0 + a1;
+    return spmv_row_sell<float>(d.slice_ptr, d.scol, d.sval, x, i);
 }
 
 __device__ __forceinline__ float warp_sumf(float v) {
@@ -378,12 +402,42 @@ __global__ void k_refine_apply(double *__restrict__ x, const float *__restrict__
 
 }  // namespace
 
-// Four 256-thread blocks per SM: each thread then handles several rows, so
-// the FP64 shuffle reductions of the dot products (which issue per warp at
-// the FP64 rate) are amortised over several rows.
+// Each kernel runs SMs x (its resident 256-thread blocks per SM) blocks, one
+// wave; each thread then handles several rows of a large system, so the FP64
+// shuffle reductions of the dot products (which issue per warp at the FP64
+// rate) are amortised over several rows.
+static int sm_count_attr() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
 int pcg_blocks(int64_t n) {
     const int64_t want = (n + kThreads - 1) / kThreads;
-    return int(want < 152 * 4 ? (want < 1 ? 1 : want) : 152 * 4);
+    const int64_t cap = int64_t(sm_count_attr()) * (2048 / kThreads);
+    return int(want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
+namespace {
+template <class K>
+int wave(K kernel, int64_t n) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+    const int64_t cap = int64_t(sm_count_attr()) * (per_sm > 0 ? per_sm : 1);
+    const int64_t want = (n + kThreads - 1) / kThreads;
+    const int g = int(want < cap ? (want < 1 ? 1 : want) : cap);
+    return g < pcg_blocks(n) ? g : pcg_blocks(n);  // the partials hold pcg_blocks(n) blocks
+}
+}  // namespace
+
+PcgGrid pcg_grid64(int64_t n) {
+    PcgGrid g;
+    g.setup = wave(k_setup, n);
+    g.spmv = wave(k_spmv_dot, n);
+    g.update = wave(k_update, n);
+    g.pupdate = wave(k_pupdate, n);
+    return g;
 }
 
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
@@ -396,23 +450,46 @@ void launch_node_rho(const double *node_q, const double *dual_vol, double *rho, 
 }
 
 void launch_pcg_setup(const PcgDev &d, const double *b, cudaStream_t s) {
-    k_setup<<<d.blocks, kThreads, 0, s>>>(d, b);
+    k_setup<<<d.grid.setup, kThreads, 0, s>>>(d, b);
+}
+
+void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s) {
+    k_setup_amg<<<d.grid.setup, kThreads, 0, s>>>(d, b);
+    launch_amg_vcycle(a, d.r, d.z, d.sc, s);
+    k_rz_amg<<<d.grid.update, kThreads, 0, s>>>(d, 1);
+}
+
+void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s) {
+    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
+    k_update_amg<<<d.grid.update, kThreads, 0, s>>>(d);
+    launch_amg_vcycle(a, d.r, d.z, d.sc, s);
+    k_rz_amg<<<d.grid.update, kThreads, 0, s>>>(d, 0);
+    k_pupdate<<<d.grid.pupdate, kThreads, 0, s>>>(d);
 }
 
 void launch_pcg_iteration(PcgDev &d, cudaStream_t s) {
-    k_spmv_dot<<<d.blocks, kThreads, 0, s>>>(d);
-    k_update<<<d.blocks, kThreads, 0, s>>>(d);
-    k_pupdate<<<d.blocks, kThreads, 0, s>>>(d);
+    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
+    k_update<<<d.grid.update, kThreads, 0, s>>>(d);
+    k_pupdate<<<d.grid.pupdate, kThreads, 0, s>>>(d);
 }
 
-void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val,
-                  std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval) {
+// Entries that are exactly zero off the diagonal are left out (the P1
+// stiffness of a Kuhn-split lattice is the 7-point stencil: 8 of its 15
+// structural couplings per row are exact zeros); a product with an exact
+// zero adds nothing to a sum, so A x is unchanged.
+template <class RP>
+void build_sell32_t(int64_t n, const RP *row_ptr, const int32_t *col, const double *val,
+                    std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval) {
+    auto kept = [&](int64_t r, int64_t k) { return val[k] != 0.0 || col[k] == r; };
+    std::vector<int64_t> len(n, 0);
+    for (int64_t r = 0; r < n; ++r)
+        for (int64_t k = int64_t(row_ptr[r]); k < int64_t(row_ptr[r + 1]); ++k) len[r] += kept(r, k) ? 1 : 0;
     const int64_t ns = (n + 31) / 32;
     slice_ptr.assign(ns + 1, 0);
     for (int64_t sl = 0; sl < ns; ++sl) {
-        int32_t w = 0;
-        for (int64_t r = sl * 32; r < std::min(n, sl * 32 + 32); ++r) w = std::max(w, row_ptr[r + 1] - row_ptr[r]);
-        slice_ptr[sl + 1] = slice_ptr[sl] + 32 * int64_t(w);
+        int64_t w = 0;
+        for (int64_t r = sl * 32; r < std::min(n, sl * 32 + 32); ++r) w = std::max(w, len[r]);
+        slice_ptr[sl + 1] = slice_ptr[sl] + 32 * w;
     }
     scol.assign(slice_ptr[ns], 0);
     sval.assign(slice_ptr[ns], 0.0);
@@ -420,19 +497,35 @@ void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const d
         const int64_t w = (slice_ptr[sl + 1] - slice_ptr[sl]) / 32;
         for (int64_t l = 0; l < 32; ++l) {
             const int64_t r = sl * 32 + l;
-            const int32_t len = r < n ? row_ptr[r + 1] - row_ptr[r] : 0;
-            for (int64_t j = 0; j < w; ++j) {
-                const int64_t k = slice_ptr[sl] + 32 * j + l;
-                if (j < len) {
-                    scol[k] = col[row_ptr[r] + j];
-                    sval[k] = val[row_ptr[r] + j];
-                } else {
-                    scol[k] = r < n ? int32_t(r) : 0;
-                    sval[k] = 0.0;
+            int64_t j = 0;
+            int32_t first = 0;
+            if (r < n)
+                for (int64_t k = int64_t(row_ptr[r]); k < int64_t(row_ptr[r + 1]); ++k) {
+                    if (!kept(r, k)) continue;
+                    const int64_t o = slice_ptr[sl] + 32 * j + l;
+                    scol[o] = col[k];
+                    sval[o] = val[k];
+                    if (j == 0) first = col[k];
+                    ++j;
                 }
+            // padding: value 0 at a column the row already reads (or column
+            // 0), always inside x also for a rectangular matrix
+            for (; j < w; ++j) {
+                const int64_t o = slice_ptr[sl] + 32 * j + l;
+                scol[o] = first;
+                sval[o] = 0.0;
             }
         }
     }
+}
+
+void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val,
+                  std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval) {
+    build_sell32_t(n, row_ptr, col, val, slice_ptr, scol, sval);
+}
+void build_sell32(int64_t n, const int64_t *row_ptr, const int32_t *col, const double *val,
+                  std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval) {
+    build_sell32_t(n, row_ptr, col, val, slice_ptr, scol, sval);
 }
 
 }  // namespace spg
@@ -440,13 +533,22 @@ void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const d
 namespace spg {
 
 void launch_refine_setup(const PcgDev &d, const PcgDev32 &f, const double *b, cudaStream_t s) {
-    k_refine_setup<<<d.blocks, kThreads, 0, s>>>(d, f, b);
+    k_refine_setup<<<f.grid.setup, kThreads, 0, s>>>(d, f, b);
 }
 
 void launch_pcg32_iteration(PcgDev32 &f, cudaStream_t s) {
-    k_spmv_dot32<<<f.blocks, kThreads, 0, s>>>(f);
-    k_update32<<<f.blocks, kThreads, 0, s>>>(f);
-    k_pupdate32<<<f.blocks, kThreads, 0, s>>>(f);
+    k_spmv_dot32<<<f.grid.spmv, kThreads, 0, s>>>(f);
+    k_update32<<<f.grid.update, kThreads, 0, s>>>(f);
+    k_pupdate32<<<f.grid.pupdate, kThreads, 0, s>>>(f);
+}
+
+PcgGrid pcg_grid32(int64_t n) {
+    PcgGrid g;
+    g.setup = wave(k_refine_setup, n);
+    g.spmv = wave(k_spmv_dot32, n);
+    g.update = wave(k_update32, n);
+    g.pupdate = wave(k_pupdate32, n);
+    return g;
 }
 
 void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s) {

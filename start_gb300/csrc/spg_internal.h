@@ -265,6 +265,11 @@ struct PcgScalars {
     unsigned int ticket;
     unsigned int pad2;
 };
+// Grid of each PCG kernel: SMs x resident blocks per SM (occupancy of that
+// kernel), capped by the rows; every kernel loops over rows grid-stride.
+struct PcgGrid {
+    int setup = 1, spmv = 1, update = 1, pupdate = 1;
+};
 struct PcgDev {
     int64_t n;
     const int32_t *row_ptr, *col;
@@ -275,7 +280,7 @@ struct PcgDev {
     double *x, *r, *z, *p, *p2, *q;
     double *partials;  // 3 doubles per block
     PcgScalars *sc;
-    int blocks;
+    PcgGrid grid;
 };
 struct PcgDev32 {
     int64_t n;
@@ -286,9 +291,12 @@ struct PcgDev32 {
     float *e, *r, *z, *p, *q;
     double *partials;  // 3 doubles per block (separate from the FP64 solver's)
     PcgScalars *sc;
-    int blocks;
+    PcgGrid grid;
 };
+// Upper bound of any PCG grid (partials sizing) and the per-kernel grids.
 int pcg_blocks(int64_t n);
+PcgGrid pcg_grid64(int64_t n);
+PcgGrid pcg_grid32(int64_t n);
 // Mixed-precision solve pieces (kernels_pcg.cu).
 void launch_refine_setup(const PcgDev &d, const PcgDev32 &f, const double *b, cudaStream_t s);
 void launch_pcg32_iteration(PcgDev32 &f, cudaStream_t s);
@@ -296,6 +304,61 @@ void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s);
 // CSR -> SELL-32 (slices of 32 rows, column-major, zero padding).
 void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val,
                   std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval);
+void build_sell32(int64_t n, const int64_t *row_ptr, const int32_t *col, const double *val,
+                  std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval);
+
+// ---------------------------------------------------------------- AMG
+// Smoothed-aggregation hierarchy (amg_setup.cpp) and its GPU V-cycle
+// (kernels_amg.cu), the preconditioner of SPG_PRECOND_AMG.
+struct AmgCsr {
+    int64_t n = 0, m = 0;
+    std::vector<int64_t> rp;
+    std::vector<int32_t> ci;
+    std::vector<double> v;
+};
+struct AmgLevelHost {
+    AmgCsr A, P, R;  // P, R empty on the coarsest level
+    std::vector<double> dinv;
+    double lam = 0.0;  // upper bound of the spectrum of D^-1 A
+};
+struct AmgHost {
+    std::vector<AmgLevelHost> levels;  // levels[0].A is the solver's matrix
+    int64_t nc = 0;                    // rows of the coarsest level
+    std::vector<double> coarse_inv;    // its dense inverse, row-major
+};
+int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val, AmgHost &out,
+              std::string &err);
+
+constexpr int kAmgMaxLevels = 12;
+struct DevSell {
+    int64_t n = 0;
+    const int64_t *slice_ptr = nullptr;
+    const int32_t *scol = nullptr;
+    const double *sval = nullptr;
+};
+// One level of the V-cycle on the device. Chebyshev smoothing of degree 2
+// on D^-1 A over [lam/30, lam]: theta = (hi+lo)/2, delta = (hi-lo)/2.
+struct AmgLevelDev {
+    int64_t n = 0;
+    DevSell A, P, R;       // P: n x n_next, R: n_next x n
+    const double *dinv = nullptr;
+    double *x[2] = {nullptr, nullptr};  // iterate ping-pong
+    double *b = nullptr, *r = nullptr, *d = nullptr;
+    double inv_theta = 0.0, cheb_a = 0.0, cheb_b = 0.0;  // step 2: d = a d + b D^-1 r
+};
+struct AmgDev {
+    int levels = 0;  // including the coarsest (dense) level
+    AmgLevelDev lev[kAmgMaxLevels];
+    int64_t nc = 0;
+    const double *coarse_inv = nullptr;
+};
+// z = M^-1 r by one V-cycle (level 0 vectors: b = r, x[0] = z, x[1] scratch);
+// every kernel returns at once when sc->converged is set.
+void launch_amg_vcycle(const AmgDev &a, const double *r, double *z, const PcgScalars *sc, cudaStream_t s);
+// PCG with the V-cycle: setup and one iteration (spmv_dot, update, V-cycle,
+// r.z and beta, p update).
+void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s);
+void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
                     const double *dir_value, double *b, int64_t n, cudaStream_t s);

@@ -54,7 +54,8 @@ def _base_params(**kw):
     p = dict(dt=1e-8, charge=E_CHARGE, mass=TI_MASS, weight=1.0, collision_model=0, precision=0,
              gas_mass=AR_MASS, gas_concentration=0.0, hs_diameter=3.6e-10, vhs_dref=4.17e-10, omega=0.81,
              alpha=1.40, kT_ref=KT_REF, epsilon0=EPS0, min_velocity=10.0, bbox_expansion=1.01, seed=0,
-             poisson_every=10, resort_every=20, max_crossings=4096, cg_max_iter=20000, cg_rtol=1e-10, device=0)
+             poisson_every=10, resort_every=20, max_crossings=4096, cg_max_iter=20000, cg_rtol=1e-10, device=0,
+             preconditioner=0)
     p.update(kw)
     return p
 

@@ -60,16 +60,18 @@ def test_gradient_matches_oracle(built, collisions):
 
 
 def test_checkpoint_interval_does_not_change_gradient(built):
-    """Recompute from checkpoints every 32 steps gives the same gradient as
-    keeping one window per step (bit-identical forward replay)."""
+    """Recompute from checkpoints every 32 steps gives the gradient of 7-step
+    windows: the forward replay is bit-identical, only the order of the FP64
+    atomic sums into dJ/dE differs."""
     p = _gpu_problem(2000, collisions=True)
     p.forward(V0, A0)
     g32 = p.engine.grad_backward(particles=True)
     p.every = 7
     p.forward(V0, A0)
     g7 = p.engine.grad_backward(particles=True)
-    for a, b in zip(g32[:3], g7[:3]):
+    for a, b in zip(g32[1:3], g7[1:3]):  # per-particle adjoints do not go through atomics
         assert np.array_equal(a, b)
+    assert np.allclose(g32[0], g7[0], rtol=0, atol=1e-12 * np.abs(g32[0]).max())
     p.close()
 
 
