@@ -75,7 +75,7 @@ typedef enum spg_precision {
 typedef enum spg_preconditioner {
     SPG_PRECOND_JACOBI = 0, /* diagonal scaling */
     SPG_PRECOND_AMG = 1     /* smoothed-aggregation AMG V-cycle, degree-2 Jacobi-Chebyshev smoothing
-                               (FP64 form; the mixed form keeps Jacobi in its FP32 inner solve) */
+                               (FP64 in the plain form, FP32 in the mixed form's inner solve) */
 } spg_preconditioner;
 
 /* Particle flag bits returned by spg_get_particles. */

@@ -11,7 +11,8 @@
 //     aggregate and stay on the fine level;
 //   * tentative prolongator: the normalised constant on each aggregate;
 //   * P = (I - omega D^-1 A) T with omega = 4 / (3 lambda_max(D^-1 A));
-//   * A_c = P^T A P, R = P^T; levels until at most kCoarseRows rows remain;
+//   * A_c = P^T A P (weak couplings optionally lumped onto the diagonal),
+//     R = P^T; levels until at most AmgOptions::coarse_rows rows remain;
 //   * the coarsest operator is inverted densely (Cholesky).
 // lambda_max comes from 30 power iterations on D^-1 A (times 1.1), the same
 // bound the Chebyshev smoother uses.
@@ -29,8 +30,6 @@ namespace spg {
 
 namespace {
 
-constexpr double kTheta = 0.08;
-constexpr int64_t kCoarseRows = 600;
 constexpr int kMaxLevels = 12;
 constexpr int kPowerIters = 30;
 
@@ -147,7 +146,7 @@ double lambda_max(const AmgCsr &A, const std::vector<double> &dinv) {
 
 // Aggregates of the strength graph; agg[i] = -1 for rows with no strong
 // neighbour. Returns the number of aggregates.
-int64_t aggregate(const AmgCsr &A, std::vector<int64_t> &agg) {
+int64_t aggregate(const AmgCsr &A, double theta, std::vector<int64_t> &agg) {
     const int64_t n = A.n;
     std::vector<double> d(n, 0.0);
     for (int64_t i = 0; i < n; ++i)
@@ -159,7 +158,7 @@ int64_t aggregate(const AmgCsr &A, std::vector<int64_t> &agg) {
     for (int64_t i = 0; i < n; ++i) {
         for (int64_t k = A.rp[i]; k < A.rp[i + 1]; ++k) {
             const int32_t j = A.ci[k];
-            if (j != i && std::fabs(A.v[k]) >= kTheta * std::sqrt(d[i] * d[j])) sci.push_back(j);
+            if (j != i && std::fabs(A.v[k]) >= theta * std::sqrt(d[i] * d[j])) sci.push_back(j);
         }
         srp[i + 1] = int64_t(sci.size());
     }
@@ -204,6 +203,40 @@ int64_t aggregate(const AmgCsr &A, std::vector<int64_t> &agg) {
     return na;
 }
 
+// Moves the weak couplings |a_ij| < eps sqrt(|a_ii a_jj|) of a coarse operator
+// onto the diagonal (row sums, hence the constant near-null space, are kept;
+// the criterion is symmetric, so the operator stays symmetric).
+void filter_weak(AmgCsr &A, double eps) {
+    std::vector<double> d(A.n, 0.0);
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t k = A.rp[i]; k < A.rp[i + 1]; ++k)
+            if (A.ci[k] == i) d[i] = A.v[k];
+    std::vector<int64_t> rp(A.n + 1, 0);
+    int64_t o = 0;
+    for (int64_t i = 0; i < A.n; ++i) {
+        double lump = 0.0;
+        const int64_t start = o;
+        int64_t diag = -1;
+        for (int64_t k = A.rp[i]; k < A.rp[i + 1]; ++k) {
+            const int32_t j = A.ci[k];
+            if (j != i && std::fabs(A.v[k]) < eps * std::sqrt(std::fabs(d[i] * d[j]))) {
+                lump += A.v[k];
+                continue;
+            }
+            if (j == i) diag = o;
+            A.ci[o] = j;
+            A.v[o] = A.v[k];
+            ++o;
+        }
+        if (diag >= 0) A.v[diag] += lump;
+        (void)start;
+        rp[i + 1] = o;
+    }
+    A.rp.swap(rp);
+    A.ci.resize(o);
+    A.v.resize(o);
+}
+
 // In-place Cholesky of a dense SPD matrix (lower), then its inverse.
 bool dense_inverse(int64_t n, std::vector<double> &a, std::vector<double> &inv) {
     for (int64_t j = 0; j < n; ++j) {
@@ -241,7 +274,7 @@ bool dense_inverse(int64_t n, std::vector<double> &a, std::vector<double> &inv) 
 }  // namespace
 
 int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val, AmgHost &out,
-              std::string &err) {
+              std::string &err, const AmgOptions &opt) {
     out = AmgHost{};
     AmgCsr A;
     A.n = A.m = n;
@@ -256,7 +289,7 @@ int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const doubl
             for (int64_t k = A.rp[i]; k < A.rp[i + 1]; ++k)
                 if (A.ci[k] == i) L.dinv[i] = A.v[k] != 0.0 ? 1.0 / A.v[k] : 0.0;
         L.lam = 1.1 * lambda_max(A, L.dinv);
-        if (A.n <= kCoarseRows) {
+        if (A.n <= opt.coarse_rows) {
             // coarsest level: dense inverse
             std::vector<double> dense(A.n * A.n, 0.0);
             for (int64_t i = 0; i < A.n; ++i)
@@ -271,9 +304,9 @@ int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const doubl
             return SPG_OK;
         }
         std::vector<int64_t> agg;
-        const int64_t na = aggregate(A, agg);
+        const int64_t na = aggregate(A, opt.theta, agg);
         if (na == 0 || na * 5 > A.n * 4) {  // no coarsening progress: stop here with a dense coarse level
-            if (A.n > 8 * kCoarseRows) {
+            if (A.n > 8 * opt.coarse_rows) {
                 err = "amg: aggregation stalled at " + std::to_string(A.n) + " rows";
                 return SPG_E_INVALID;
             }
@@ -304,10 +337,10 @@ int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const doubl
                 T.v.push_back(1.0 / std::sqrt(double(size[agg[i]])));
             }
         }
-        // P = T - omega D^-1 A T
+        // P = T - omega D^-1 A T (P = T past opt.smooth_levels)
         AmgCsr AT;
         spgemm(A, T, AT);
-        const double omega = 4.0 / (3.0 * L.lam);
+        const double omega = lev < opt.smooth_levels ? 4.0 / (3.0 * L.lam) : 0.0;
         AmgCsr P;
         P.n = A.n;
         P.m = na;
@@ -345,6 +378,7 @@ int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const doubl
         spgemm(A, P, AP);
         spgemm(R, AP, Ac);
         drop_zeros(Ac);
+        if (opt.filter > 0.0) filter_weak(Ac, opt.filter);
         L.A = std::move(A);
         L.P = std::move(P);
         L.R = std::move(R);

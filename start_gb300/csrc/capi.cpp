@@ -28,6 +28,10 @@ constexpr int kPcgChunk = 8;
 // FP32 matrix can resolve for kappa ~ 1e4), at most this many inner
 // iterations per correction and outer refinement steps per solve.
 constexpr double kInnerRtol = 1e-4;
+// with the FP32 V-cycle the inner solve converges in a few iterations, so it
+// goes further per outer step (FP32 still resolves a 1e-5 reduction)
+constexpr double kInnerRtolAmg = 1e-5;
+constexpr int kInnerMaxIterAmg = 60;
 constexpr int kInnerMaxIter = 2000;
 constexpr int kOuterMax = 40;
 
@@ -63,6 +67,7 @@ struct spg_handle {
     int32_t *scol = nullptr;
     double *sval = nullptr;
     int64_t sell_entries = 0;
+    int64_t nnz_kept = 0;  // stiffness entries in the device format (exact zeros off the diagonal dropped)
     double *val = nullptr, *inv_diag = nullptr, *dir_value = nullptr, *lift = nullptr, *dual_vol = nullptr;
     uint8_t *is_dir = nullptr;
     int32_t *vox_seed = nullptr;
@@ -81,8 +86,9 @@ struct spg_handle {
     // (3 kernels each); converged solves turn the remaining kernels into no-ops.
     cudaGraphExec_t pcg_graph = nullptr;
     // AMG preconditioner (prm.preconditioner == SPG_PRECOND_AMG)
-    bool amg = false;
+    bool amg = false, amg32 = false;
     AmgDev amgd{};
+    AmgDev32 amgd32{};
     std::vector<void *> amg_alloc;
     std::vector<int64_t> amg_rows, amg_nnz;
     int amg_launches = 0;         // kernel launches of one V-cycle
@@ -242,31 +248,42 @@ PcgDev32 pcg_dev32(spg_handle *h) {
     return f;
 }
 
-// Builds the AMG hierarchy on the host and uploads it: every operator as
-// SELL-32 (level 0 uses the solver's matrix), D^-1, the Chebyshev constants
-// and the work vectors of each level, the dense inverse of the coarsest.
-int setup_amg(spg_handle *h, const HostMesh &hm) {
-    AmgHost ah;
-    std::string err;
-    int rc = amg_setup(hm.n_nodes, hm.row_ptr.data(), hm.col.data(), hm.val.data(), ah, err);
-    if (rc) return fail(h, rc, err);
+// Uploads an AMG hierarchy in value type T: every operator as SELL-32 or
+// CSR with g lanes per row (level 0 uses the solver's matrix, sval0), D^-1,
+// the Chebyshev constants and the work vectors of each level, the dense
+// inverse of the coarsest. Returns the V-cycle's launches and bytes.
+template <class T>
+int upload_amg(spg_handle *h, const AmgHost &ah, const T *sval0, AmgDevT<T> &a) {
     const int L = int(ah.levels.size());
     if (L > kAmgMaxLevels) return fail(h, SPG_E_INVALID, "amg: too many levels");
     cudaStream_t s = h->stream;
+    int rc;
     auto keep = [&](void *p) { h->amg_alloc.push_back(p); };
-    auto up_sell = [&](const AmgCsr &M, DevSell &D) -> int {
+    auto conv = [](const std::vector<double> &v) { return std::vector<T>(v.begin(), v.end()); };
+    // short rows: SELL-32, one thread per row; long rows: CSR, g lanes per row
+    auto up_mat = [&](const AmgCsr &M, DevSellT<T> &D) -> int {
         std::vector<int64_t> sp;
         std::vector<int32_t> sc;
         std::vector<double> sv;
-        build_sell32(M.n, M.rp.data(), M.ci.data(), M.v.data(), sp, sc, sv);
+        const double avg = M.n ? double(M.ci.size()) / double(M.n) : 0.0;
+        D.g = 0;
+        if (avg > 12.0) {
+            D.g = 4;
+            while (D.g < 32 && 4.0 * D.g < avg) D.g *= 2;
+            sp = M.rp;
+            sc = M.ci;
+            sv = M.v;
+        } else {
+            build_sell32(M.n, M.rp.data(), M.ci.data(), M.v.data(), sp, sc, sv);
+        }
         int64_t *dsp = nullptr;
         int32_t *dsc = nullptr;
-        double *dsv = nullptr;
+        T *dsv = nullptr;
         CK(upload(&dsp, sp, s));
         keep(dsp);
         CK(upload(&dsc, sc, s));
         keep(dsc);
-        CK(upload(&dsv, sv, s));
+        CK(upload(&dsv, conv(sv), s));
         keep(dsv);
         D.n = M.n;
         D.slice_ptr = dsp;
@@ -274,33 +291,35 @@ int setup_amg(spg_handle *h, const HostMesh &hm) {
         D.sval = dsv;
         return SPG_OK;
     };
-    auto vec = [&](double **p, int64_t n) -> int {
+    auto vec = [&](T **p, int64_t n) -> int {
         CK(dalloc(p, std::max<int64_t>(n, 1)));
         keep(*p);
         return SPG_OK;
     };
-    AmgDev &a = h->amgd;
     a.levels = L;
     h->amg_launches = 0;
     h->amg_bytes = 0.0;
+    h->amg_rows.clear();
+    h->amg_nnz.clear();
+    const double wv = double(sizeof(T)), wm = 4.0 + double(sizeof(T));  // bytes per vector entry / per nonzero
     for (int l = 0; l < L; ++l) {
         const AmgLevelHost &H = ah.levels[l];
-        AmgLevelDev &D = a.lev[l];
+        AmgLevelDevT<T> &D = a.lev[l];
         D.n = H.A.n;
         h->amg_rows.push_back(H.A.n);
         h->amg_nnz.push_back(int64_t(H.A.ci.size()));
         if (l == 0) {
-            D.A.n = hm.n_nodes;
+            D.A.n = H.A.n;
             D.A.slice_ptr = h->slice_ptr;
             D.A.scol = h->scol;
-            D.A.sval = h->sval;
-        } else if ((rc = up_sell(H.A, D.A))) {
+            D.A.sval = sval0;
+        } else if ((rc = up_mat(H.A, D.A))) {
             return rc;
         }
         if (l < L - 1) {
-            if ((rc = up_sell(H.P, D.P)) || (rc = up_sell(H.R, D.R))) return rc;
-            double *dv = nullptr;
-            CK(upload(&dv, H.dinv, s));
+            if ((rc = up_mat(H.P, D.P)) || (rc = up_mat(H.R, D.R))) return rc;
+            T *dv = nullptr;
+            CK(upload(&dv, conv(H.dinv), s));
             keep(dv);
             D.dinv = dv;
             if ((rc = vec(&D.x[1], D.n)) || (rc = vec(&D.r, D.n)) || (rc = vec(&D.d, D.n))) return rc;
@@ -312,23 +331,39 @@ int setup_amg(spg_handle *h, const HostMesh &hm) {
             D.cheb_b = 2.0 * rho1 / delta;
             const double nnzA = double(H.A.ci.size()), n = double(D.n);
             const double nnzP = double(H.P.ci.size()), nc = double(H.P.m);
-            // cheb0 32n; 3 Chebyshev steps (12 nnz + 48 n); residual (12 nnz + 24 n);
-            // restriction (12 nnz(P) + 8 n + 8 nc); prolongation (12 nnz(P) + 16 n + 8 nc)
-            h->amg_bytes += 32.0 * n + 3.0 * (12.0 * nnzA + 48.0 * n) + (12.0 * nnzA + 24.0 * n) +
-                            2.0 * (12.0 * nnzP + 8.0 * nc) + 24.0 * n;
+            // cheb0 4 n; 3 Chebyshev steps (nnz + 6 n); residual (nnz + 3 n);
+            // restriction (nnz(P) + n + nc); prolongation (nnz(P) + 2 n + nc); vector words
+            h->amg_bytes += wv * (4.0 * n + 3.0 * 6.0 * n + 3.0 * n + 3.0 * n + 2.0 * nc) + wm * (4.0 * nnzA + 2.0 * nnzP);
             h->amg_launches += 7;
         }
         if (l > 0 && (rc = vec(&D.b, D.n))) return rc;
         if (l > 0 && (rc = vec(&D.x[0], D.n))) return rc;
     }
     a.nc = ah.nc;
-    double *inv = nullptr;
-    CK(upload(&inv, ah.coarse_inv, s));
+    T *inv = nullptr;
+    CK(upload(&inv, conv(ah.coarse_inv), s));
     keep(inv);
     a.coarse_inv = inv;
     h->amg_launches += 1;
-    h->amg_bytes += 8.0 * double(ah.nc) * double(ah.nc + 2);
-    h->amg = true;
+    h->amg_bytes += wv * double(ah.nc) * double(ah.nc + 2);
+    return SPG_OK;
+}
+
+// Builds the smoothed-aggregation hierarchy of the stiffness matrix on the
+// host and uploads it for the FP64 V-cycle (plain form) or the FP32 V-cycle
+// (inner solve of the mixed form).
+int setup_amg(spg_handle *h, const HostMesh &hm) {
+    AmgHost ah;
+    std::string err;
+    int rc = amg_setup(hm.n_nodes, hm.row_ptr.data(), hm.col.data(), hm.val.data(), ah, err);
+    if (rc) return fail(h, rc, err);
+    if (h->mixed) {
+        if ((rc = upload_amg<float>(h, ah, h->sval32, h->amgd32))) return rc;
+        h->amg32 = true;
+    } else {
+        if ((rc = upload_amg<double>(h, ah, h->sval, h->amgd))) return rc;
+        h->amg = true;
+    }
     return SPG_OK;
 }
 
@@ -345,8 +380,8 @@ void pcg_iteration_any(spg_handle *h, PcgDev &d) {
     else
         launch_pcg_iteration(d, h->stream);
 }
-int pcg_iter_launches(const spg_handle *h) { return h->amg ? 4 + h->amg_launches : 3; }
-int pcg_chunk(const spg_handle *h) { return h->amg ? 2 : kPcgChunk; }
+int pcg_iter_launches(const spg_handle *h) { return (h->amg || h->amg32) ? 4 + h->amg_launches : 3; }
+int pcg_chunk(const spg_handle *h) { return (h->amg || h->amg32) ? 2 : kPcgChunk; }
 
 // Allocates both particle buffers (and the walk queue) for n particles.
 int alloc_particles(spg_handle *h, int64_t n) {
@@ -587,12 +622,12 @@ int do_gather(spg_handle *h) {
 // E from phi for both forms (and the FP32 push increment of the mixed form).
 int update_field(spg_handle *h) {
     ev_begin(h, h->ev_ef);
-    launch_efield64(mesh_dev(h), h->rec, h->efield, h->phi, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
+    if (h->mixed)
+        launch_efield_mixed(h->tet_nodes, h->rec, h->rec32, h->efield, h->phi, h->n_tets, h->prm.charge, h->prm.mass,
+                            h->prm.dt, h->stream);
+    else
+        launch_efield64(mesh_dev(h), h->rec, h->efield, h->phi, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
     h->launches += 1;
-    if (h->mixed) {
-        launch_push32(h->rec32, h->efield, h->n_tets, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
-        h->launches += 1;
-    }
     ev_end(h, h->ev_ef);
     CK(cudaGetLastError());
     return SPG_OK;
@@ -644,9 +679,9 @@ int do_solve64(spg_handle *h) {
     if (h->prof) {
         h->pcg_iters_prof += hs.iters;
         if (h->amg)  // spmv_dot 12 nnz + 24 n, update 48 n, V-cycle, r.z 16 n, p update 24 n
-            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz) + 112.0 * double(n) + h->amg_bytes);
+            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 112.0 * double(n) + h->amg_bytes);
         else
-            h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz) + 4.0 * double(n + 1) + 72.0 * double(n));
+            h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz_kept) + 4.0 * double(n + 1) + 72.0 * double(n));
     }
     return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
 }
@@ -657,16 +692,23 @@ int do_solve_mixed(spg_handle *h) {
     const int64_t n = h->n_nodes;
     PcgScalars outer{}, inner{};
     outer.tol2 = h->prm.cg_rtol * h->prm.cg_rtol;
-    inner.tol2 = kInnerRtol * kInnerRtol;
-    inner.max_iter = kInnerMaxIter;
+    const double inner_rtol = h->amg32 ? kInnerRtolAmg : kInnerRtol;
+    inner.tol2 = inner_rtol * inner_rtol;
+    inner.max_iter = h->amg32 ? kInnerMaxIterAmg : kInnerMaxIter;
     CK(cudaMemcpyAsync(h->sc, &outer, sizeof(outer), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->sc32, &inner, sizeof(inner), cudaMemcpyHostToDevice, h->stream));
     PcgDev d = pcg_dev(h);
     PcgDev32 f = pcg_dev32(h);
+    const int chunk = pcg_chunk(h);
     if (!h->pcg32_graph) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < kPcgChunk; ++k) launch_pcg32_iteration(f, h->stream);
+        for (int k = 0; k < chunk; ++k) {
+            if (h->amg32)
+                launch_pcg32_iteration_amg(f, h->amgd32, h->stream);
+            else
+                launch_pcg32_iteration(f, h->stream);
+        }
         CK(cudaStreamEndCapture(h->stream, &g));
         CK(cudaGraphInstantiate(&h->pcg32_graph, g, 0));
         cudaGraphDestroy(g);
@@ -676,8 +718,13 @@ int do_solve_mixed(spg_handle *h) {
     PcgScalars hs{}, hi{};
     bool capped = true;
     for (int outer_it = 0; outer_it <= kOuterMax; ++outer_it) {
-        launch_refine_setup(d, f, h->b, h->stream);
-        h->launches += 1;
+        if (h->amg32) {
+            launch_refine_setup_amg(d, f, h->amgd32, h->b, h->stream);
+            h->launches += 2 + h->amg_launches;
+        } else {
+            launch_refine_setup(d, f, h->b, h->stream);
+            h->launches += 1;
+        }
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         if (hs.converged) {
@@ -687,7 +734,7 @@ int do_solve_mixed(spg_handle *h) {
         if (outer_it == kOuterMax || total >= h->prm.cg_max_iter) break;
         for (;;) {
             CK(cudaGraphLaunch(h->pcg32_graph, h->stream));
-            h->launches += 3 * kPcgChunk;
+            h->launches += pcg_iter_launches(h) * chunk;
             CK(cudaMemcpyAsync(&hi, h->sc32, sizeof(hi), cudaMemcpyDeviceToHost, h->stream));
             CK(cudaStreamSynchronize(h->stream));
             if (hi.converged) break;
@@ -699,7 +746,10 @@ int do_solve_mixed(spg_handle *h) {
     ev_end(h, h->ev_pcg);
     if (h->prof) {
         h->pcg_iters_prof += total;
-        h->pcg_bytes += double(total) * (8.0 * double(h->nnz) + 4.0 * double(n + 1) + 36.0 * double(n));
+        if (h->amg32)  // spmv_dot 8 nnz + 12 n, update 20 n, V-cycle, r.z 8 n, p update 12 n
+            h->pcg_bytes += double(total) * (8.0 * double(h->nnz_kept) + 52.0 * double(n) + h->amg_bytes);
+        else
+            h->pcg_bytes += double(total) * (8.0 * double(h->nnz_kept) + 4.0 * double(n + 1) + 36.0 * double(n));
     }
     return finish_solve(h, total, hs.rr, hs.bb, capped);
 }
@@ -888,6 +938,10 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         std::vector<double> sv;
         build_sell32(hm.n_nodes, hm.row_ptr.data(), hm.col.data(), hm.val.data(), sp, sc, sv);
         h->sell_entries = int64_t(sv.size());
+        h->nnz_kept = 0;
+        for (int64_t r = 0; r < hm.n_nodes; ++r)
+            for (int32_t k = hm.row_ptr[r]; k < hm.row_ptr[r + 1]; ++k)
+                h->nnz_kept += (hm.val[k] != 0.0 || hm.col[k] == r) ? 1 : 0;
         CK(upload(&h->slice_ptr, sp, s));
         CK(upload(&h->scol, sc, s));
         CK(upload(&h->sval, sv, s));
@@ -896,7 +950,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
             CK(upload(&h->sval32, sv32, s));
         }
     }
-    if (h->prm.preconditioner == SPG_PRECOND_AMG && !h->mixed) {  // the mixed inner solve stays Jacobi
+    if (h->prm.preconditioner == SPG_PRECOND_AMG) {
         int rc = setup_amg(h, hm);
         if (rc) return rc;
     }

@@ -4,8 +4,9 @@
 // Chebyshev post-smoothing of degree 2; the coarsest level multiplies by its
 // dense inverse. Pre- and post-smoother are the same polynomial in D^-1 A, so
 // the V-cycle is a symmetric positive definite operator and CG stays CG.
-// Every operator is stored SELL-32 (level 0 shares the solver's matrix); one
-// row per thread; no atomics, so z = M^-1 r is deterministic.
+// Operators with short rows are stored SELL-32 with one thread per row (level
+// 0 shares the solver's matrix); long rows (coarse operators, restriction)
+// CSR with 4-32 lanes per row. No atomics, so z = M^-1 r is deterministic.
 #include "sell.cuh"
 #include "spg_internal.h"
 
@@ -15,103 +16,191 @@ namespace {
 
 constexpr int kT = 256;
 
+// converged: 1 or 2 (plain PCG), or 3 (inner cap of the mixed form)
 __device__ __forceinline__ bool done(const PcgScalars *sc) { return sc && *(volatile const int *)&sc->converged; }
 
-__device__ __forceinline__ double row_mul(const DevSell &M, const double *__restrict__ x, int64_t i) {
-    return spmv_row_sell<double>(M.slice_ptr, M.scol, M.sval, x, i);
+// Row `row` of M x. G = 0: SELL-32, the calling thread owns the row. G > 0:
+// CSR, the G lanes of a group (lane = lane index within the group) stride
+// over the row's entries and a butterfly over the group leaves the sum in
+// every lane of the group.
+template <class T, int G>
+__device__ __forceinline__ T mat_row(const DevSellT<T> &M, const T *__restrict__ x, int64_t row, int lane) {
+    if constexpr (G == 0) {
+        return spmv_row_sell<T>(M.slice_ptr, M.scol, M.sval, x, row);
+    } else {
+        const int64_t k0 = __ldg(M.slice_ptr + row), k1 = __ldg(M.slice_ptr + row + 1);
+        T a0 = T(0), a1 = T(0);
+        int64_t k = k0 + lane;
+        for (; k + G < k1; k += 2 * G) {
+            const int32_t c0 = __ldg(M.scol + k), c1 = __ldg(M.scol + k + G);
+            const T v0 = __ldg(M.sval + k), v1 = __ldg(M.sval + k + G);
+            a0 = fma(v0, __ldg(x + c0), a0);
+            a1 = fma(v1, __ldg(x + c1), a1);
+        }
+        if (k < k1) a0 = fma(__ldg(M.sval + k), __ldg(x + __ldg(M.scol + k)), a0);
+        T s = a0 + a1;
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, G);
+        return s;
+    }
+}
+
+// Thread -> (row, lane within the row's group); `own`: this thread writes the row.
+template <int G>
+__device__ __forceinline__ void row_of(int64_t n, int64_t &row, int &lane, bool &own) {
+    const int64_t t = int64_t(blockIdx.x) * kT + threadIdx.x;
+    if constexpr (G == 0) {
+        row = t;
+        lane = 0;
+    } else {
+        row = t / G;
+        lane = int(t % G);
+    }
+    own = row < n && lane == 0;
+}
+
+// Every lane of a warp joins the group shuffles; rows past n read nothing.
+template <class T, int G>
+__device__ __forceinline__ T mat_row_safe(const DevSellT<T> &M, const T *__restrict__ x, int64_t row, int lane,
+                                          int64_t n) {
+    if constexpr (G == 0) {
+        return row < n ? mat_row<T, 0>(M, x, row, 0) : T(0);
+    } else {
+        if (row >= n) {
+            T s = T(0);
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, G);
+            return s;
+        }
+        return mat_row<T, G>(M, x, row, lane);
+    }
 }
 
 // x = d = D^-1 b / theta (first Chebyshev step from x = 0)
-__global__ void __launch_bounds__(kT) k_cheb0(const AmgLevelDev L, const double *__restrict__ b,
-                                              double *__restrict__ x, const PcgScalars *sc) {
+template <class T>
+__global__ void __launch_bounds__(kT) k_cheb0(const AmgLevelDevT<T> L, const T *__restrict__ b, T *__restrict__ x,
+                                              const PcgScalars *sc) {
     if (done(sc)) return;
     const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
     if (i >= L.n) return;
-    const double v = L.inv_theta * (L.dinv[i] * b[i]);
+    const T v = T(L.inv_theta) * (L.dinv[i] * b[i]);
     x[i] = v;
     L.d[i] = v;
 }
 
 // r = b - A x_in; d = ca d + cb D^-1 r; x_out = x_in + d
-__global__ void __launch_bounds__(kT) k_cheb_step(const AmgLevelDev L, const double *__restrict__ b,
-                                                  const double *__restrict__ xin, double *__restrict__ xout,
-                                                  double ca, double cb, const PcgScalars *sc) {
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_cheb_step(const AmgLevelDevT<T> L, const T *__restrict__ b,
+                                                  const T *__restrict__ xin, T *__restrict__ xout, double ca,
+                                                  double cb, const PcgScalars *sc) {
     if (done(sc)) return;
-    const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
-    if (i >= L.n) return;
-    const double r = b[i] - row_mul(L.A, xin, i);
-    const double d = ca * L.d[i] + cb * (L.dinv[i] * r);
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(L.n, i, lane, own);
+    const T ax = mat_row_safe<T, G>(L.A, xin, i, lane, L.n);
+    if (!own) return;
+    const T r = b[i] - ax;
+    const T d = T(ca) * L.d[i] + T(cb) * (L.dinv[i] * r);
     L.d[i] = d;
     xout[i] = xin[i] + d;
 }
 
-__global__ void __launch_bounds__(kT) k_resid(const AmgLevelDev L, const double *__restrict__ b,
-                                              const double *__restrict__ xin, const PcgScalars *sc) {
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_resid(const AmgLevelDevT<T> L, const T *__restrict__ b,
+                                              const T *__restrict__ xin, const PcgScalars *sc) {
     if (done(sc)) return;
-    const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
-    if (i >= L.n) return;
-    L.r[i] = b[i] - row_mul(L.A, xin, i);
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(L.n, i, lane, own);
+    const T ax = mat_row_safe<T, G>(L.A, xin, i, lane, L.n);
+    if (own) L.r[i] = b[i] - ax;
 }
 
 // b_next = R r
-__global__ void __launch_bounds__(kT) k_restrict(const DevSell R, const double *__restrict__ r,
-                                                 double *__restrict__ bnext, const PcgScalars *sc) {
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_restrict(const DevSellT<T> R, const T *__restrict__ r, T *__restrict__ bnext,
+                                                 const PcgScalars *sc) {
     if (done(sc)) return;
-    const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
-    if (i >= R.n) return;
-    bnext[i] = row_mul(R, r, i);
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(R.n, i, lane, own);
+    const T v = mat_row_safe<T, G>(R, r, i, lane, R.n);
+    if (own) bnext[i] = v;
 }
 
 // x_out = x_in + P x_coarse
-__global__ void __launch_bounds__(kT) k_prolong(const DevSell P, const double *__restrict__ xin,
-                                                const double *__restrict__ xc, double *__restrict__ xout,
-                                                const PcgScalars *sc) {
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_prolong(const DevSellT<T> P, const T *__restrict__ xin,
+                                                const T *__restrict__ xc, T *__restrict__ xout, const PcgScalars *sc) {
     if (done(sc)) return;
-    const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
-    if (i >= P.n) return;
-    xout[i] = xin[i] + row_mul(P, xc, i);
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(P.n, i, lane, own);
+    const T v = mat_row_safe<T, G>(P, xc, i, lane, P.n);
+    if (own) xout[i] = xin[i] + v;
 }
 
 // x = A_c^-1 b: one warp per row of the dense inverse, fixed-order lane sums.
-__global__ void __launch_bounds__(kT) k_coarse(const double *__restrict__ inv, int64_t nc,
-                                               const double *__restrict__ b, double *__restrict__ x,
-                                               const PcgScalars *sc) {
+template <class T>
+__global__ void __launch_bounds__(kT) k_coarse(const T *__restrict__ inv, int64_t nc, const T *__restrict__ b,
+                                               T *__restrict__ x, const PcgScalars *sc) {
     if (done(sc)) return;
     const int64_t row = (int64_t(blockIdx.x) * kT + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= nc) return;
-    double s = 0.0;
+    T s = T(0);
     for (int64_t k = lane; k < nc; k += 32) s += inv[row * nc + k] * b[k];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) x[row] = s;
 }
 
-inline unsigned blocks_for(int64_t n) { return unsigned((n + kT - 1) / kT); }
+inline unsigned blocks_for(int64_t n, int g = 0) {
+    const int64_t threads = n * (g > 0 ? g : 1);
+    return unsigned((threads + kT - 1) / kT);
+}
 
-void vcycle_level(const AmgDev &a, int l, const double *b, double *xa, const PcgScalars *sc, cudaStream_t s) {
-    const AmgLevelDev &L = a.lev[l];
+#define SPG_AMG_DISPATCH(g, KERNEL, GRIDN, ...)                                          \
+    switch (g) {                                                                         \
+    case 4: KERNEL<T, 4><<<blocks_for(GRIDN, 4), kT, 0, s>>>(__VA_ARGS__); break;       \
+    case 8: KERNEL<T, 8><<<blocks_for(GRIDN, 8), kT, 0, s>>>(__VA_ARGS__); break;       \
+    case 16: KERNEL<T, 16><<<blocks_for(GRIDN, 16), kT, 0, s>>>(__VA_ARGS__); break;    \
+    case 32: KERNEL<T, 32><<<blocks_for(GRIDN, 32), kT, 0, s>>>(__VA_ARGS__); break;    \
+    default: KERNEL<T, 0><<<blocks_for(GRIDN, 0), kT, 0, s>>>(__VA_ARGS__); break;      \
+    }
+
+template <class T>
+void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalars *sc, cudaStream_t s) {
+    const AmgLevelDevT<T> &L = a.lev[l];
     if (l == a.levels - 1) {
-        k_coarse<<<unsigned((a.nc * 32 + kT - 1) / kT), kT, 0, s>>>(a.coarse_inv, a.nc, b, xa, sc);
+        k_coarse<T><<<unsigned((a.nc * 32 + kT - 1) / kT), kT, 0, s>>>(a.coarse_inv, a.nc, b, xa, sc);
         return;
     }
-    double *xb = L.x[1];
-    const unsigned g = blocks_for(L.n);
-    k_cheb0<<<g, kT, 0, s>>>(L, b, xa, sc);
-    k_cheb_step<<<g, kT, 0, s>>>(L, b, xa, xb, L.cheb_a, L.cheb_b, sc);
-    k_resid<<<g, kT, 0, s>>>(L, b, xb, sc);
-    const AmgLevelDev &N = a.lev[l + 1];
-    k_restrict<<<blocks_for(N.n), kT, 0, s>>>(L.R, L.r, N.b, sc);
-    vcycle_level(a, l + 1, N.b, N.x[0], sc, s);
-    k_prolong<<<g, kT, 0, s>>>(L.P, xb, N.x[0], xa, sc);
-    k_cheb_step<<<g, kT, 0, s>>>(L, b, xa, xb, 0.0, L.inv_theta, sc);
-    k_cheb_step<<<g, kT, 0, s>>>(L, b, xb, xa, L.cheb_a, L.cheb_b, sc);
+    T *xb = L.x[1];
+    const int ga = L.A.g;
+    k_cheb0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
+    SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xa, xb, L.cheb_a, L.cheb_b, sc)
+    SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xb, sc)
+    const AmgLevelDevT<T> &N = a.lev[l + 1];
+    SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
+    vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
+    SPG_AMG_DISPATCH(L.P.g, k_prolong, L.P.n, L.P, xb, N.x[0], xa, sc)
+    SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xa, xb, 0.0, L.inv_theta, sc)
+    SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xb, xa, L.cheb_a, L.cheb_b, sc)
 }
 
 }  // namespace
 
 void launch_amg_vcycle(const AmgDev &a, const double *r, double *z, const PcgScalars *sc, cudaStream_t s) {
-    vcycle_level(a, 0, r, z, sc, s);
+    vcycle_level<double>(a, 0, r, z, sc, s);
+}
+
+void launch_amg_vcycle(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s) {
+    vcycle_level<float>(a, 0, r, z, sc, s);
 }
 
 }  // namespace spg

@@ -16,6 +16,7 @@
 #include <cmath>
 
 #include "philox.h"
+#include "deposit.cuh"
 #include "spg_internal.h"
 
 namespace spg {
@@ -352,7 +353,6 @@ __device__ __forceinline__ long long fix_round32(float x, int k) {
 
 __global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned long long *__restrict__ node_fix) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
     int key = -1;
     long long v[4] = {0, 0, 0, 0};
     if (i < a.n && !(a.p.idf[i] & kDead)) {
@@ -366,34 +366,7 @@ __global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned 
         v[3] = fix_round32(l[3], k);
         v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
-    const int prev = __shfl_up_sync(kFull, key, 1);
-    const bool head = lane == 0 || prev != key;
-    const unsigned heads = __ballot_sync(kFull, head);
-    if (heads != 1u) {
-        const int start = 31 - __clz(heads & (kFull >> (31 - lane)));
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const long long up = __shfl_up_sync(kFull, v[q], off);
-                if (lane - off >= start) v[q] += up;
-            }
-        }
-    } else {
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(kFull, v[q], off);
-        }
-    }
-    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
-    if (tail && key >= 0) {
-        const int4 tn = __ldg(a.tet_nodes + key);
-        atomicAdd(node_fix + tn.x, (unsigned long long)v[0]);
-        atomicAdd(node_fix + tn.y, (unsigned long long)v[1]);
-        atomicAdd(node_fix + tn.z, (unsigned long long)v[2]);
-        atomicAdd(node_fix + tn.w, (unsigned long long)v[3]);
-    }
+    deposit_block_flush<256>(key, v, a.tet_nodes, node_fix);
 }
 
 // Push increment in FP32 from the FP64 field of the plain form's kernel.
@@ -406,6 +379,30 @@ __global__ void k_push32(TetRec32 *__restrict__ rec, const double *__restrict__ 
     rec[t].H[1] = float(((charge * E1) / mass * dt) / 2.0);
     rec[t].H[2] = float(((charge * E2) / mass * dt) / 2.0);
     rec[t].ezero = (E0 == 0.0 && E1 == 0.0 && E2 == 0.0) ? 1u : 0u;
+}
+
+// Mixed form: E per tet in FP64 from phi (the FP32 potential differences
+// across a tet would lose the field), then the FP32 push increment
+// H = float(E c) with c = q dt / (2 m) formed once on the host, so no FP64
+// division runs per tet. The FP64 record of the plain form is not touched.
+__global__ void k_efield_mixed(const int4 *__restrict__ tet_nodes, const TetRec *__restrict__ rec64,
+                               TetRec32 *__restrict__ rec, double *__restrict__ efield,
+                               const double *__restrict__ phi, int64_t n, double c) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 tn = __ldg(tet_nodes + t);
+    const double f0 = phi[tn.x], f1 = phi[tn.y], f2 = phi[tn.z], f3 = phi[tn.w];
+    const double d1 = f1 - f0, d2 = f2 - f0, d3 = f3 - f0;
+    const TetRec &r = rec64[t];
+    double E[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        efield[3 * t + k] = E[k];
+        rec[t].H[k] = float(E[k] * c);
+    }
+    rec[t].ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
 }
 
 // Global FP64 state -> local FP32 state (and back).
@@ -502,6 +499,12 @@ void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, in
                       cudaStream_t s) {
     if (n <= 0) return;
     k_deposit32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), k, node_fix);
+}
+
+void launch_efield_mixed(const int4 *tet_nodes, const TetRec *rec64, TetRec32 *rec, double *efield, const double *phi,
+                         int64_t n_tets, double charge, double mass, double dt, cudaStream_t s) {
+    const double c = ((charge / mass) * dt) / 2.0;
+    k_efield_mixed<<<grid_for(n_tets, 256), 256, 0, s>>>(tet_nodes, rec64, rec, efield, phi, n_tets, c);
 }
 
 void launch_push32(TetRec32 *rec, const double *efield, int64_t n_tets, double charge, double mass, double dt,

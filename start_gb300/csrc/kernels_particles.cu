@@ -18,6 +18,7 @@
 #include <cstdio>
 
 #include "philox.h"
+#include "deposit.cuh"
 #include "spg_internal.h"
 
 namespace spg {
@@ -446,12 +447,11 @@ __device__ __forceinline__ long long fix_round(double x, int k) {
 // exactly 2^k and charge is conserved exactly. Integer sums do not depend on
 // summation order, so the result is the same for any particle order, grid
 // or atomic interleaving. Lanes of a warp hold consecutive (tet-sorted)
-// particles; runs of equal tet are summed with a segmented shuffle scan and
-// the last lane of each run issues the four atomics.
+// particles; runs of equal tet are summed over the block (deposit.cuh) and
+// the last thread of each run issues the four atomics.
 __global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, MeshDev m, int k,
                                                    unsigned long long *__restrict__ node_fix) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
     int key = -1;
     long long v[4] = {0, 0, 0, 0};
     if (i < n && !(p.idf[i] & kDead)) {
@@ -467,35 +467,7 @@ __global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, Me
         v[3] = fix_round(l3, k);
         v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
-    const int prev = __shfl_up_sync(kFull, key, 1);
-    const bool head = lane == 0 || prev != key;
-    const unsigned heads = __ballot_sync(kFull, head);
-    if (heads != 1u) {
-        const unsigned le = kFull >> (31 - lane);
-        const int start = 31 - __clz(heads & le);
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const long long up = __shfl_up_sync(kFull, v[q], off);
-                if (lane - off >= start) v[q] += up;
-            }
-        }
-    } else {  // one run covers the warp: butterfly sum, every lane holds it
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(kFull, v[q], off);
-        }
-    }
-    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
-    if (tail && key >= 0) {
-        const int4 tn = __ldg(m.tet_nodes + key);
-        atomicAdd(node_fix + tn.x, (unsigned long long)v[0]);
-        atomicAdd(node_fix + tn.y, (unsigned long long)v[1]);
-        atomicAdd(node_fix + tn.z, (unsigned long long)v[2]);
-        atomicAdd(node_fix + tn.w, (unsigned long long)v[3]);
-    }
+    deposit_block_flush<256>(key, v, m.tet_nodes, node_fix);
 }
 
 __global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix, double scale,

@@ -247,6 +247,8 @@ void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const
                    unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s);
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
                       cudaStream_t s);
+void launch_efield_mixed(const int4 *tet_nodes, const TetRec *rec64, TetRec32 *rec, double *efield, const double *phi,
+                         int64_t n_tets, double charge, double mass, double dt, cudaStream_t s);
 void launch_push32(TetRec32 *rec, const double *efield, int64_t n_tets, double charge, double mass, double dt,
                    cudaStream_t s);
 void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
@@ -326,39 +328,63 @@ struct AmgHost {
     int64_t nc = 0;                    // rows of the coarsest level
     std::vector<double> coarse_inv;    // its dense inverse, row-major
 };
+struct AmgOptions {
+    double theta = 0.08;   // strength of connection
+    double filter = 0.0;   // coarse operators: couplings below filter * sqrt(|a_ii a_jj|) move to the diagonal
+    int64_t coarse_rows = 600;
+    int smooth_levels = 99;  // levels whose prolongator is smoothed (the rest use plain aggregation)
+};
 int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val, AmgHost &out,
-              std::string &err);
+              std::string &err, const AmgOptions &opt = AmgOptions{});
 
 constexpr int kAmgMaxLevels = 12;
-struct DevSell {
+// A V-cycle operator on the device: SELL-32 with one thread per row (g = 0,
+// short rows), or CSR with g lanes per row (g = 4, 8, 16 or 32; the long rows
+// of coarse operators and of the restriction). T: double (FP64 form) or
+// float (the inner solve of the mixed form).
+template <class T>
+struct DevSellT {
     int64_t n = 0;
-    const int64_t *slice_ptr = nullptr;
+    int g = 0;
+    const int64_t *slice_ptr = nullptr;  // SELL: slice offsets; CSR: row offsets
     const int32_t *scol = nullptr;
-    const double *sval = nullptr;
+    const T *sval = nullptr;
 };
 // One level of the V-cycle on the device. Chebyshev smoothing of degree 2
 // on D^-1 A over [lam/30, lam]: theta = (hi+lo)/2, delta = (hi-lo)/2.
-struct AmgLevelDev {
+template <class T>
+struct AmgLevelDevT {
     int64_t n = 0;
-    DevSell A, P, R;       // P: n x n_next, R: n_next x n
-    const double *dinv = nullptr;
-    double *x[2] = {nullptr, nullptr};  // iterate ping-pong
-    double *b = nullptr, *r = nullptr, *d = nullptr;
+    DevSellT<T> A, P, R;  // P: n x n_next, R: n_next x n
+    const T *dinv = nullptr;
+    T *x[2] = {nullptr, nullptr};  // iterate ping-pong
+    T *b = nullptr, *r = nullptr, *d = nullptr;
     double inv_theta = 0.0, cheb_a = 0.0, cheb_b = 0.0;  // step 2: d = a d + b D^-1 r
 };
-struct AmgDev {
+template <class T>
+struct AmgDevT {
     int levels = 0;  // including the coarsest (dense) level
-    AmgLevelDev lev[kAmgMaxLevels];
+    AmgLevelDevT<T> lev[kAmgMaxLevels];
     int64_t nc = 0;
-    const double *coarse_inv = nullptr;
+    const T *coarse_inv = nullptr;
 };
+using DevSell = DevSellT<double>;
+using AmgLevelDev = AmgLevelDevT<double>;
+using AmgDev = AmgDevT<double>;
+using AmgDev32 = AmgDevT<float>;
 // z = M^-1 r by one V-cycle (level 0 vectors: b = r, x[0] = z, x[1] scratch);
-// every kernel returns at once when sc->converged is set.
+// every kernel returns at once when sc->converged is set (sc->converged == 3,
+// the inner cap of the mixed form, also stops it).
 void launch_amg_vcycle(const AmgDev &a, const double *r, double *z, const PcgScalars *sc, cudaStream_t s);
+void launch_amg_vcycle(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s);
 // PCG with the V-cycle: setup and one iteration (spmv_dot, update, V-cycle,
 // r.z and beta, p update).
 void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s);
 void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s);
+// The mixed form's inner FP32 PCG with the FP32 V-cycle: outer FP64 residual
+// and inner start, and one inner iteration.
+void launch_refine_setup_amg(const PcgDev &d, const PcgDev32 &f, const AmgDev32 &a, const double *b, cudaStream_t s);
+void launch_pcg32_iteration_amg(PcgDev32 &f, const AmgDev32 &a, cudaStream_t s);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
                     const double *dir_value, double *b, int64_t n, cudaStream_t s);
