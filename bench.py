@@ -427,8 +427,8 @@ def main():
     ap.add_argument("--particles", type=int, default=10_000_000)
     ap.add_argument("--cells", type=int, default=100)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "amg"],
-                    help="Poisson PCG preconditioner of the FP64 form")
+    ap.add_argument("--precond", default="amg", choices=["jacobi", "amg"],
+                    help="Poisson PCG preconditioner (both forms)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU sample (0: all)")
     ap.add_argument("--cpu-steps", type=int, default=0, help="timed CPU steps (0: --steps)")
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient leg")

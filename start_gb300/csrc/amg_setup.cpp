@@ -203,9 +203,11 @@ int64_t aggregate(const AmgCsr &A, double theta, std::vector<int64_t> &agg) {
     return na;
 }
 
-// Moves the weak couplings |a_ij| < eps sqrt(|a_ii a_jj|) of a coarse operator
-// onto the diagonal (row sums, hence the constant near-null space, are kept;
-// the criterion is symmetric, so the operator stays symmetric).
+// Moves the weak positive couplings 0 < a_ij < eps sqrt(|a_ii a_jj|) of a
+// coarse operator onto the diagonal. Row sums, hence the constant near-null
+// space, are kept; the criterion is symmetric, so the operator stays
+// symmetric; and the change for one pair, a_ij (e_i - e_j)(e_i - e_j)^T, is
+// positive semidefinite, so the operator stays positive definite.
 void filter_weak(AmgCsr &A, double eps) {
     std::vector<double> d(A.n, 0.0);
     for (int64_t i = 0; i < A.n; ++i)
@@ -219,7 +221,7 @@ void filter_weak(AmgCsr &A, double eps) {
         int64_t diag = -1;
         for (int64_t k = A.rp[i]; k < A.rp[i + 1]; ++k) {
             const int32_t j = A.ci[k];
-            if (j != i && std::fabs(A.v[k]) < eps * std::sqrt(std::fabs(d[i] * d[j]))) {
+            if (j != i && A.v[k] > 0.0 && A.v[k] < eps * std::sqrt(std::fabs(d[i] * d[j]))) {
                 lump += A.v[k];
                 continue;
             }
@@ -245,6 +247,7 @@ bool dense_inverse(int64_t n, std::vector<double> &a, std::vector<double> &inv) 
         if (!(s > 0.0)) return false;
         const double l = std::sqrt(s);
         a[j * n + j] = l;
+#pragma omp parallel for schedule(static)
         for (int64_t i = j + 1; i < n; ++i) {
             double t = a[i * n + j];
             for (int64_t k = 0; k < j; ++k) t -= a[i * n + k] * a[j * n + k];
@@ -252,9 +255,9 @@ bool dense_inverse(int64_t n, std::vector<double> &a, std::vector<double> &inv) 
         }
     }
     inv.assign(n * n, 0.0);
-    std::vector<double> e(n);
+#pragma omp parallel for schedule(dynamic, 8)
     for (int64_t c = 0; c < n; ++c) {
-        std::fill(e.begin(), e.end(), 0.0);
+        std::vector<double> e(n, 0.0);
         e[c] = 1.0;
         for (int64_t i = 0; i < n; ++i) {  // L y = e
             double t = e[i];

@@ -268,8 +268,10 @@ int upload_amg(spg_handle *h, const AmgHost &ah, const T *sval0, AmgDevT<T> &a) 
         const double avg = M.n ? double(M.ci.size()) / double(M.n) : 0.0;
         D.g = 0;
         if (avg > 12.0) {
+            // FP64: 4 lanes per row (each FP64 shuffle add costs a full warp
+            // instruction at the FP64 rate); FP32: about 4 entries per lane
             D.g = 4;
-            while (D.g < 32 && 4.0 * D.g < avg) D.g *= 2;
+            while (sizeof(T) == 4 && D.g < 32 && 4.0 * D.g < avg) D.g *= 2;
             sp = M.rp;
             sc = M.ci;
             sv = M.v;
@@ -323,7 +325,8 @@ int upload_amg(spg_handle *h, const AmgHost &ah, const T *sval0, AmgDevT<T> &a) 
             keep(dv);
             D.dinv = dv;
             if ((rc = vec(&D.x[1], D.n)) || (rc = vec(&D.r, D.n)) || (rc = vec(&D.d, D.n))) return rc;
-            const double hi = H.lam, lo = H.lam / 30.0;
+            D.degree = l == 0 ? 2 : 1;
+            const double hi = H.lam, lo = D.degree == 2 ? H.lam / 30.0 : H.lam / 4.0;
             const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
             const double sigma = theta / delta, rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
             D.inv_theta = 1.0 / theta;
@@ -331,10 +334,13 @@ int upload_amg(spg_handle *h, const AmgHost &ah, const T *sval0, AmgDevT<T> &a) 
             D.cheb_b = 2.0 * rho1 / delta;
             const double nnzA = double(H.A.ci.size()), n = double(D.n);
             const double nnzP = double(H.P.ci.size()), nc = double(H.P.m);
-            // cheb0 4 n; 3 Chebyshev steps (nnz + 6 n); residual (nnz + 3 n);
-            // restriction (nnz(P) + n + nc); prolongation (nnz(P) + 2 n + nc); vector words
-            h->amg_bytes += wv * (4.0 * n + 3.0 * 6.0 * n + 3.0 * n + 3.0 * n + 2.0 * nc) + wm * (4.0 * nnzA + 2.0 * nnzP);
-            h->amg_launches += 7;
+            // cheb0 4 n; Chebyshev steps (nnz + 6 n each: 3 at degree 2, 1 at degree 1);
+            // residual (nnz + 3 n); restriction (nnz(P) + n + nc); prolongation
+            // (nnz(P) + 2 n + nc); vector words
+            const double steps = D.degree == 2 ? 3.0 : 1.0;
+            h->amg_bytes += wv * (4.0 * n + steps * 6.0 * n + 3.0 * n + 3.0 * n + 2.0 * nc) +
+                            wm * ((steps + 1.0) * nnzA + 2.0 * nnzP);
+            h->amg_launches += D.degree == 2 ? 7 : 5;
         }
         if (l > 0 && (rc = vec(&D.b, D.n))) return rc;
         if (l > 0 && (rc = vec(&D.x[0], D.n))) return rc;

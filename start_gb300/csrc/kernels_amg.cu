@@ -31,13 +31,18 @@ __device__ __forceinline__ T mat_row(const DevSellT<T> &M, const T *__restrict__
         const int64_t k0 = __ldg(M.slice_ptr + row), k1 = __ldg(M.slice_ptr + row + 1);
         T a0 = T(0), a1 = T(0);
         int64_t k = k0 + lane;
-        for (; k + G < k1; k += 2 * G) {
+        for (; k + 3 * G < k1; k += 4 * G) {  // four entries per lane in flight
             const int32_t c0 = __ldg(M.scol + k), c1 = __ldg(M.scol + k + G);
+            const int32_t c2 = __ldg(M.scol + k + 2 * G), c3 = __ldg(M.scol + k + 3 * G);
             const T v0 = __ldg(M.sval + k), v1 = __ldg(M.sval + k + G);
-            a0 = fma(v0, __ldg(x + c0), a0);
-            a1 = fma(v1, __ldg(x + c1), a1);
+            const T v2 = __ldg(M.sval + k + 2 * G), v3 = __ldg(M.sval + k + 3 * G);
+            const T x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+            a0 = fma(v0, x0, a0);
+            a1 = fma(v1, x1, a1);
+            a0 = fma(v2, x2, a0);
+            a1 = fma(v3, x3, a1);
         }
-        if (k < k1) a0 = fma(__ldg(M.sval + k), __ldg(x + __ldg(M.scol + k)), a0);
+        for (; k < k1; k += G) a0 = fma(__ldg(M.sval + k), __ldg(x + __ldg(M.scol + k)), a0);
         T s = a0 + a1;
 #pragma unroll
         for (int off = G / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, G);
@@ -182,10 +187,19 @@ void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalar
     }
     T *xb = L.x[1];
     const int ga = L.A.g;
+    const AmgLevelDevT<T> &N = a.lev[l + 1];
+    if (L.degree == 1) {  // x = D^-1 b / theta; residual; coarse correction; one damped Jacobi step
+        k_cheb0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
+        SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xa, sc)
+        SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
+        vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
+        SPG_AMG_DISPATCH(L.P.g, k_prolong, L.P.n, L.P, xa, N.x[0], xb, sc)
+        SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xb, xa, 0.0, L.inv_theta, sc)
+        return;
+    }
     k_cheb0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
     SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xa, xb, L.cheb_a, L.cheb_b, sc)
     SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xb, sc)
-    const AmgLevelDevT<T> &N = a.lev[l + 1];
     SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
     vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
     SPG_AMG_DISPATCH(L.P.g, k_prolong, L.P.n, L.P, xb, N.x[0], xa, sc)

@@ -331,7 +331,7 @@ struct AmgHost {
 struct AmgOptions {
     double theta = 0.08;   // strength of connection
     double filter = 0.0;   // coarse operators: couplings below filter * sqrt(|a_ii a_jj|) move to the diagonal
-    int64_t coarse_rows = 600;
+    int64_t coarse_rows = 1500;
     int smooth_levels = 99;  // levels whose prolongator is smoothed (the rest use plain aggregation)
 };
 int amg_setup(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val, AmgHost &out,
@@ -350,11 +350,14 @@ struct DevSellT {
     const int32_t *scol = nullptr;
     const T *sval = nullptr;
 };
-// One level of the V-cycle on the device. Chebyshev smoothing of degree 2
-// on D^-1 A over [lam/30, lam]: theta = (hi+lo)/2, delta = (hi-lo)/2.
+// One level of the V-cycle on the device. Jacobi-Chebyshev smoothing on
+// D^-1 A: degree 2 over [lam/30, lam] on level 0, degree 1 (damped Jacobi,
+// 1/theta = 1.6/lam) over [lam/4, lam] on the coarser levels; theta =
+// (hi+lo)/2, delta = (hi-lo)/2.
 template <class T>
 struct AmgLevelDevT {
     int64_t n = 0;
+    int degree = 2;
     DevSellT<T> A, P, R;  // P: n x n_next, R: n_next x n
     const T *dinv = nullptr;
     T *x[2] = {nullptr, nullptr};  // iterate ping-pong
