@@ -126,3 +126,25 @@ $EndElements
     assert m.volumes()[0] > 0
     assert m.triangles.tolist() == [[0, 1, 2]] and m.tri_tag.tolist() == [5]
     assert np.allclose(m.nodes[3], [0, 0, 1e-3])
+
+
+def test_triangle_count_writer_roundtrip(tmp_path):
+    from start_gb300 import mesh as M
+    from start_gb300 import output
+
+    m = M.kuhn_box((3, 3, 3), (0.03, 0.03, 0.03))
+    tris = np.asarray(m.triangles).reshape(-1, 3)
+    counts = np.arange(len(tris), dtype=np.uint32) % 7
+    p = tmp_path / "tri.npz"
+    output.write_triangle_counts(p, m.nodes, tris, counts, length_scale=1e3)
+    d = output.read(p)
+    assert d["Coordinates"].shape == (len(tris), 9)
+    assert np.array_equal(d["Counter"], counts.astype(np.uint64))
+    # each boundary face of the 30 mm cube is 900 mm^2, split into 2*9 triangles
+    assert np.isclose(d["Area"].sum(), 6 * 900.0)
+    assert np.allclose(d["Area"], 50.0)
+    pos = np.random.default_rng(0).random((10, 3))
+    flags = np.array([1, 0, 1, 2, 0, 1, 0, 0, 3, 0], np.uint32)
+    output.write_settled_particles(tmp_path / "s.npz", pos, flags)
+    s = output.read(tmp_path / "s.npz")
+    assert np.array_equal(s["positions"], pos[(flags & 1) != 0])
