@@ -39,14 +39,20 @@ __device__ __forceinline__ void deposit_block_flush(int key, long long v[4], con
                 if (lane - off >= start) v[q] += up;
             }
         }
-    } else {  // one run covers the warp: inclusive prefix = plain prefix sum
+    } else {
+        // One run covers the warp (the common case: hundreds of particles per
+        // occupied tet); only its total is used (at lane 31). It goes through
+        // the integer reduce unit instead of 64-bit shuffles: each value is
+        // split into 21-bit pieces whose 32-lane sums cannot overflow 32 bits
+        // (a particle's weights are at most 2^52 in magnitude, so the top
+        // piece v >> 42 is at most 2^10).
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const long long up = __shfl_up_sync(kAll, v[q], off);
-                if (lane >= off) v[q] += up;
-            }
+        for (int q = 0; q < 4; ++q) {
+            const unsigned b0 = unsigned(v[q] & 0x1FFFFF), b1 = unsigned((v[q] >> 21) & 0x1FFFFF);
+            const int b2 = int(v[q] >> 42);
+            const unsigned s0 = __reduce_add_sync(kAll, b0), s1 = __reduce_add_sync(kAll, b1);
+            const int s2 = __reduce_add_sync(kAll, b2);
+            v[q] = (long long)s0 + (long long)s1 * (1LL << 21) + (long long)s2 * (1LL << 42);
         }
     }
     if (lane == 0) s_kf[w] = key;

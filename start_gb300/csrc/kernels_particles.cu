@@ -104,6 +104,36 @@ __device__ __forceinline__ bool inside_sure(const TetGeo &g, double d0, double d
     return l[0] > b[0] && l[1] > b[1] && l[2] > b[2] && l0 > b0;
 }
 
+// The same screen from the position itself, with no FP64 instruction: d is
+// formed in FP32 from p and x0 truncated to 20 mantissa bits (integer ops).
+// |p - pf| < 2^-20 |p| <= 9.6e-7 |pf| (pf truncates toward zero) and the FP32
+// difference rounds by at most 2^-24 |d_f|, so each d_k is within
+// delta_k = 9.6e-7 (|pf_k| + |x0f_k|) + 6e-8 |d_fk| + 1e-30 of p_k - x0_k.
+// That adds sum_k |M_ik| delta_k (times 1.01 for the truncation of M) to the
+// margin of lambda_i.
+__device__ __forceinline__ bool inside_sure_pos(const TetGeo &g, double px, double py, double pz) {
+    const float pf[3] = {hi_float(px), hi_float(py), hi_float(pz)};
+    float e[3], dl[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float x0 = hi_float(g.x0[k]);
+        e[k] = pf[k] - x0;
+        dl[k] = fmaf(9.6e-7f, fabsf(pf[k]) + fabsf(x0), fmaf(6e-8f, fabsf(e[k]), 1e-30f));
+    }
+    float l[3], b[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float m0 = hi_float(g.M[3 * r]), m1 = hi_float(g.M[3 * r + 1]), m2 = hi_float(g.M[3 * r + 2]);
+        l[r] = fmaf(m2, e[2], fmaf(m1, e[1], m0 * e[0]));
+        const float s = fmaf(fabsf(m2), fabsf(e[2]), fmaf(fabsf(m1), fabsf(e[1]), fabsf(m0) * fabsf(e[0])));
+        const float pd = fmaf(fabsf(m2), dl[2], fmaf(fabsf(m1), dl[1], fabsf(m0) * dl[0]));
+        b[r] = fmaf(4e-6f, s, fmaf(1.01f, pd, 1e-30f));
+    }
+    const float l0 = 1.0f - l[0] - l[1] - l[2];
+    const float b0 = b[0] + b[1] + b[2] + 1e-6f;
+    return l[0] > b[0] && l[1] > b[1] && l[2] > b[2] && l0 > b0;
+}
+
 struct WalkOut {
     int tet, status, tri, crossings, face;
     double s;
@@ -334,7 +364,7 @@ __global__ void __launch_bounds__(256, 4) k_step64(DevParticles p, int64_t n, Me
                     } else {
                         TetGeo g;
                         load_geo(m.rec, t, g);
-                        want_walk = !inside_sure(g, nx - g.x0[0], ny - g.x0[1], nz - g.x0[2]);
+                        want_walk = !inside_sure_pos(g, nx, ny, nz);
                         p.x[i] = nx;
                         p.y[i] = ny;
                         p.z[i] = nz;
