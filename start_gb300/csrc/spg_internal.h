@@ -351,9 +351,8 @@ struct DevSellT {
     const T *sval = nullptr;
 };
 // One level of the V-cycle on the device. Jacobi-Chebyshev smoothing on
-// D^-1 A: degree 2 over [lam/30, lam] on level 0, degree 1 (damped Jacobi,
-// 1/theta = 1.6/lam) over [lam/4, lam] on the coarser levels; theta =
-// (hi+lo)/2, delta = (hi-lo)/2.
+// D^-1 A: degree 2 over [lam/30, lam], or degree 1 (damped Jacobi,
+// 1/theta = 1.6/lam) over [lam/4, lam]; theta = (hi+lo)/2, delta = (hi-lo)/2.
 template <class T>
 struct AmgLevelDevT {
     int64_t n = 0;
