@@ -123,10 +123,14 @@ def measured_peak():
 
 
 def build_workload(args):
-    from start_gb300.workloads import workload1
+    from start_gb300.workloads import workload1, workload3
 
-    cells = args.cells
-    w = workload1(n_particles=args.particles, cells=cells, seed=0, steps=args.warmup + args.steps)
+    if args.workload == 3:
+        # jittered 200 x 200 x 100 mm box with two plate electrodes, VSS argon 2 Pa
+        n = args.particles if args.particles != 10_000_000 else 50_000_000
+        w = workload3(n_particles=n, seed=0, steps=args.warmup + args.steps)
+    else:
+        w = workload1(n_particles=args.particles, cells=args.cells, seed=0, steps=args.warmup + args.steps)
     w.params["precision"] = 1 if args.precision == "mixed" else 0
     w.params["preconditioner"] = 1 if args.precond == "amg" else 0
     return w
@@ -237,10 +241,12 @@ def grad_leg(args, local):
 def config_dict(args, w):
     return {"workload": w.name, "n_particles": int(len(w.pos)), "n_tets": int(w.mesh.n_tets),
             "n_nodes": int(w.mesh.n_nodes), "n_triangles": int(w.mesh.n_triangles),
-            "collision_model": "VHS", "poisson_every": w.params["poisson_every"],
+            "collision_model": {1: "HS", 2: "VHS", 3: "VSS"}.get(w.params["collision_model"], "none"),
+            "poisson_every": w.params["poisson_every"],
             "resort_every": w.params["resort_every"], "dt": w.params["dt"], "precision": args.precision,
             "preconditioner": args.precond,
-            "l2_policy": "inputs larger than L2 (particles 560 MB, mesh ~1.4 GB)",
+            "l2_policy": f"inputs larger than L2 (particles {len(w.pos) * 56 / 1e6:.0f} MB, "
+                         f"mesh {w.mesh.n_tets * 200 / 1e9:.1f} GB)",
             "timed_steps_start_at": args.warmup}
 
 
@@ -424,6 +430,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", type=int, default=1, choices=[1, 3],
+                    help="1: 200 mm Kuhn cube, 1e7 ions (headline); 3: jittered plate box, 5e7 ions")
     ap.add_argument("--particles", type=int, default=10_000_000)
     ap.add_argument("--cells", type=int, default=100)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])

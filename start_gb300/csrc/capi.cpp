@@ -267,13 +267,14 @@ int upload_amg(spg_handle *h, const AmgHost &ah, const T *sval0, AmgDevT<T> &a) 
         std::vector<double> sv;
         const double avg = M.n ? double(M.ci.size()) / double(M.n) : 0.0;
         D.g = 0;
-        // FP64: one thread per row up to 48 entries per row, then 4 lanes per
-        // row (each FP64 shuffle add of a lane group costs a full warp
-        // instruction at the FP64 rate); FP32: lanes from 12 entries per row,
-        // about 4 entries per lane
+        // FP64: one thread per row up to 48 entries per row, then lanes with
+        // about 12 entries each (each FP64 shuffle add of a lane group costs a
+        // full warp instruction at the FP64 rate); FP32: lanes from 12
+        // entries per row, about 4 entries per lane
         if (sizeof(T) == 8 ? avg > 48.0 : avg > 12.0) {
+            const double per_lane = sizeof(T) == 8 ? 12.0 : 4.0;
             D.g = 4;
-            while (sizeof(T) == 4 && D.g < 32 && 4.0 * D.g < avg) D.g *= 2;
+            while (D.g < 32 && per_lane * D.g < avg) D.g *= 2;
             sp = M.rp;
             sc = M.ci;
             sv = M.v;

@@ -56,9 +56,10 @@ def test_amg_iterations_do_not_grow_with_the_mesh(built):
         e, phi, st = _solve_after_gather(w)
         its.append(st["cg_iters_last"])
         e.close()
-    # SA-AMG with a fixed smoother degree grows slowly with the mesh; Jacobi
-    # grows with 1/h (about 80 -> 160 -> 320 here)
-    assert max(its) <= 30 and its[-1] <= 2 * its[0], its
+    # SA-AMG with a fixed smoother degree grows slowly with the mesh (the
+    # 20^3 mesh is almost all coarsest level); Jacobi doubles with each
+    # halving of h (about 80 -> 160 -> 320 here)
+    assert max(its) <= 30 and its[2] <= 1.5 * its[1], its
 
 
 def test_amg_potential_matches_oracle(built):
