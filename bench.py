@@ -300,12 +300,14 @@ def run_gpu(args):
         ps = int(c.item())
     value = ps / (ms / 1e3)
     peak, peak_src = measured_peak()
+    sfx = "32" if args.precision == "mixed" else "64"
     phases = {
-        "step": ("k_step64 + k_walk_queue64 (push, move, collide, walk, settle)", prof["step_ms"],
+        "step": (f"k_step{sfx} + k_walk_queue{sfx} (push, move, collide, walk, settle)", prof["step_ms"],
                  prof["step_bytes"], prof["step_launches"]),
-        "pcg": ("PCG iteration kernels (SELL-32 SpMV + dots, updates)", prof["pcg_ms"], prof["pcg_bytes"],
+        "pcg": ("PCG iterations (SELL-32 SpMV + dots, updates"
+                + (", AMG V-cycle)" if args.precond == "amg" else ")"), prof["pcg_ms"], prof["pcg_bytes"],
                 prof["pcg_iters"]),
-        "deposit": ("k_deposit64 (fixed-point P1 deposit)", prof["deposit_ms"], prof["deposit_bytes"],
+        "deposit": (f"k_deposit{sfx} (fixed-point P1 deposit)", prof["deposit_ms"], prof["deposit_bytes"],
                     prof["deposit_launches"]),
     }
     dom = max(phases, key=lambda k: phases[k][1])

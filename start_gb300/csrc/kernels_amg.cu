@@ -1,9 +1,10 @@
 // V-cycle of the smoothed-aggregation AMG preconditioner (hierarchy from
-// amg_setup.cpp). Per level: Chebyshev pre-smoothing of degree 2 from a zero
+// amg_setup.cpp). Per level: Jacobi-Chebyshev pre-smoothing from a zero
 // guess, residual, restriction R = P^T, the coarser level, prolongation, and
-// Chebyshev post-smoothing of degree 2; the coarsest level multiplies by its
-// dense inverse. Pre- and post-smoother are the same polynomial in D^-1 A, so
-// the V-cycle is a symmetric positive definite operator and CG stays CG.
+// post-smoothing with the same polynomial (degree 1, damped Jacobi, or
+// degree 2, per level); the coarsest level multiplies by its dense inverse.
+// Pre- and post-smoother are the same polynomial in D^-1 A, so the V-cycle
+// is a symmetric positive definite operator and CG stays CG.
 // Operators with short rows are stored SELL-32 with one thread per row (level
 // 0 shares the solver's matrix); long rows (coarse operators, restriction)
 // CSR with 4-32 lanes per row. No atomics, so z = M^-1 r is deterministic.

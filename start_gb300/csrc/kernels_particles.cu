@@ -19,6 +19,7 @@
 
 #include "philox.h"
 #include "deposit.cuh"
+#include "exact_div.h"
 #include "spg_internal.h"
 
 namespace spg {
@@ -82,35 +83,18 @@ __device__ __forceinline__ bool same_value(double a, double b) {
 }
 
 // Screened inside test: true = lambda(p) >= 0 in all four coordinates for
-// certain; false = undecided (the caller evaluates the exact FP64 walk).
-// The FP32 barycentrics use d = p - x0 (the exact FP64 subtraction of the
-// oracle) and M, d truncated to 20 mantissa bits, so each product carries a
-// relative error below 2^-19 + 3*2^-24; with S_i = sum_j |M_ij d_j| the
-// FP32 value is within 2.2e-6 S_i of the FP64 one. The margin used is
-// 4e-6 S_i + 1e-30 (for terms flushed to zero), and lambda_0 = 1 - sum gets
-// the sum of the three margins plus 1e-6 for its own FP32 rounding.
-__device__ __forceinline__ bool inside_sure(const TetGeo &g, double d0, double d1, double d2) {
-    const float e0 = hi_float(d0), e1 = hi_float(d1), e2 = hi_float(d2);
-    float l[3], b[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        const float m0 = hi_float(g.M[3 * r]), m1 = hi_float(g.M[3 * r + 1]), m2 = hi_float(g.M[3 * r + 2]);
-        l[r] = fmaf(m2, e2, fmaf(m1, e1, m0 * e0));
-        const float s = fmaf(fabsf(m2), fabsf(e2), fmaf(fabsf(m1), fabsf(e1), fabsf(m0) * fabsf(e0)));
-        b[r] = fmaf(4e-6f, s, 1e-30f);
-    }
-    const float l0 = 1.0f - l[0] - l[1] - l[2];
-    const float b0 = b[0] + b[1] + b[2] + 1e-6f;
-    return l[0] > b[0] && l[1] > b[1] && l[2] > b[2] && l0 > b0;
-}
-
-// The same screen from the position itself, with no FP64 instruction: d is
-// formed in FP32 from p and x0 truncated to 20 mantissa bits (integer ops).
+// certain; false = undecided (the caller evaluates the exact FP64 walk). No
+// FP64 instruction runs: M is truncated to 20 mantissa bits and
+// d = p - x0 is formed in FP32 from p and x0 truncated the same way (integer
+// ops). With S_i = sum_j |M_ij d_j|, the truncation of M and the FP32
+// products put lambda_i within 2.2e-6 S_i of its value for the exact d; the
+// margin takes 4e-6 S_i + 1e-30 (for terms flushed to zero).
 // |p - pf| < 2^-20 |p| <= 9.6e-7 |pf| (pf truncates toward zero) and the FP32
 // difference rounds by at most 2^-24 |d_f|, so each d_k is within
 // delta_k = 9.6e-7 (|pf_k| + |x0f_k|) + 6e-8 |d_fk| + 1e-30 of p_k - x0_k.
 // That adds sum_k |M_ik| delta_k (times 1.01 for the truncation of M) to the
-// margin of lambda_i.
+// margin of lambda_i; lambda_0 = 1 - sum gets the sum of the three margins
+// plus 1e-6 for its own FP32 rounding.
 __device__ __forceinline__ bool inside_sure_pos(const TetGeo &g, double px, double py, double pz) {
     const float pf[3] = {hi_float(px), hi_float(py), hi_float(pz)};
     float e[3], dl[3];
@@ -512,7 +496,7 @@ __global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix,
 // sign and scale of E = -grad(phi)), plus the push increment
 // H = ((q E / m) dt) / 2, the operations of Particle::electroMagneticPush.
 __global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, double *__restrict__ efield,
-                           const double *__restrict__ phi, double charge, double mass, double dt) {
+                           const double *__restrict__ phi, double charge, double mass, double inv_mass, double dt) {
     const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= m.n_tets) return;
     const int4 tn = __ldg(m.tet_nodes + t);
@@ -525,7 +509,7 @@ __global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, double *__restri
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         efield[3 * t + k] = E[k];
-        const double a = (charge * E[k]) / mass;
+        const double a = div_by_known(charge * E[k], mass, inv_mass);  // (q E) / m
         r.H[k] = (a * dt) / 2.0;
     }
     r.ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
@@ -772,7 +756,7 @@ void launch_fix_to_charge(const unsigned long long *node_fix, double scale, doub
 
 void launch_efield64(const MeshDev &m, TetRec *rec, double *efield, const double *phi, double charge, double mass,
                      double dt, cudaStream_t s) {
-    k_efield64<<<grid_for(m.n_tets, 256), 256, 0, s>>>(m, rec, efield, phi, charge, mass, dt);
+    k_efield64<<<grid_for(m.n_tets, 256), 256, 0, s>>>(m, rec, efield, phi, charge, mass, 1.0 / mass, dt);
 }
 
 void launch_zero_efield(TetRec *rec, double *efield, int64_t n_tets, cudaStream_t s) {
