@@ -207,9 +207,11 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes);
  * (The reference sets them once from its config, MatrixBoundaryConditionsManager.) */
 int spg_set_dirichlet(spg_handle *h, const double *g);
 
-/* Gradient of a smoothed landing objective through the particle steps (FP64
- * form; collisions none/HS/VHS with their events and random numbers held
- * fixed). spg_grad_forward runs nsteps particle steps in the current field
+/* Gradient of a smoothed landing objective through the particle steps, of
+ * the FP64 form or of the mixed form's FP32 step (collisions none/HS/VHS,
+ * with their events and random numbers held fixed; the cell whose field
+ * pushes each step also counts as fixed: the field is constant per tet).
+ * spg_grad_forward runs nsteps particle steps in the current field
  * (no deposit or solve), keeping the particle state every checkpoint_every
  * steps and where each particle lands, and returns
  *   J = (1/N) sum over the N particles that landed of exp(-|r - target|^2 / (2 sigma^2)).

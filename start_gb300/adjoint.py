@@ -34,7 +34,7 @@ class LandingSetup:
     landing problem; no device state (the oracle tests reuse it)."""
 
     def __init__(self, n_particles=1_000_000, cells=25, steps=300, seed=1, sigma=0.01, checkpoint_every=32,
-                 collisions=True, energy_ev=1.0, gas_scale=1.0, cg_rtol=1e-12, preconditioner=0):
+                 collisions=True, energy_ev=1.0, gas_scale=1.0, cg_rtol=1e-12, preconditioner=0, precision=0):
         L = 0.1
         self.mesh = M.kuhn_box((cells,) * 3, (L,) * 3)
         owner = np.full(self.mesh.n_nodes, -1)
@@ -47,7 +47,7 @@ class LandingSetup:
         self.target = np.array([L / 2, L / 2, L])
         self.params = _base_params(dt=1e-8, weight=1e6, seed=seed, collision_model=1 if collisions else 0,
                                    gas_concentration=gas_concentration(1.0, 300.0) * gas_scale, cg_rtol=cg_rtol,
-                                   resort_every=0, preconditioner=preconditioner)
+                                   resort_every=0, preconditioner=preconditioner, precision=precision)
         rng = np.random.default_rng(seed)
         self.p_disk = disk_points(rng, n_particles, (L / 2, L / 2, 0.0), 0.02)
         self.u1 = rng.random(n_particles)

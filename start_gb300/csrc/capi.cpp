@@ -153,6 +153,7 @@ struct spg_handle {
     AdjHist hist{};
     unsigned int *tri_scratch = nullptr;
     DevCounters *ctr_scratch = nullptr;
+    std::vector<DevParticles32> ckpt32;  // the same for the FP32 form
     int64_t ckpt_cap = 0, land_cap = 0, hist_cap = 0;  // particles (x window steps for hist) allocated
     double grad_inv_n = 0.0;                            // 1 / landed count of the last forward
     bool grad_ready = false;
@@ -1071,6 +1072,10 @@ int spg_destroy(spg_handle *h) {
         for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
                         (void *)P.tet, (void *)P.idf})
             cudaFree(q);
+    for (auto &P : h->ckpt32)
+        for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
+                        (void *)P.tet, (void *)P.idf})
+            cudaFree(q);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return SPG_OK;
@@ -1511,6 +1516,39 @@ int alloc_dev_particles(spg_handle *h, DevParticles &P, int64_t n) {
     return SPG_OK;
 }
 
+int copy_particles32(spg_handle *h, const DevParticles32 &dst, const DevParticles32 &src, int64_t n) {
+    if (n == 0) return SPG_OK;
+    cudaStream_t s = h->stream;
+    for (int k = 0; k < 6; ++k) {
+        float *d = k == 0 ? dst.x : k == 1 ? dst.y : k == 2 ? dst.z : k == 3 ? dst.vx : k == 4 ? dst.vy : dst.vz;
+        const float *q = k == 0 ? src.x : k == 1 ? src.y : k == 2 ? src.z : k == 3 ? src.vx : k == 4 ? src.vy : src.vz;
+        CK(cudaMemcpyAsync(d, q, 4 * n, cudaMemcpyDeviceToDevice, s));
+    }
+    CK(cudaMemcpyAsync(dst.tet, src.tet, 4 * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(dst.idf, src.idf, 4 * n, cudaMemcpyDeviceToDevice, s));
+    return SPG_OK;
+}
+
+int alloc_dev_particles32(spg_handle *h, DevParticles32 &P, int64_t n) {
+    CK(dalloc(&P.x, n));
+    CK(dalloc(&P.y, n));
+    CK(dalloc(&P.z, n));
+    CK(dalloc(&P.vx, n));
+    CK(dalloc(&P.vy, n));
+    CK(dalloc(&P.vz, n));
+    CK(dalloc(&P.tet, n));
+    CK(dalloc(&P.idf, n));
+    return SPG_OK;
+}
+
+void free_particle_set32(std::vector<DevParticles32> &v) {
+    for (auto &P : v)
+        for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
+                        (void *)P.tet, (void *)P.idf})
+            cudaFree(q);
+    v.clear();
+}
+
 // Solves K x = b (b, x device vectors of n_nodes) with the FP64 PCG of spg_solve.
 int solve_into(spg_handle *h, double *b, double *x, int32_t *iters) {
     PcgScalars init{};
@@ -1559,7 +1597,6 @@ int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, co
                      double *J, int64_t *n_landed) {
     if (!h || !target || !(sigma > 0.0) || nsteps < 1 || checkpoint_every < 1)
         return fail(h, SPG_E_INVALID, "grad_forward: bad arguments");
-    if (h->mixed) return fail(h, SPG_E_INVALID, "grad_forward: the adjoint is available in the FP64 form");
     if (h->prm.collision_model == SPG_COLL_VSS)
         return fail(h, SPG_E_INVALID, "grad_forward: VSS scattering has no adjoint here (HS, VHS or none)");
     if (!h->have_particles) return fail(h, SPG_E_STATE, "grad_forward: no particles set");
@@ -1568,12 +1605,20 @@ int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, co
     int rc;
     const int nck = (nsteps + checkpoint_every - 1) / checkpoint_every;
     h->grad_ready = false;
-    if (int(h->ckpt.size()) < nck || n > h->ckpt_cap) {
+    const size_t have = h->mixed ? h->ckpt32.size() : h->ckpt.size();
+    if (int(have) < nck || n > h->ckpt_cap) {
         free_particle_set(h->ckpt);
+        free_particle_set32(h->ckpt32);
         h->ckpt_cap = 0;
-        h->ckpt.assign(nck, DevParticles{});
-        for (auto &P : h->ckpt)
-            if ((rc = alloc_dev_particles(h, P, std::max<int64_t>(n, 1)))) return rc;
+        if (h->mixed) {
+            h->ckpt32.assign(nck, DevParticles32{});
+            for (auto &P : h->ckpt32)
+                if ((rc = alloc_dev_particles32(h, P, std::max<int64_t>(n, 1)))) return rc;
+        } else {
+            h->ckpt.assign(nck, DevParticles{});
+            for (auto &P : h->ckpt)
+                if ((rc = alloc_dev_particles(h, P, std::max<int64_t>(n, 1)))) return rc;
+        }
         h->ckpt_cap = std::max<int64_t>(n, 1);
     }
     if (n > h->land_cap) {
@@ -1598,16 +1643,27 @@ int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, co
     h->grad_every = checkpoint_every;
     h->grad_step0 = h->step;
     for (int k = 0; k < nsteps; ++k) {
-        if (k % checkpoint_every == 0)
-            if ((rc = copy_particles(h, h->ckpt[k / checkpoint_every], h->P[h->cur], n))) return rc;
+        if (k % checkpoint_every == 0) {
+            const int w = k / checkpoint_every;
+            rc = h->mixed ? copy_particles32(h, h->ckpt32[w], h->Q[h->cur], n)
+                          : copy_particles(h, h->ckpt[w], h->P[h->cur], n);
+            if (rc) return rc;
+        }
         StepConst c = step_const(h);
-        launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
-                      h->stream, h->land);
+        if (h->mixed)
+            launch_step32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
+                          h->stream, h->land);
+        else
+            launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
+                          h->stream, h->land);
         CK(cudaGetLastError());
         h->step++;
     }
     CK(cudaMemsetAsync(h->sums, 0, 2 * sizeof(double), h->stream));
-    launch_objective(h->P[h->cur], n, h->land, target, sigma, h->gr, h->sums, h->stream);
+    if (h->mixed)
+        launch_objective32(h->Q[h->cur], n, mesh_dev32(h), h->land, target, sigma, h->gr, h->sums, h->stream);
+    else
+        launch_objective(h->P[h->cur], n, h->land, target, sigma, h->gr, h->sums, h->stream);
     CK(cudaGetLastError());
     double sums[2];
     CK(cudaMemcpyAsync(sums, h->sums, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
@@ -1643,21 +1699,32 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
     CK(cudaMemsetAsync(h->adj_v, 0, sizeof(double) * 3 * n, s));
     CK(cudaMemsetAsync(h->gE, 0, sizeof(double) * 3 * h->n_tets, s));
     DevParticles &work = h->P[1 - h->cur];
+    DevParticles32 &work32 = h->Q[1 - h->cur];
     const int nck = (h->grad_steps + W - 1) / W;
     for (int w = nck - 1; w >= 0; --w) {
         const int k0 = w * W, k1 = std::min(h->grad_steps, k0 + W);
-        if ((rc = copy_particles(h, work, h->ckpt[w], n))) return rc;
+        rc = h->mixed ? copy_particles32(h, work32, h->ckpt32[w], n) : copy_particles(h, work, h->ckpt[w], n);
+        if (rc) return rc;
         CK(cudaMemsetAsync(h->ctr_scratch, 0, sizeof(DevCounters), s));
         for (int k = k0; k < k1; ++k) {
-            launch_record(work, n, h->hist, k - k0, s);
             StepConst c = step_const(h);
             c.step = h->grad_step0 + k;
-            launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
+            if (h->mixed) {
+                launch_record32(work32, n, h->hist, k - k0, s);
+                launch_step32(work32, n, mesh_dev32(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
+            } else {
+                launch_record(work, n, h->hist, k - k0, s);
+                launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
+            }
         }
         StepConst c = step_const(h);
         c.step = h->grad_step0;  // absolute step of k = 0 (landing steps and Philox counters are absolute)
-        launch_backward(work, n, h->hist, k0, k1, h->rec, h->land, h->gr, h->grad_inv_n, h->adj_x, h->adj_v, h->gE,
-                        c, s);
+        if (h->mixed)
+            launch_backward32(work32, n, mesh_dev32(h), h->hist, k0, k1, h->land, h->gr, h->grad_inv_n, h->adj_x,
+                              h->adj_v, h->gE, c, s);
+        else
+            launch_backward(work, n, h->hist, k0, k1, h->rec, h->land, h->gr, h->grad_inv_n, h->adj_x, h->adj_v,
+                            h->gE, c, s);
         CK(cudaGetLastError());
     }
     CK(cudaMemsetAsync(h->lam, 0, sizeof(double) * h->n_nodes, s));
@@ -1675,7 +1742,10 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
         double *dx = nullptr, *dv = nullptr;
         if (dJ_dx0) CK(dalloc(&dx, 3 * n));
         if (dJ_dv0) CK(dalloc(&dv, 3 * n));
-        launch_gather_adj(h->P[h->cur], n, h->adj_x, h->adj_v, dx, dv, s);
+        if (h->mixed)
+            launch_gather_adj32(h->Q[h->cur], n, h->adj_x, h->adj_v, dx, dv, s);
+        else
+            launch_gather_adj(h->P[h->cur], n, h->adj_x, h->adj_v, dx, dv, s);
         if (dJ_dx0) CK(cudaMemcpyAsync(dJ_dx0, dx, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
         if (dJ_dv0) CK(cudaMemcpyAsync(dJ_dv0, dv, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));

@@ -51,18 +51,20 @@ SPG_XHD inline double div_by_known(double x, double m, double r) {
     const int eq = int((qb0 >> 52) & 0x7ff);
     const long long mb = as_bits(m);
     const int em = int((mb >> 52) & 0x7ff);
-    if (x == 0.0 || eq < 64 || eq > 2000 || em + eq < 1140 || em + eq > 3000) return x / m;
+    // (x == 0 is a zero exponent of x r; the tests below are integer operations)
+    if (eq < 64 || eq > 2000 || em + eq < 1140 || em + eq > 3000) return x / m;
     const double q0 = from_bits(qb0);
     const double q1 = std::fma(std::fma(-q0, m, x), r, q0);
     const double e1 = std::fma(-q1, m, x);  // exact: q1 is faithful
-    const long long b1 = as_bits(q1);
+    const long long b1 = as_bits(q1), be = as_bits(e1);
     const int e = int((b1 >> 52) & 0x7ff);
-    const bool away = (e1 > 0.0) == (q1 > 0.0);  // the true quotient lies farther from zero
+    // the true quotient lies farther from zero: e1 nonzero with the sign of q1
+    const bool away = (be << 1) != 0 && ((be ^ b1) >= 0);
     const bool pow2 = (b1 & 0xFFFFFFFFFFFFFLL) == 0;
     // m ulp(q1) / 2 = m 2^(e - 1076); toward zero from a power of two: m 2^(e - 1077)
     const int sh = (!away && pow2) ? e - 1077 : e - 1076;
     const long long lim = (mb & 0x7fffffffffffffffLL) + ((long long)sh << 52);
-    const long long ae = as_bits(e1) & 0x7fffffffffffffffLL;
+    const long long ae = be & 0x7fffffffffffffffLL;
     if (ae < lim || (ae == lim && (pow2 || !(b1 & 1)))) return q1;
     return from_bits(away ? b1 + 1 : b1 - 1);
 }

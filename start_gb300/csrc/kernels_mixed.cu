@@ -100,8 +100,9 @@ __device__ __forceinline__ void rebase(const double *__restrict__ cen, int ta, i
 }
 
 struct Walk32 {
-    int tet, status, tri, crossings;
+    int tet, status, tri, crossings, face;
     float hx, hy, hz;  // end (or hit) point in the final tet's frame
+    float s;           // crossing parameter of the hit (W_SURFACE)
 };
 
 // Segment walk in local frames: p0, p1 are given in tet t's frame and are
@@ -112,6 +113,8 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
     Walk32 o;
     o.crossings = 0;
     o.tri = -1;
+    o.face = -1;
+    o.s = 1.0f;
     int enter = -1;
     Geo32 g;
     load_geo32(a.rec, t, g);
@@ -151,6 +154,8 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
             o.tet = t;
             o.status = W_SURFACE;
             o.tri = tri;
+            o.face = best;
+            o.s = sb;
             o.hx = fmaf(sb, p1x - p0x, p0x);
             o.hy = fmaf(sb, p1y - p0y, p0y);
             o.hz = fmaf(sb, p1z - p0z, p0z);
@@ -175,26 +180,33 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
     }
 }
 
-// Collision in FP32 (same Philox streams and laws as the FP64 form).
-__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, float &vx, float &vy, float &vz) {
-    const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
+// FP32 collision decision of step `step` (u0 < P) and, on a hit, the
+// scattering direction's cosine xc, sine xs and azimuth (cos, sin).
+__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, float vx, float vy,
+                                                  float vz, float &xc, float &xs, float &cp, float &sp) {
+    const Philox4 r = collision_draw(step, 0u, id, c.seed_lo, c.seed_hi);
     const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
     const float P = c.kp_f * exp2f(c.pexp_f * log2f(v2));
     const float u0 = float(r.v[0] >> 8) * 5.9604644775390625e-8f;
     if (!(u0 < P)) return false;
     const float u1 = float(r.v[2] >> 8) * 5.9604644775390625e-8f;
-    const Philox4 r2 = collision_draw(uint64_t(c.step), 1u, id, c.seed_lo, c.seed_hi);
+    const Philox4 r2 = collision_draw(step, 1u, id, c.seed_lo, c.seed_hi);
     const float u2 = float(r2.v[0] >> 8) * 5.9604644775390625e-8f;
-    float xc;
     if (c.model == SPG_COLL_HS)
         xc = -1.0f + 2.0f * u1;
     else if (c.model == SPG_COLL_VHS)
         xc = u1;
     else
         xc = 2.0f * powf(u1, float(c.inv_alpha)) - 1.0f;
-    const float xs = sqrtf(fmaxf(0.0f, 1.0f - xc * xc));
-    float sp, cp;
+    xs = sqrtf(fmaxf(0.0f, 1.0f - xc * xc));
     sincosf((2.0f * kPiF) * u2, &sp, &cp);
+    return true;
+}
+
+// Collision in FP32 (same Philox streams and laws as the FP64 form).
+__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, float &vx, float &vy, float &vz) {
+    float xc, xs, cp, sp;
+    if (!collision_event32(c, id, uint64_t(c.step), vx, vy, vz, xc, xs, cp, sp)) return false;
     const float mcp = float(c.mass_cp), mct = float(c.mass_ct);
     const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
     const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
@@ -298,9 +310,12 @@ __global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkIt
     }
 }
 
+// With land != nullptr a particle that settles records the step, the exit
+// face, its tet and the hit fraction (adjoint).
 __global__ void __launch_bounds__(128) k_walk_queue32(MixedArgs a, int max_cross, const WalkItem32 *__restrict__ wq,
                                                       const unsigned int *__restrict__ wq_n,
-                                                      unsigned int *__restrict__ tri_count, DevCounters *ctr) {
+                                                      unsigned int *__restrict__ tri_count, DevCounters *ctr,
+                                                      LandRec *__restrict__ land, int64_t step) {
     const unsigned nq = *wq_n;
     unsigned cross = 0, settled = 0, lost = 0, capped = 0;
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
@@ -317,6 +332,12 @@ __global__ void __launch_bounds__(128) k_walk_queue32(MixedArgs a, int max_cross
             atomicAdd(tri_count + w.tri, 1u);
             a.p.idf[i] = idf | kSettled;
             settled++;
+            if (land) {
+                land[i].step = int32_t(step);
+                land[i].face = w.face;
+                land[i].tet = w.tet;
+                land[i].s = double(w.s);
+            }
         } else if (w.status != W_INSIDE) {
             a.p.idf[i] = idf | kLost;
             lost++;
@@ -470,6 +491,155 @@ __global__ void k_sort_scatter32(DevParticles32 src, DevParticles32 dst, int64_t
 
 inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1) / block); }
 
+// ------------------------------------------------------------ adjoint (FP32 form)
+// The gradient of the FP32 step itself: the recorded FP32 velocities and the
+// FP32 push increments rebuild the pushed velocity exactly as the forward
+// computed it, and the adjoint recursion (the one of the FP64 form, see
+// kernels_adjoint.cu) runs in FP64 on those values. Collision events are the
+// FP32 form's own decisions, recomputed from the same FP32 velocity.
+
+__global__ void k_record32(DevParticles32 p, int64_t n, AdjHist h, int k) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t o = int64_t(k) * n + i;
+    h.tet[o] = (p.idf[i] & kDead) ? -1 : p.tet[i];
+    h.vx[o] = double(p.vx[i]);
+    h.vy[o] = double(p.vy[i]);
+    h.vz[o] = double(p.vz[i]);
+}
+
+// dg/dr of each landed particle (r = centroid + local position, in FP64) and
+// the sums of g and of the landed count.
+__global__ void k_objective32(MixedArgs a, const LandRec *__restrict__ land, double tx, double ty, double tz,
+                              double inv_2s2, double *__restrict__ gr, double *__restrict__ sums) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double g = 0.0, cnt = 0.0;
+    if (i < a.n) {
+        gr[3 * i] = gr[3 * i + 1] = gr[3 * i + 2] = 0.0;
+        if ((a.p.idf[i] & kSettled) && land[i].step >= 0) {
+            const int t = a.p.tet[i];
+            const double dx = (a.cen[3 * t] + double(a.p.x[i])) - tx;
+            const double dy = (a.cen[3 * t + 1] + double(a.p.y[i])) - ty;
+            const double dz = (a.cen[3 * t + 2] + double(a.p.z[i])) - tz;
+            g = exp(-(dx * dx + dy * dy + dz * dz) * inv_2s2);
+            const double f = -2.0 * inv_2s2 * g;
+            gr[3 * i] = f * dx;
+            gr[3 * i + 1] = f * dy;
+            gr[3 * i + 2] = f * dz;
+            cnt = 1.0;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        g += __shfl_down_sync(kFull, g, off);
+        cnt += __shfl_down_sync(kFull, cnt, off);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt > 0.0) {
+        atomicAdd(sums, g);
+        atomicAdd(sums + 1, cnt);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int k0, int k1,
+                                                    const LandRec *__restrict__ land, const double *__restrict__ gr,
+                                                    double gscale, double *__restrict__ ax, double *__restrict__ av,
+                                                    double *__restrict__ gE, StepConst c, double cq) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int64_t n = a.n;
+    const LandRec L = land[i];
+    const int N = L.step < 0 ? -1 : int(int64_t(L.step) - c.step);
+    if (N < k0) return;
+    const uint32_t id = a.p.idf[i] & kIdMask;
+    double Ax = ax[3 * i], Ay = ax[3 * i + 1], Az = ax[3 * i + 2];
+    double Vx = av[3 * i], Vy = av[3 * i + 1], Vz = av[3 * i + 2];
+    const float vmin = float(c.vmin);
+    const double mcp = double(float(c.mass_cp)), mct = double(float(c.mass_ct));
+    int run = -1;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int k = min(k1 - 1, N); k >= k0; --k) {
+        const int64_t o = int64_t(k - k0) * n + i;
+        const int t = h.tet[o];
+        if (t < 0) continue;
+        float vx = float(h.vx[o]), vy = float(h.vy[o]), vz = float(h.vz[o]);
+        if (fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin) continue;  // the step did not move it
+        const TetRec32 &R = a.rec[t];
+        if (!R.ezero) {
+            vx = (vx + R.H[0]) + R.H[0];
+            vy = (vy + R.H[1]) + R.H[1];
+            vz = (vz + R.H[2]) + R.H[2];
+        }
+        const double wx = vx, wy = vy, wz = vz;  // pushed velocity, as the forward had it
+        double bx, by, bz;
+        if (k == N) {
+            const double *M = a.rec64[L.tet].M;  // exit-face normal from the FP64 map
+            double nn[3];
+            for (int q = 0; q < 3; ++q)
+                nn[q] = L.face == 0 ? -(M[q] + M[3 + q] + M[6 + q]) : M[3 * (L.face - 1) + q];
+            const double gx = gr[3 * i] * gscale, gy = gr[3 * i + 1] * gscale, gz = gr[3 * i + 2] * gscale;
+            const double nv = nn[0] * wx + nn[1] * wy + nn[2] * wz;
+            const double vg = (wx * gx + wy * gy + wz * gz) / nv;
+            Ax = gx - nn[0] * vg;
+            Ay = gy - nn[1] * vg;
+            Az = gz - nn[2] * vg;
+            const double sdt = L.s * c.dt;
+            bx = sdt * Ax;
+            by = sdt * Ay;
+            bz = sdt * Az;
+        } else {
+            float xc, xs, cp, sp;
+            if (c.model != SPG_COLL_NONE && collision_event32(c, id, uint64_t(c.step + k), vx, vy, vz, xc, xs, cp, sp)) {
+                // v' = m_cp v + m_ct |v| n:  J^T a = m_cp a + m_ct v/|v| (n . a)
+                const double vm = sqrt(wx * wx + wy * wy + wz * wz);
+                const double na = (double(xs * cp) * Vx + double(xs * sp) * Vy + double(xc) * Vz) * mct / vm;
+                Vx = mcp * Vx + na * wx;
+                Vy = mcp * Vy + na * wy;
+                Vz = mcp * Vz + na * wz;
+            }
+            bx = Vx + c.dt * Ax;
+            by = Vy + c.dt * Ay;
+            bz = Vz + c.dt * Az;
+        }
+        if (t != run) {
+            if (run >= 0) {
+                atomicAdd(gE + 3 * run, cq * sx);
+                atomicAdd(gE + 3 * run + 1, cq * sy);
+                atomicAdd(gE + 3 * run + 2, cq * sz);
+            }
+            run = t;
+            sx = sy = sz = 0.0;
+        }
+        sx += bx;
+        sy += by;
+        sz += bz;
+        Vx = bx;
+        Vy = by;
+        Vz = bz;
+    }
+    if (run >= 0) {
+        atomicAdd(gE + 3 * run, cq * sx);
+        atomicAdd(gE + 3 * run + 1, cq * sy);
+        atomicAdd(gE + 3 * run + 2, cq * sz);
+    }
+    ax[3 * i] = Ax;
+    ax[3 * i + 1] = Ay;
+    ax[3 * i + 2] = Az;
+    av[3 * i] = Vx;
+    av[3 * i + 1] = Vy;
+    av[3 * i + 2] = Vz;
+}
+
+__global__ void k_gather_adj32(DevParticles32 p, int64_t n, const double *__restrict__ ax,
+                               const double *__restrict__ av, double *dx, double *dv) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t id = p.idf[i] & kIdMask;
+    for (int k = 0; k < 3; ++k) {
+        if (dx) dx[3 * id + k] = ax[3 * i + k];
+        if (dv) dv[3 * id + k] = av[3 * i + k];
+    }
+}
+
 MixedArgs make_args(const DevParticles32 &p, int64_t n, const MeshDev32 &m) {
     MixedArgs a;
     a.p = p;
@@ -487,18 +657,44 @@ MixedArgs make_args(const DevParticles32 &p, int64_t n, const MeshDev32 &m) {
 }  // namespace
 
 void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c,
-                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s) {
+                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
+                   LandRec *land) {
     if (n <= 0) return;
     const MixedArgs a = make_args(p, n, m);
     cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
     k_step32<<<grid_for(n, 256), 256, 0, s>>>(a, c, static_cast<WalkItem32 *>(wq), wq_n, ctr);
-    k_walk_queue32<<<152 * 8, 128, 0, s>>>(a, c.max_cross, static_cast<WalkItem32 *>(wq), wq_n, tri_count, ctr);
+    k_walk_queue32<<<152 * 8, 128, 0, s>>>(a, c.max_cross, static_cast<WalkItem32 *>(wq), wq_n, tri_count, ctr,
+                                            land, c.step);
 }
 
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
                       cudaStream_t s) {
     if (n <= 0) return;
     k_deposit32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), k, node_fix);
+}
+
+void launch_record32(const DevParticles32 &p, int64_t n, const AdjHist &h, int k, cudaStream_t s) {
+    if (n > 0) k_record32<<<grid_for(n, 256), 256, 0, s>>>(p, n, h, k);
+}
+
+void launch_objective32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const LandRec *land,
+                        const double *target, double sigma, double *gr, double *sums, cudaStream_t s) {
+    if (n > 0)
+        k_objective32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), land, target[0], target[1], target[2],
+                                                        1.0 / (2.0 * sigma * sigma), gr, sums);
+}
+
+void launch_backward32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const AdjHist &h, int k0, int k1,
+                       const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
+                       const StepConst &c, cudaStream_t s) {
+    if (n > 0)
+        k_backward32<<<grid_for(n, 128), 128, 0, s>>>(make_args(p, n, m), h, k0, k1, land, gr, gscale, ax, av, gE, c,
+                                                       c.charge / c.mass * c.dt);
+}
+
+void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, const double *av, double *dx,
+                         double *dv, cudaStream_t s) {
+    if (n > 0) k_gather_adj32<<<grid_for(n, 256), 256, 0, s>>>(p, n, ax, av, dx, dv);
 }
 
 void launch_efield_mixed(const int4 *tet_nodes, const TetRec *rec64, TetRec32 *rec, double *efield, const double *phi,

@@ -512,7 +512,8 @@ __global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, double *__restri
         const double a = div_by_known(charge * E[k], mass, inv_mass);  // (q E) / m
         r.H[k] = (a * dt) / 2.0;
     }
-    r.ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
+    r.ezero = (((__double_as_longlong(E[0]) | __double_as_longlong(E[1]) | __double_as_longlong(E[2])) << 1) == 0)
+                  ? 1u : 0u;  // all three +-0
 }
 
 __global__ void k_zero_efield(TetRec *__restrict__ rec, double *__restrict__ efield, int64_t n) {

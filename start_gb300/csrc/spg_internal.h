@@ -244,7 +244,17 @@ struct MeshDev32 {
 
 // kernels_mixed.cu
 void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c,
-                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s);
+                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
+                   LandRec *land = nullptr);
+// adjoint of the FP32 form (kernels_mixed.cu)
+void launch_record32(const DevParticles32 &p, int64_t n, const AdjHist &h, int k, cudaStream_t s);
+void launch_objective32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const LandRec *land,
+                        const double *target, double sigma, double *gr, double *sums, cudaStream_t s);
+void launch_backward32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const AdjHist &h, int k0, int k1,
+                       const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
+                       const StepConst &c, cudaStream_t s);
+void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, const double *av, double *dx,
+                         double *dv, cudaStream_t s);
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
                       cudaStream_t s);
 void launch_efield_mixed(const int4 *tet_nodes, const TetRec *rec64, TetRec32 *rec, double *efield, const double *phi,
