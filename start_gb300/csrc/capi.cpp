@@ -473,6 +473,15 @@ StepConst step_const(const spg_handle *h) {
     }
     const double two_vmin = 2.0 * std::fabs(p.min_velocity);
     std::memcpy(&c.two_vmin_bits, &two_vmin, sizeof(two_vmin));
+    for (int k = 0; k < 3; ++k) {
+        c.lo_f[k] = float(c.lo[k]);
+        c.hi_f[k] = float(c.hi[k]);
+    }
+    c.vmin_f = float(c.vmin);
+    c.dt_f = float(c.dt);
+    c.mass_cp_f = float(c.mass_cp);
+    c.mass_ct_f = float(c.mass_ct);
+    c.inv_alpha_f = float(c.inv_alpha);
     // FP32 screen of P = sigma |v| n dt: HS kp (v^2)^(1/2); VHS/VSS
     // pi c1 (2 kT/m_r)^(w-1/2) n dt (v^2)^(1-w).
     if (p.collision_model == SPG_COLL_HS) {

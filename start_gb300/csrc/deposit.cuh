@@ -5,12 +5,13 @@
 // Each thread holds one particle's four fixed-point weights v[0..3] and its
 // tet (key, -1 for none). Consecutive threads hold consecutive particles of
 // the tet-sorted order, so equal keys form runs. A segmented shuffle scan
-// sums each run within a warp; thread 0 then chains the runs that cross warp
-// boundaries (a run can span several warps when a tet holds hundreds of
-// particles), and only the last lane of each run of the block adds the four
-// sums to the nodes. Integer sums do not depend on order, so the result is
-// the same as one atomic per particle; there are just far fewer atomics on
-// the few nodes of densely occupied tets.
+// sums each run within a warp; the last lane of each run adds its four sums
+// into a per-block hash table of nodes in shared memory, and the table is
+// flushed with one global atomic per distinct node. Runs that cross warps,
+// and runs of one tet broken up once particles have drifted since the last
+// re-sort, merge in the table, so a block issues about as many global
+// atomics as it touches nodes. Integer sums do not depend on order, so the
+// result is the same as one atomic per particle.
 #ifndef SPG_DEPOSIT_CUH
 #define SPG_DEPOSIT_CUH
 
@@ -22,10 +23,14 @@ template <int NT>
 __device__ __forceinline__ void deposit_block_flush(int key, long long v[4], const int4 *__restrict__ tet_nodes,
                                                     unsigned long long *__restrict__ node_fix) {
     constexpr unsigned kAll = 0xffffffffu;
-    constexpr int NW = NT / 32;
-    __shared__ int s_kf[NW], s_kl[NW], s_whole[NW];
-    __shared__ long long s_sl[NW][4], s_carry[NW][4];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int HS = 2 * NT;  // hash slots: node -> block sum
+    __shared__ int s_node[HS];
+    __shared__ unsigned long long s_sum[HS];
+    for (int k = threadIdx.x; k < HS; k += NT) {
+        s_node[k] = -1;
+        s_sum[k] = 0ull;
+    }
+    const int lane = threadIdx.x & 31;
     const int prev = __shfl_up_sync(kAll, key, 1);
     const bool head = lane == 0 || prev != key;
     const unsigned heads = __ballot_sync(kAll, head);
@@ -55,37 +60,35 @@ __device__ __forceinline__ void deposit_block_flush(int key, long long v[4], con
             v[q] = (long long)s0 + (long long)s1 * (1LL << 21) + (long long)s2 * (1LL << 42);
         }
     }
-    if (lane == 0) s_kf[w] = key;
-    if (lane == 31) {
-        s_kl[w] = key;
-        s_whole[w] = heads == 1u;
+    __syncthreads();  // the table is cleared
+    // The last lane of each run adds its four node sums to the block's table
+    // (open addressing, linear probing); a full table falls back to a global atomic.
+    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+    if (tail && key >= 0) {
+        const int4 tn = __ldg(tet_nodes + key);
+        const int nodes[4] = {tn.x, tn.y, tn.z, tn.w};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s_sl[w][q] = v[q];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s_carry[0][q] = 0;
-        for (int u = 1; u < NW; ++u) {
-            const bool cont = s_kf[u] >= 0 && s_kl[u - 1] == s_kf[u];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                s_carry[u][q] = cont ? s_sl[u - 1][q] + (s_whole[u - 1] ? s_carry[u - 1][q] : 0) : 0;
+        for (int q = 0; q < 4; ++q) {
+            const int node = nodes[q];
+            int h = int((unsigned(node) * 2654435761u) >> 8) & (HS - 1);
+            bool placed = false;
+            for (int probe = 0; probe < HS; ++probe) {
+                const int old = atomicCAS(&s_node[h], -1, node);
+                if (old == -1 || old == node) {
+                    atomicAdd(&s_sum[h], (unsigned long long)v[q]);
+                    placed = true;
+                    break;
+                }
+                h = (h + 1) & (HS - 1);
+            }
+            if (!placed) atomicAdd(node_fix + node, (unsigned long long)v[q]);
         }
     }
     __syncthreads();
-    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
-    if (!tail || key < 0) return;
-    if (lane == 31 && w + 1 < NW && s_kf[w + 1] == key) return;  // the run goes on in the next warp
-    const bool first_run = (heads & (kAll >> (31 - lane))) == 1u;
-    long long t[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) t[q] = v[q] + (first_run ? s_carry[w][q] : 0);
-    const int4 tn = __ldg(tet_nodes + key);
-    atomicAdd(node_fix + tn.x, (unsigned long long)t[0]);
-    atomicAdd(node_fix + tn.y, (unsigned long long)t[1]);
-    atomicAdd(node_fix + tn.z, (unsigned long long)t[2]);
-    atomicAdd(node_fix + tn.w, (unsigned long long)t[3]);
+    for (int k = threadIdx.x; k < HS; k += NT) {
+        const int node = s_node[k];
+        if (node >= 0) atomicAdd(node_fix + node, s_sum[k]);
+    }
 }
 
 }  // namespace spg

@@ -197,7 +197,7 @@ __device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t i
     else if (c.model == SPG_COLL_VHS)
         xc = u1;
     else
-        xc = 2.0f * powf(u1, float(c.inv_alpha)) - 1.0f;
+        xc = 2.0f * powf(u1, c.inv_alpha_f) - 1.0f;
     xs = sqrtf(fmaxf(0.0f, 1.0f - xc * xc));
     sincosf((2.0f * kPiF) * u2, &sp, &cp);
     return true;
@@ -207,7 +207,7 @@ __device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t i
 __device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, float &vx, float &vy, float &vz) {
     float xc, xs, cp, sp;
     if (!collision_event32(c, id, uint64_t(c.step), vx, vy, vz, xc, xs, cp, sp)) return false;
-    const float mcp = float(c.mass_cp), mct = float(c.mass_ct);
+    const float mcp = c.mass_cp_f, mct = c.mass_ct_f;
     const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
     const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
     float ex = xs * cp * mp, ey = xs * sp * mp, ez = xc * mp;
@@ -248,12 +248,12 @@ __global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkIt
             y = a.p.y[i];
             z = a.p.z[i];
             float vx = a.p.vx[i], vy = a.p.vy[i], vz = a.p.vz[i];
-            const float vmin = float(c.vmin);
+            const float vmin = c.vmin_f;
             const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
             const TetRec32 &R = a.rec[t];
             const float gx = __ldg(&R.cen[0]) + x, gy = __ldg(&R.cen[1]) + y, gz = __ldg(&R.cen[2]) + z;
-            const bool in_box = gx >= float(c.lo[0]) && gx <= float(c.hi[0]) && gy >= float(c.lo[1]) &&
-                                gy <= float(c.hi[1]) && gz >= float(c.lo[2]) && gz <= float(c.hi[2]);
+            const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
+                                gz >= c.lo_f[2] && gz <= c.hi_f[2];
             if (!slow && in_box) {
                 if (!__ldg(&R.ezero)) {
                     const float hx = __ldg(&R.H[0]), hy = __ldg(&R.H[1]), hz = __ldg(&R.H[2]);
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkIt
                     vy = (vy + hy) + hy;
                     vz = (vz + hz) + hz;
                 }
-                const float dt = float(c.dt);
+                const float dt = c.dt_f;
                 const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
                 if (!(nx == x && ny == y && nz == z)) {
                     if (c.model != SPG_COLL_NONE) coll = collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
@@ -553,8 +553,8 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
     const uint32_t id = a.p.idf[i] & kIdMask;
     double Ax = ax[3 * i], Ay = ax[3 * i + 1], Az = ax[3 * i + 2];
     double Vx = av[3 * i], Vy = av[3 * i + 1], Vz = av[3 * i + 2];
-    const float vmin = float(c.vmin);
-    const double mcp = double(float(c.mass_cp)), mct = double(float(c.mass_ct));
+    const float vmin = c.vmin_f;
+    const double mcp = double(c.mass_cp_f), mct = double(c.mass_ct_f);
     int run = -1;
     double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int k = min(k1 - 1, N); k >= k0; --k) {

@@ -123,6 +123,9 @@ struct StepConst {
     double inv_alpha;  // 1 / alpha
     uint32_t seed_lo, seed_hi;
     int64_t step;
+    // FP32 copies for the mixed form (rounded once on the host, so no thread
+    // spends FP64-pipe conversions on them)
+    float lo_f[3], hi_f[3], vmin_f, dt_f, mass_cp_f, mass_ct_f, inv_alpha_f;
 };
 
 struct MeshDev {
