@@ -172,6 +172,52 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
 int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_t *tet,
                       uint32_t *flags);
 
+/* Particle source sampled on the device, in place of ParticleGeneratorDevice
+ * (src/Generators/CUDA/ParticleGeneratorDevice.cu:95-304) and the host sampling of
+ * ParticleDynamicUtils.hpp:52-97: points uniform over a disk or a rectangle,
+ * directions uniform in a cone or Lambert (cosine) about the normal, energies
+ * monoenergetic or Thompson f(E) ~ E/(E+U)^3 truncated at E_max, then the
+ * ParticleDisplacer shift (src/Particle/ParticleDisplacer.cpp:20-35):
+ * p += d / max|d_k| * displacement. Particle i draws from Philox4x32-10 keyed
+ * by (seed) and counted by (i, block), so a source is reproducible and does
+ * not depend on the launch shape. */
+typedef enum spg_source_shape { SPG_SRC_DISK = 0, SPG_SRC_RECT = 1 } spg_source_shape;
+typedef enum spg_source_directions { SPG_DIR_CONE = 0, SPG_DIR_COSINE = 1 } spg_source_directions;
+typedef enum spg_source_energy { SPG_ENERGY_MONO = 0, SPG_ENERGY_THOMPSON = 1 } spg_source_energy;
+typedef struct spg_source {
+    int32_t shape;        /* spg_source_shape */
+    int32_t directions;   /* spg_source_directions */
+    int32_t energy;       /* spg_source_energy */
+    int32_t reserved0;
+    double centre[3];     /* disk centre [m] */
+    double normal[3];     /* disk normal; directions are about it (rectangles: +z) */
+    double radius;        /* disk radius [m] */
+    double xlim[2], ylim[2], z; /* rectangle in the plane z = const [m] */
+    double half_angle;    /* cone half-angle [rad] */
+    double energy_ev;     /* monoenergetic energy [eV] */
+    double binding_ev;    /* Thompson U [eV] */
+    double emax_ev;       /* Thompson truncation [eV] */
+    double displacement;  /* shift along the direction [m]; 0.05 mm in the reference */
+    uint64_t seed;
+} spg_source;
+void spg_default_source(spg_source *src);
+
+/* Trajectory sampling, in place of ParticleMovementTracker::recordMovement
+ * (src/ParticleInCellEngine/ParticleDynamicsProcessor/ParticleMovementTracker.cpp:4-16):
+ * the k particles ids[] (0 <= id < n) have their position appended before
+ * every step in which they are alive, up to `capacity` positions each. A new
+ * particle set, a restore, or k = 0 ends the tracking.
+ * spg_get_tracks: counts [k], xyz [k * capacity * 3] (row t holds counts[t]
+ * positions), and each tracked particle's current position and flags; a
+ * settled particle's current position is its surface hit point, the last
+ * point the reference's surface handler records. Any output may be NULL. */
+int spg_track_particles(spg_handle *h, int32_t k, const int64_t *ids, int32_t capacity);
+int spg_get_tracks(spg_handle *h, int32_t *counts, double *xyz, double *last_xyz, uint32_t *last_flags);
+/* Samples n particles of mass params.mass on the device and installs them as
+ * spg_set_particles does (location, LOST flags, reset of step, counters and
+ * potential); nothing crosses the host link. */
+int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src);
+
 /* (a) P1 charge deposit of all alive particles; rho_out [n_nodes] C/m^3 (nullable). */
 int spg_gather(spg_handle *h, double *rho_out);
 /* (b) Poisson solve K phi = rho*Vdual/eps0 with Dirichlet lifting, warm started

@@ -57,6 +57,21 @@ class Params(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Source(C.Structure):
+    _fields_ = [
+        ("shape", C.c_int32), ("directions", C.c_int32), ("energy", C.c_int32), ("reserved0", C.c_int32),
+        ("centre", C.c_double * 3), ("normal", C.c_double * 3), ("radius", C.c_double),
+        ("xlim", C.c_double * 2), ("ylim", C.c_double * 2), ("z", C.c_double),
+        ("half_angle", C.c_double), ("energy_ev", C.c_double), ("binding_ev", C.c_double),
+        ("emax_ev", C.c_double), ("displacement", C.c_double), ("seed", C.c_uint64),
+    ]
+
+
+SPG_SRC_DISK, SPG_SRC_RECT = 0, 1
+SPG_DIR_CONE, SPG_DIR_COSINE = 0, 1
+SPG_ENERGY_MONO, SPG_ENERGY_THOMPSON = 0, 1
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("step", C.c_int64), ("n_particles", C.c_int64), ("n_alive", C.c_int64), ("n_settled", C.c_int64),
@@ -93,6 +108,10 @@ SIGNATURES = {
     "spg_destroy": (C.c_int, [_H]),
     "spg_mesh_info": (C.c_int, [_H, C.POINTER(C.c_int64)]),
     "spg_set_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32]),
+    "spg_default_source": (None, [C.POINTER(Source)]),
+    "spg_generate_particles": (C.c_int, [_H, C.c_int64, C.POINTER(Source)]),
+    "spg_track_particles": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
+    "spg_get_tracks": (C.c_int, [_H, _pi32, _pd, _pd, C.POINTER(C.c_uint32)]),
     "spg_get_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32, C.POINTER(C.c_uint32)]),
     "spg_gather": (C.c_int, [_H, _pd]),
     "spg_solve": (C.c_int, [_H, _pd, _pd, _pi32, _pd]),

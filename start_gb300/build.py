@@ -45,6 +45,8 @@ def _sources():
         ("noalloc.cu", common_nv),
         ("kernels_adjoint.cu", common_nv + ["--fmad=false"]),
         ("kernels_amg.cu", common_nv),
+        ("kernels_sources.cu", common_nv),
+        ("kernels_track.cu", common_nv),
         ("mesh_prep.cpp", common_cc + ["-fopenmp"]),
         ("amg_setup.cpp", common_cc + ["-O3", "-fopenmp"]),
         ("capi.cpp", common_cc),

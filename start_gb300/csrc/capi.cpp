@@ -87,6 +87,12 @@ struct spg_handle {
     // (3 kernels each); converged solves turn the remaining kernels into no-ops.
     cudaGraphExec_t pcg_graph = nullptr;
     // AMG preconditioner (prm.preconditioner == SPG_PRECOND_AMG)
+    // trajectory sampling (spg_track_particles)
+    int32_t track_k = 0, track_cap = 0;
+    int64_t *track_ids = nullptr;
+    int32_t *track_of_id = nullptr, *track_slot = nullptr, *track_count = nullptr;
+    double *track_xyz = nullptr, *track_cur = nullptr;
+    uint32_t *track_flags = nullptr;
     bool amg = false, amg32 = false;
     AmgDev amgd{};
     AmgDev32 amgd32{};
@@ -783,7 +789,38 @@ int do_solve(spg_handle *h) {
     return h->mixed ? do_solve_mixed(h) : do_solve64(h);
 }
 
+// Appends the position of each tracked particle that is still alive (before
+// the step, as the reference records it before the move).
+int record_tracks(spg_handle *h) {
+    const uint32_t *idf = h->mixed ? h->Q[h->cur].idf : h->P[h->cur].idf;
+    launch_track_find(idf, h->np, h->track_of_id, h->track_slot, h->stream);
+    if (h->mixed)
+        launch_track_record32(h->Q[h->cur], h->cen, h->track_slot, h->track_k, h->track_cap, h->track_count,
+                              h->track_xyz, h->stream);
+    else
+        launch_track_record64(h->P[h->cur], h->track_slot, h->track_k, h->track_cap, h->track_count, h->track_xyz,
+                              h->stream);
+    h->launches += 2;
+    CK(cudaGetLastError());
+    return SPG_OK;
+}
+
+void free_tracks(spg_handle *h) {
+    for (void *q : {(void *)h->track_ids, (void *)h->track_of_id, (void *)h->track_slot, (void *)h->track_count,
+                    (void *)h->track_xyz, (void *)h->track_cur, (void *)h->track_flags})
+        cudaFree(q);
+    h->track_ids = nullptr;
+    h->track_of_id = h->track_slot = h->track_count = nullptr;
+    h->track_xyz = h->track_cur = nullptr;
+    h->track_flags = nullptr;
+    h->track_k = h->track_cap = 0;
+}
+
 int do_process(spg_handle *h) {
+    if (h->track_k > 0) {
+        const int rc = record_tracks(h);
+        if (rc) return rc;
+    }
     StepConst c = step_const(h);
     ev_begin(h, h->ev_step);
     if (h->mixed)
@@ -1075,6 +1112,7 @@ int spg_destroy(spg_handle *h) {
     for (void *ptr : ptrs) cudaFree(ptr);
     for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
     for (void *ptr : h->amg_alloc) cudaFree(ptr);
+    free_tracks(h);
     if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
     if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
     for (auto &P : h->ckpt)
@@ -1106,6 +1144,7 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
     if (n < 0 || n > kMaxParticles) return fail(h, SPG_E_INVALID, "set_particles: n out of range");
     if (n > 0 && (!pos || !vel)) return fail(h, SPG_E_INVALID, "set_particles: null pos/vel");
     CK(cudaSetDevice(h->device));
+    free_tracks(h);  // a new particle set ends any tracking
     cudaStream_t s = h->stream;
     {
         const int rc = alloc_particles(h, n);
@@ -1154,6 +1193,164 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
     h->have_particles = true;
     h->fix_bits = fix_bits_for(n);
     return reset_run_state(h);
+}
+
+void spg_default_source(spg_source *src) {
+    if (!src) return;
+    std::memset(src, 0, sizeof(*src));
+    src->shape = SPG_SRC_DISK;
+    src->directions = SPG_DIR_CONE;
+    src->energy = SPG_ENERGY_MONO;
+    src->normal[2] = 1.0;
+    src->radius = 0.02;
+    src->half_angle = 30.0 * 3.14159265358979323846 / 180.0;
+    src->energy_ev = 1.0;
+    src->binding_ev = 4.9;
+    src->emax_ev = 50.0;
+    src->displacement = 0.05e-3;
+}
+
+int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
+    if (!h) return SPG_E_INVALID;
+    if (!src) return fail(h, SPG_E_INVALID, "generate_particles: null source");
+    if (n < 0 || n > kMaxParticles) return fail(h, SPG_E_INVALID, "generate_particles: n out of range");
+    if (src->shape != SPG_SRC_DISK && src->shape != SPG_SRC_RECT)
+        return fail(h, SPG_E_INVALID, "generate_particles: bad shape");
+    if (src->directions != SPG_DIR_CONE && src->directions != SPG_DIR_COSINE)
+        return fail(h, SPG_E_INVALID, "generate_particles: bad directions");
+    if (src->energy != SPG_ENERGY_MONO && src->energy != SPG_ENERGY_THOMPSON)
+        return fail(h, SPG_E_INVALID, "generate_particles: bad energy law");
+    const double eV = 1.60217733000001e-19;  // Constants.hpp eV_J
+    if (src->energy == SPG_ENERGY_MONO ? !(src->energy_ev > 0.0) : !(src->binding_ev > 0.0 && src->emax_ev > 0.0))
+        return fail(h, SPG_E_INVALID, "generate_particles: energies must be > 0");
+    SourceConst c{};
+    c.shape = src->shape;
+    c.directions = src->directions;
+    c.energy = src->energy;
+    // frame about the normal (rectangles emit about +z)
+    double nv[3] = {src->normal[0], src->normal[1], src->normal[2]};
+    if (src->shape == SPG_SRC_RECT) nv[0] = nv[1] = 0.0, nv[2] = 1.0;
+    const double nn = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+    if (!(nn > 0.0)) return fail(h, SPG_E_INVALID, "generate_particles: zero normal");
+    for (double &x : nv) x /= nn;
+    const double t[3] = {std::fabs(nv[0]) < 0.9 ? 1.0 : 0.0, std::fabs(nv[0]) < 0.9 ? 0.0 : 1.0, 0.0};
+    double e1[3] = {nv[1] * t[2] - nv[2] * t[1], nv[2] * t[0] - nv[0] * t[2], nv[0] * t[1] - nv[1] * t[0]};
+    const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (double &x : e1) x /= l1;
+    const double e2[3] = {nv[1] * e1[2] - nv[2] * e1[1], nv[2] * e1[0] - nv[0] * e1[2], nv[0] * e1[1] - nv[1] * e1[0]};
+    for (int k = 0; k < 3; ++k) {
+        c.centre[k] = src->centre[k];
+        c.e1[k] = e1[k];
+        c.e2[k] = e2[k];
+        c.nrm[k] = nv[k];
+    }
+    c.radius = src->radius;
+    c.xlim[0] = src->xlim[0];
+    c.xlim[1] = src->xlim[1];
+    c.ylim[0] = src->ylim[0];
+    c.ylim[1] = src->ylim[1];
+    c.z = src->z;
+    c.one_minus_cos = 1.0 - std::cos(src->half_angle);
+    c.mass = h->prm.mass;
+    c.speed_mono = std::sqrt(2.0 * src->energy_ev * eV / h->prm.mass);
+    c.binding_j = src->binding_ev * eV;
+    c.s_max = src->emax_ev / (src->emax_ev + src->binding_ev);
+    c.displacement = src->displacement;
+    c.seed_lo = uint32_t(src->seed);
+    c.seed_hi = uint32_t(src->seed >> 32);
+    CK(cudaSetDevice(h->device));
+    free_tracks(h);  // a new particle set ends any tracking
+    cudaStream_t s = h->stream;
+    {
+        const int rc = alloc_particles(h, n);
+        if (rc) return rc;
+    }
+    h->cur = 0;
+    h->np = n;
+    h->n_active = n;
+    h->init_lost = 0;
+    h->occupied = 0;
+    if (n > 0) {
+        double *dpos = nullptr, *dvel = nullptr;
+        int32_t *dtet = nullptr;
+        unsigned long long *dlost = nullptr;
+        CK(dalloc(&dpos, 3 * n));
+        CK(dalloc(&dvel, 3 * n));
+        CK(dalloc(&dtet, n));
+        CK(dalloc(&dlost, 1));
+        launch_generate(c, n, dpos, dvel, s);
+        launch_locate(dpos, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings, dtet, s);
+        CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
+        launch_count_lost(dtet, n, dlost, s);
+        if (h->mixed)
+            launch_to_local(dpos, dvel, dtet, h->cen, n, h->Q[0], s);
+        else
+            launch_init_particles(dpos, dvel, dtet, n, h->P[0], s);
+        CK(cudaGetLastError());
+        unsigned long long lost = 0;
+        CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        h->init_lost = int64_t(lost);
+        cudaFree(dpos);
+        cudaFree(dvel);
+        cudaFree(dtet);
+        cudaFree(dlost);
+    }
+    h->have_particles = true;
+    h->fix_bits = fix_bits_for(n);
+    return reset_run_state(h);
+}
+
+int spg_track_particles(spg_handle *h, int32_t k, const int64_t *ids, int32_t capacity) {
+    if (!h) return SPG_E_INVALID;
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "track_particles: no particles set");
+    if (k < 0 || (k > 0 && (!ids || capacity < 1))) return fail(h, SPG_E_INVALID, "track_particles: bad arguments");
+    for (int32_t t = 0; t < k; ++t)
+        if (ids[t] < 0 || ids[t] >= h->np) return fail(h, SPG_E_INVALID, "track_particles: id out of range");
+    CK(cudaSetDevice(h->device));
+    free_tracks(h);
+    if (k == 0) return SPG_OK;
+    cudaStream_t s = h->stream;
+    CK(dalloc(&h->track_ids, k));
+    CK(dalloc(&h->track_of_id, std::max<int64_t>(h->np, 1)));
+    CK(dalloc(&h->track_slot, k));
+    CK(dalloc(&h->track_count, k));
+    CK(dalloc(&h->track_xyz, 3 * int64_t(k) * capacity));
+    CK(dalloc(&h->track_cur, 3 * int64_t(k)));
+    CK(dalloc(&h->track_flags, k));
+    CK(cudaMemcpyAsync(h->track_ids, ids, sizeof(int64_t) * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(h->track_of_id, 0xff, sizeof(int32_t) * std::max<int64_t>(h->np, 1), s));
+    CK(cudaMemsetAsync(h->track_slot, 0xff, sizeof(int32_t) * k, s));
+    CK(cudaMemsetAsync(h->track_count, 0, sizeof(int32_t) * k, s));
+    launch_track_map(h->track_ids, k, h->track_of_id, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    h->track_k = k;
+    h->track_cap = capacity;
+    return SPG_OK;
+}
+
+int spg_get_tracks(spg_handle *h, int32_t *counts, double *xyz, double *last_xyz, uint32_t *last_flags) {
+    if (!h) return SPG_E_INVALID;
+    if (h->track_k == 0) return fail(h, SPG_E_STATE, "get_tracks: no particles tracked");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const int k = h->track_k;
+    const uint32_t *idf = h->mixed ? h->Q[h->cur].idf : h->P[h->cur].idf;
+    launch_track_find(idf, h->np, h->track_of_id, h->track_slot, s);
+    if (h->mixed)
+        launch_track_current32(h->Q[h->cur], h->cen, h->track_slot, k, h->track_cur, h->track_flags, s);
+    else
+        launch_track_current64(h->P[h->cur], h->track_slot, k, h->track_cur, h->track_flags, s);
+    CK(cudaGetLastError());
+    if (counts) CK(cudaMemcpyAsync(counts, h->track_count, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, s));
+    if (xyz)
+        CK(cudaMemcpyAsync(xyz, h->track_xyz, sizeof(double) * 3 * int64_t(k) * h->track_cap, cudaMemcpyDeviceToHost,
+                           s));
+    if (last_xyz) CK(cudaMemcpyAsync(last_xyz, h->track_cur, sizeof(double) * 3 * k, cudaMemcpyDeviceToHost, s));
+    if (last_flags) CK(cudaMemcpyAsync(last_flags, h->track_flags, sizeof(uint32_t) * k, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SPG_OK;
 }
 
 int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags) {
@@ -1437,6 +1634,7 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     const int64_t n = hd.np;
     if (bytes < ckpt_bytes_for(h, n)) return fail(h, SPG_E_INVALID, "restore: buffer too small");
     CK(cudaSetDevice(h->device));
+    free_tracks(h);  // slots and particle count may change
     {
         const int rc = alloc_particles(h, n);
         if (rc) return rc;

@@ -299,7 +299,7 @@ __device__ __forceinline__ void queue_walk(WalkItem *__restrict__ q, unsigned in
 // with its start point; k_walk_queue64 then walks it in full warps (FP64
 // instructions issue per warp on GB300, so a walk taken by a few lanes of
 // every warp would cost the whole warp its FP64 throughput).
-__global__ void __launch_bounds__(256, 4) k_step64(DevParticles p, int64_t n, MeshDev m, StepConst c,
+__global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, MeshDev m, StepConst c,
                                                 WalkItem *__restrict__ wq, unsigned int *__restrict__ wq_n,
                                                 DevCounters *ctr) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

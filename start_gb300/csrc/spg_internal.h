@@ -322,6 +322,34 @@ void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const d
 void build_sell32(int64_t n, const int64_t *row_ptr, const int32_t *col, const double *val,
                   std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval);
 
+// ---------------------------------------------------------------- sources
+// A particle source on the device (kernels_sources.cu): the spg_source with
+// its frame (e1, e2, normal) and energy constants formed on the host.
+struct SourceConst {
+    int32_t shape, directions, energy;
+    double centre[3], e1[3], e2[3], nrm[3];
+    double radius, xlim[2], ylim[2], z;
+    double one_minus_cos;  // 1 - cos(half_angle)
+    double speed_mono;     // sqrt(2 E / m) of the monoenergetic source
+    double binding_j, s_max, mass;  // Thompson: U [J], Emax/(Emax+U); particle mass
+    double displacement;
+    uint32_t seed_lo, seed_hi;
+};
+void launch_generate(const SourceConst &c, int64_t n, double *pos, double *vel, cudaStream_t s);
+
+// ---------------------------------------------------------------- tracks
+// Trajectory sampling of a fixed set of particle ids (kernels_track.cu).
+void launch_track_map(const int64_t *ids, int k, int32_t *track_of_id, cudaStream_t s);
+void launch_track_find(const uint32_t *idf, int64_t n, const int32_t *track_of_id, int32_t *slot, cudaStream_t s);
+void launch_track_record64(const DevParticles &p, const int32_t *slot, int k, int cap, int32_t *count, double *xyz,
+                           cudaStream_t s);
+void launch_track_record32(const DevParticles32 &p, const double *cen, const int32_t *slot, int k, int cap,
+                           int32_t *count, double *xyz, cudaStream_t s);
+void launch_track_current64(const DevParticles &p, const int32_t *slot, int k, double *xyz, uint32_t *flags,
+                            cudaStream_t s);
+void launch_track_current32(const DevParticles32 &p, const double *cen, const int32_t *slot, int k, double *xyz,
+                            uint32_t *flags, cudaStream_t s);
+
 // ---------------------------------------------------------------- AMG
 // Smoothed-aggregation hierarchy (amg_setup.cpp) and its GPU V-cycle
 // (kernels_amg.cu), the preconditioner of SPG_PRECOND_AMG.

@@ -136,6 +136,57 @@ class StartPIC:
                                                N.as_ptr(vel, C.c_double), tp))
         self.n_particles = len(pos)
 
+    def generate_particles(self, n, *, shape="disk", directions="cone", energy="mono", centre=(0.0, 0.0, 0.0),
+                           normal=(0.0, 0.0, 1.0), radius=0.02, xlim=(0.0, 0.0), ylim=(0.0, 0.0), z=0.0,
+                           half_angle=None, energy_ev=1.0, binding_ev=4.9, emax_ev=50.0, displacement=0.05e-3,
+                           seed=0):
+        """Samples n particles on the device (spg_generate_particles): disk or
+        rectangle points, cone or cosine directions, monoenergetic or
+        Thompson energies, and the reference's 0.05 mm displacement."""
+        src = N.Source()
+        self.lib.spg_default_source(C.byref(src))
+        src.shape = {"disk": N.SPG_SRC_DISK, "rect": N.SPG_SRC_RECT, "plate": N.SPG_SRC_RECT}[shape]
+        src.directions = {"cone": N.SPG_DIR_CONE, "cosine": N.SPG_DIR_COSINE}[directions]
+        src.energy = {"mono": N.SPG_ENERGY_MONO, "thompson": N.SPG_ENERGY_THOMPSON}[energy]
+        src.centre[:] = [float(v) for v in centre]
+        src.normal[:] = [float(v) for v in normal]
+        src.radius = radius
+        src.xlim[:] = [float(v) for v in xlim]
+        src.ylim[:] = [float(v) for v in ylim]
+        src.z = z
+        if half_angle is not None:
+            src.half_angle = half_angle
+        src.energy_ev, src.binding_ev, src.emax_ev = energy_ev, binding_ev, emax_ev
+        src.displacement = displacement
+        src.seed = int(seed)
+        self._check(self.lib.spg_generate_particles(self.h, int(n), C.byref(src)))
+        self.n_particles = int(n)
+
+    def track(self, ids, capacity=10000):
+        """Samples the positions of particles `ids` before every step they are
+        alive in (ParticleMovementTracker)."""
+        ids = np.ascontiguousarray(ids, np.int64)
+        self._check(self.lib.spg_track_particles(self.h, len(ids), N.as_ptr(ids, C.c_int64), int(capacity)))
+        self._track = (ids, int(capacity))
+
+    def tracks(self):
+        """{id: (m, 3) positions}; a settled particle ends with its hit point."""
+        ids, cap = self._track
+        k = len(ids)
+        counts = np.zeros(k, np.int32)
+        xyz = np.zeros((k, cap, 3))
+        last = np.zeros((k, 3))
+        flags = np.zeros(k, np.uint32)
+        self._check(self.lib.spg_get_tracks(self.h, N.as_ptr(counts, C.c_int32), N.as_ptr(xyz, C.c_double),
+                                            N.as_ptr(last, C.c_double), N.as_ptr(flags, C.c_uint32)))
+        out = {}
+        for t, pid in enumerate(ids):
+            path = xyz[t, :counts[t]]
+            if flags[t] & N.SPG_FLAG_SETTLED:
+                path = np.vstack([path, last[t]])
+            out[int(pid)] = path
+        return out
+
     def particles(self):
         n = self.n_particles
         pos = np.empty((n, 3))

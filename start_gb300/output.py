@@ -52,6 +52,17 @@ def write_settled_particles(path, positions, flags, settled_bit=1, length_scale=
     np.savez(path, kind="SettledParticles", positions=positions[sel] * length_scale)
 
 
+def write_movements_json(path, tracks: dict):
+    """Tracks in the layout of ParticleMovementTracker::saveMovementsToJson
+    (ParticleMovementTracker.cpp:18-46): {"<id>": [{"x":..,"y":..,"z":..}, ...]}
+    for every particle with more than one recorded position."""
+    import json
+
+    out = {str(k): [{"x": float(p[0]), "y": float(p[1]), "z": float(p[2])} for p in v]
+           for k, v in tracks.items() if len(v) > 1}
+    Path(path).write_text(json.dumps(out, indent=4))
+
+
 def read(path) -> dict:
     with np.load(path, allow_pickle=False) as z:
         return {k: z[k] for k in z.files}

@@ -83,8 +83,8 @@ def test_struct_layouts_match_header(built):
     #include <stdio.h>
     #include "start_gpu.h"
     int main(void) {
-      printf("%zu %zu %zu %zu\n", sizeof(spg_mesh_desc), sizeof(spg_params), sizeof(spg_stats),
-             sizeof(spg_profile));
+      printf("%zu %zu %zu %zu %zu\n", sizeof(spg_mesh_desc), sizeof(spg_params), sizeof(spg_stats),
+             sizeof(spg_profile), sizeof(spg_source));
       return 0; }
     '''
     with tempfile.TemporaryDirectory() as d:
@@ -93,7 +93,8 @@ def test_struct_layouts_match_header(built):
         exe = Path(d) / "probe"
         subprocess.run(["gcc", "-I", str(ROOT / "include"), str(c), "-o", str(exe)], check=True)
         sizes = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()))
-    assert sizes == [C.sizeof(N.MeshDesc), C.sizeof(N.Params), C.sizeof(N.Stats), C.sizeof(N.Profile)]
+    assert sizes == [C.sizeof(N.MeshDesc), C.sizeof(N.Params), C.sizeof(N.Stats), C.sizeof(N.Profile),
+                     C.sizeof(N.Source)]
 
 
 def test_cpp_shim_compiles():
