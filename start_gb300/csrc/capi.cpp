@@ -7,6 +7,7 @@
 // counterpart (it only changes memory order).
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -761,6 +762,15 @@ int do_solve_mixed(spg_handle *h) {
             break;
         }
         if (outer_it == kOuterMax || total >= h->prm.cg_max_iter) break;
+        if (h->amg32 && hs.rr > 0.0) {
+            // the inner solve need not reduce the residual much further than
+            // this outer step still has to (with a margin of 3)
+            const double need = std::sqrt(outer.tol2 * hs.bb / hs.rr);
+            const double rt = std::max(inner_rtol, std::min(0.5, 0.3 * need));
+            const double t2 = rt * rt;
+            CK(cudaMemcpyAsync(reinterpret_cast<char *>(h->sc32) + offsetof(PcgScalars, tol2), &t2, sizeof(t2),
+                               cudaMemcpyHostToDevice, h->stream));
+        }
         for (;;) {
             CK(cudaGraphLaunch(h->pcg32_graph, h->stream));
             h->launches += pcg_iter_launches(h) * chunk;

@@ -75,7 +75,8 @@ __global__ void k_track_current(const T *__restrict__ x, const T *__restrict__ y
     xyz[3 * t] = px;
     xyz[3 * t + 1] = py;
     xyz[3 * t + 2] = pz;
-    flags[t] = idf[i] & ~kIdMask;
+    const uint32_t f = idf[i];
+    flags[t] = ((f & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((f & kLost) ? SPG_FLAG_LOST : 0u);
 }
 
 }  // namespace
