@@ -416,7 +416,9 @@ def run_gpu(args):
                  "pcg_iters": mp["pcg_iters"],
                  "step_GBps": mp["step_bytes"] / (mp["step_ms"] / 1e3) / 1e9 if mp["step_ms"] > 0 else None,
                  "pcg_GBps": mp["pcg_bytes"] / (mp["pcg_ms"] / 1e3) / 1e9 if mp["pcg_ms"] > 0 else None,
-                 "gpu_launches": mp["kernel_launches"], "dtype": "f32 state/push/SpMV, f64 refinement + sums"}
+                 "gpu_launches": mp["kernel_launches"],
+                 "dtype": ("f32 state/push/V-cycle, f64 PCG SpMV + vectors + sums" if args.precond == "amg"
+                           else "f32 state/push/SpMV, f64 refinement + sums")}
         em.close()
     grad = None
     if not args.no_grad and rank == 0:

@@ -66,7 +66,7 @@ typedef enum spg_collision_model {
 
 typedef enum spg_precision {
     SPG_FP64 = 0,  /* plain form: FP64 state, push, walk and PCG */
-    SPG_MIXED = 1  /* FP32 tet-local state and push; FP32-SpMV PCG in FP64 refinement */
+    SPG_MIXED = 1  /* FP32 tet-local state and push; FP32 V-cycle in FP64 PCG (AMG), FP32-SpMV PCG in FP64 refinement (Jacobi) */
 } spg_precision;
 
 /* Preconditioner of the Poisson PCG. The reference preconditions Belos CG

@@ -129,6 +129,10 @@ struct WalkOut {
 // parameter s = l0/(l0 - l1) along the segment is smallest (lowest local face
 // index on ties). A face carrying a surface triangle stops the walk there
 // (when stop_surface); a boundary face without one is an exit.
+// FP64 is spent only where the decision needs it: in a tet entered by a
+// crossing the FP32 inside screen usually decides; lambda(p0) and the
+// divisions are formed only when two or more faces compete or s is returned
+// (the same expressions as the full evaluation, so the same values).
 __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double p0x, double p0y, double p0z,
                                        double p1x, double p1y, double p1z, int max_cross, bool stop_surface) {
     WalkOut o;
@@ -138,6 +142,11 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
     o.s = 1.0;
     int enter = -1;
     for (;;) {
+        if (enter >= 0 && inside_sure_pos(g, p1x, p1y, p1z)) {
+            o.tet = t;
+            o.status = W_INSIDE;
+            return o;
+        }
         double l1[4];
         bary(g, p1x, p1y, p1z, l1);
         if (l1[0] >= 0.0 && l1[1] >= 0.0 && l1[2] >= 0.0 && l1[3] >= 0.0) {
@@ -145,26 +154,43 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
             o.status = W_INSIDE;
             return o;
         }
-        double l0[4];
-        bary(g, p0x, p0y, p0z, l0);
-        int best = -1;
-        double sb = 0.0;
+        int ncand = 0, best = -1;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {
-            if (f == enter || !(l1[f] < 0.0)) continue;
-            const double s = l0[f] / (l0[f] - l1[f]);
-            if (best < 0 || s < sb) {
+        for (int f = 0; f < 4; ++f)
+            if (f != enter && l1[f] < 0.0) {
+                ++ncand;
                 best = f;
-                sb = s;
             }
-        }
-        if (best < 0) {
+        if (ncand == 0) {
             o.tet = t;
             o.status = W_INSIDE;
             return o;
         }
+        double l0[4];
+        double sb = 0.0;
+        bool have_s = false;
+        if (ncand > 1) {
+            bary(g, p0x, p0y, p0z, l0);
+            best = -1;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                if (f == enter || !(l1[f] < 0.0)) continue;
+                const double s = l0[f] / (l0[f] - l1[f]);
+                if (best < 0 || s < sb) {
+                    best = f;
+                    sb = s;
+                }
+            }
+            have_s = true;
+        }
         const int tri = comp(__ldg(m.ftri + t), best);
-        if (stop_surface && tri >= 0) {
+        const int nb = comp(__ldg(m.nbr + t), best);
+        const bool surface = stop_surface && tri >= 0;
+        if ((surface || nb < 0) && !have_s) {
+            bary(g, p0x, p0y, p0z, l0);
+            sb = l0[best] / (l0[best] - l1[best]);
+        }
+        if (surface) {
             o.tet = t;
             o.status = W_SURFACE;
             o.tri = tri;
@@ -172,7 +198,6 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
             o.s = sb;
             return o;
         }
-        const int nb = comp(__ldg(m.nbr + t), best);
         if (nb < 0) {
             o.tet = t;
             o.status = W_EXIT;

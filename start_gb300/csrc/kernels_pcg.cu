@@ -200,13 +200,19 @@ __global__ void __launch_bounds__(kThreads) k_pupdate(PcgDev d) {
 }
 
 // ------------------------------------------------- PCG with the AMG V-cycle
+// M = false: the FP64 V-cycle reads r and writes z. M = true (mixed form):
+// the FP32 V-cycle reads r32 = float(r) and writes z32; x, r, p, q and all
+// sums stay FP64, so the solve still stops on the FP64 residual.
+
 // r = b - A x; bb = b.b, rr = r.r (z = M^-1 r follows as a V-cycle)
-__global__ void __launch_bounds__(kThreads) k_setup_amg(PcgDev d, const double *__restrict__ b) {
+template <bool M>
+__global__ void __launch_bounds__(kThreads) k_setup_amg(PcgDev d, const double *__restrict__ b, float *__restrict__ r32) {
     double bb = 0.0, rr = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
         const double bi = b[i];
         const double ri = bi - spmv_row(d, d.x, i);
         d.r[i] = ri;
+        if constexpr (M) r32[i] = float(ri);
         bb += bi * bi;
         rr += ri * ri;
     }
@@ -225,7 +231,8 @@ __global__ void __launch_bounds__(kThreads) k_setup_amg(PcgDev d, const double *
 }
 
 // x += alpha p; r -= alpha q; rr = r.r and the stop test
-__global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d) {
+template <bool M>
+__global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d, float *__restrict__ r32) {
     if (d.sc->converged) return;
     const double alpha = d.sc->alpha;
     double rr = 0.0;
@@ -233,6 +240,7 @@ __global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d) {
         d.x[i] += alpha * d.p[i];
         const double ri = d.r[i] - alpha * d.q[i];
         d.r[i] = ri;
+        if constexpr (M) r32[i] = float(ri);
         rr += ri * ri;
     }
     double tot[2];
@@ -248,11 +256,16 @@ __global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d) {
 }
 
 // rz' = r.z (z from the V-cycle); first: p = z; else beta = rz'/rz
-__global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, int first) {
+template <bool M>
+__global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, const float *__restrict__ z32, int first) {
     if (d.sc->converged) return;
     double rz = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
-        const double zi = d.z[i];
+        double zi;
+        if constexpr (M)
+            zi = double(z32[i]);
+        else
+            zi = d.z[i];
         rz += d.r[i] * zi;
         if (first) d.p[i] = zi;
     }
@@ -262,6 +275,14 @@ __global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, int first) {
         if (!first) sc->beta = tot[0] / sc->rz;
         sc->rz = tot[0];
     }
+}
+
+// p = z32 + beta p (mixed form)
+__global__ void __launch_bounds__(kThreads) k_pupdate_m(PcgDev d, const float *__restrict__ z32) {
+    if (d.sc->converged) return;
+    const double beta = d.sc->beta;
+    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads)
+        d.p[i] = fma(beta, d.p[i], double(z32[i]));
 }
 
 // ------------------------------------------------- mixed precision (SPG_MIXED)
@@ -394,75 +415,6 @@ __global__ void __launch_bounds__(kThreads) k_pupdate32(PcgDev32 f) {
         f.p[i] = fmaf(beta, f.p[i], f.z[i]);
 }
 
-// Mixed form with the FP32 V-cycle. Outer step: r = b - A x in FP64,
-// rr = r.r, bb = b.b; inner start e = 0, r32 = r (z = M^-1 r32 and p follow).
-__global__ void __launch_bounds__(kThreads) k_refine_setup_amg(PcgDev d, PcgDev32 f, const double *__restrict__ b) {
-    double rr = 0.0, bb = 0.0;
-    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
-        const double bi = b[i];
-        const double ri = bi - spmv_row(d, d.x, i);
-        f.r[i] = float(ri);
-        f.e[i] = 0.0f;
-        rr += ri * ri;
-        bb += bi * bi;
-    }
-    double tot[2];
-    if (block_reduce2(rr, bb, d.partials, d.sc, tot)) {
-        PcgScalars *sc = d.sc;  // outer scalars
-        sc->rr = tot[0];
-        sc->bb = tot[1];
-        sc->converged = (tot[0] <= sc->tol2 * tot[1] || tot[1] == 0.0) ? 1 : 0;
-        PcgScalars *si = f.sc;  // inner scalars
-        si->rz = 0.0;
-        si->rr = tot[0];
-        si->bb = tot[0];  // inner tolerance relative to the outer residual
-        si->iters = 0;
-        si->converged = sc->converged;
-        si->alpha = 0.0;
-        si->beta = 0.0;
-    }
-}
-
-// e += alpha p; r -= alpha q; rr and the inner stop test (z from the V-cycle)
-__global__ void __launch_bounds__(kThreads) k_update32_amg(PcgDev32 f) {
-    if (f.sc->converged) return;
-    const float alpha = float(f.sc->alpha);
-    float rr = 0.0f;
-    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < f.n; i += int64_t(gridDim.x) * kThreads) {
-        f.e[i] = fmaf(alpha, f.p[i], f.e[i]);
-        const float ri = fmaf(-alpha, f.q[i], f.r[i]);
-        f.r[i] = ri;
-        rr = fmaf(ri, ri, rr);
-    }
-    double tot[2];
-    if (block_reduce2_w(rr, 0.0f, f.partials, f.sc, tot)) {
-        PcgScalars *sc = f.sc;
-        sc->iters += 1;
-        sc->rr = tot[0];
-        if (tot[0] <= sc->tol2 * sc->bb)
-            sc->converged = 1;
-        else if (sc->iters >= sc->max_iter)
-            sc->converged = 3;  // inner cap: the outer loop refines again
-    }
-}
-
-// rz' = r.z; first: p = z; else beta = rz'/rz
-__global__ void __launch_bounds__(kThreads) k_rz32_amg(PcgDev32 f, int first) {
-    if (f.sc->converged) return;
-    float rz = 0.0f;
-    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < f.n; i += int64_t(gridDim.x) * kThreads) {
-        const float zi = f.z[i];
-        rz = fmaf(f.r[i], zi, rz);
-        if (first) f.p[i] = zi;
-    }
-    double tot[2];
-    if (block_reduce2_w(rz, 0.0f, f.partials, f.sc, tot)) {
-        PcgScalars *sc = f.sc;
-        if (!first) sc->beta = tot[0] / sc->rz;
-        sc->rz = tot[0];
-    }
-}
-
 __global__ void k_refine_apply(double *__restrict__ x, const float *__restrict__ e, int64_t n) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -523,17 +475,32 @@ void launch_pcg_setup(const PcgDev &d, const double *b, cudaStream_t s) {
 }
 
 void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s) {
-    k_setup_amg<<<d.grid.setup, kThreads, 0, s>>>(d, b);
+    k_setup_amg<false><<<d.grid.setup, kThreads, 0, s>>>(d, b, nullptr);
     launch_amg_vcycle(a, d.r, d.z, d.sc, s);
-    k_rz_amg<<<d.grid.update, kThreads, 0, s>>>(d, 1);
+    k_rz_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr, 1);
 }
 
 void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s) {
     k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
-    k_update_amg<<<d.grid.update, kThreads, 0, s>>>(d);
+    k_update_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr);
     launch_amg_vcycle(a, d.r, d.z, d.sc, s);
-    k_rz_amg<<<d.grid.update, kThreads, 0, s>>>(d, 0);
+    k_rz_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr, 0);
     k_pupdate<<<d.grid.pupdate, kThreads, 0, s>>>(d);
+}
+
+void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
+                                cudaStream_t s) {
+    k_setup_amg<true><<<d.grid.setup, kThreads, 0, s>>>(d, b, r32);
+    launch_amg_vcycle(a, r32, z32, d.sc, s);
+    k_rz_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, z32, 1);
+}
+
+void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {
+    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
+    k_update_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, r32);
+    launch_amg_vcycle(a, r32, z32, d.sc, s);
+    k_rz_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, z32, 0);
+    k_pupdate_m<<<d.grid.pupdate, kThreads, 0, s>>>(d, z32);
 }
 
 void launch_pcg_iteration(PcgDev &d, cudaStream_t s) {
@@ -618,20 +585,6 @@ PcgGrid pcg_grid32(int64_t n) {
     g.update = wave(k_update32, n);
     g.pupdate = wave(k_pupdate32, n);
     return g;
-}
-
-void launch_refine_setup_amg(const PcgDev &d, const PcgDev32 &f, const AmgDev32 &a, const double *b, cudaStream_t s) {
-    k_refine_setup_amg<<<f.grid.setup, kThreads, 0, s>>>(d, f, b);
-    launch_amg_vcycle(a, f.r, f.z, f.sc, s);
-    k_rz32_amg<<<f.grid.update, kThreads, 0, s>>>(f, 1);
-}
-
-void launch_pcg32_iteration_amg(PcgDev32 &f, const AmgDev32 &a, cudaStream_t s) {
-    k_spmv_dot32<<<f.grid.spmv, kThreads, 0, s>>>(f);
-    k_update32_amg<<<f.grid.update, kThreads, 0, s>>>(f);
-    launch_amg_vcycle(a, f.r, f.z, f.sc, s);
-    k_rz32_amg<<<f.grid.update, kThreads, 0, s>>>(f, 0);
-    k_pupdate32<<<f.grid.pupdate, kThreads, 0, s>>>(f);
 }
 
 void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s) {

@@ -424,10 +424,11 @@ void launch_amg_vcycle(const AmgDev32 &a, const float *r, float *z, const PcgSca
 // r.z and beta, p update).
 void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s);
 void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s);
-// The mixed form's inner FP32 PCG with the FP32 V-cycle: outer FP64 residual
-// and inner start, and one inner iteration.
-void launch_refine_setup_amg(const PcgDev &d, const PcgDev32 &f, const AmgDev32 &a, const double *b, cudaStream_t s);
-void launch_pcg32_iteration_amg(PcgDev32 &f, const AmgDev32 &a, cudaStream_t s);
+// The mixed form's PCG: FP64 SpMV, vectors and sums with the FP32 V-cycle as
+// the preconditioner (r32 = float(r) in, z32 out).
+void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
+                                cudaStream_t s);
+void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
                     const double *dir_value, double *b, int64_t n, cudaStream_t s);
