@@ -20,14 +20,14 @@ constexpr int kT = 256;
 // converged: 1 or 2 (plain PCG), or 3 (inner cap of the mixed form)
 __device__ __forceinline__ bool done(const PcgScalars *sc) { return sc && *(volatile const int *)&sc->converged; }
 
-// Row `row` of M x. G = 0: SELL-32, the calling thread owns the row. G > 0:
-// CSR, the G lanes of a group (lane = lane index within the group) stride
-// over the row's entries and a butterfly over the group leaves the sum in
-// every lane of the group.
-template <class T, int G>
-__device__ __forceinline__ T mat_row(const DevSellT<T> &M, const T *__restrict__ x, int64_t row, int lane) {
+// Row `row` of M x, xf(c) = x[c]. G = 0: SELL-32, the calling thread owns
+// the row. G > 0: CSR, the G lanes of a group (lane = lane index within the
+// group) stride over the row's entries and a butterfly over the group leaves
+// the sum in every lane of the group.
+template <class T, int G, class X>
+__device__ __forceinline__ T mat_row_f(const DevSellT<T> &M, X xf, int64_t row, int lane) {
     if constexpr (G == 0) {
-        return spmv_row_sell<T>(M.slice_ptr, M.scol, M.sval, x, row);
+        return spmv_row_sell_f<T>(M.slice_ptr, M.scol, M.sval, xf, row);
     } else {
         const int64_t k0 = __ldg(M.slice_ptr + row), k1 = __ldg(M.slice_ptr + row + 1);
         T a0 = T(0), a1 = T(0);
@@ -37,13 +37,13 @@ __device__ __forceinline__ T mat_row(const DevSellT<T> &M, const T *__restrict__
             const int32_t c2 = __ldg(M.scol + k + 2 * G), c3 = __ldg(M.scol + k + 3 * G);
             const T v0 = __ldg(M.sval + k), v1 = __ldg(M.sval + k + G);
             const T v2 = __ldg(M.sval + k + 2 * G), v3 = __ldg(M.sval + k + 3 * G);
-            const T x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+            const T x0 = xf(c0), x1 = xf(c1), x2 = xf(c2), x3 = xf(c3);
             a0 = fma(v0, x0, a0);
             a1 = fma(v1, x1, a1);
             a0 = fma(v2, x2, a0);
             a1 = fma(v3, x3, a1);
         }
-        for (; k < k1; k += G) a0 = fma(__ldg(M.sval + k), __ldg(x + __ldg(M.scol + k)), a0);
+        for (; k < k1; k += G) a0 = fma(__ldg(M.sval + k), xf(__ldg(M.scol + k)), a0);
         T s = a0 + a1;
 #pragma unroll
         for (int off = G / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, G);
@@ -66,11 +66,10 @@ __device__ __forceinline__ void row_of(int64_t n, int64_t &row, int &lane, bool 
 }
 
 // Every lane of a warp joins the group shuffles; rows past n read nothing.
-template <class T, int G>
-__device__ __forceinline__ T mat_row_safe(const DevSellT<T> &M, const T *__restrict__ x, int64_t row, int lane,
-                                          int64_t n) {
+template <class T, int G, class X>
+__device__ __forceinline__ T mat_row_safe_f(const DevSellT<T> &M, X xf, int64_t row, int lane, int64_t n) {
     if constexpr (G == 0) {
-        return row < n ? mat_row<T, 0>(M, x, row, 0) : T(0);
+        return row < n ? mat_row_f<T, 0>(M, xf, row, 0) : T(0);
     } else {
         if (row >= n) {
             T s = T(0);
@@ -78,8 +77,21 @@ __device__ __forceinline__ T mat_row_safe(const DevSellT<T> &M, const T *__restr
             for (int off = G / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, G);
             return s;
         }
-        return mat_row<T, G>(M, x, row, lane);
+        return mat_row_f<T, G>(M, xf, row, lane);
     }
+}
+
+template <class T, int G>
+__device__ __forceinline__ T mat_row_safe(const DevSellT<T> &M, const T *__restrict__ x, int64_t row, int lane,
+                                          int64_t n) {
+    return mat_row_safe_f<T, G>(M, [x](int32_t c) { return __ldg(x + c); }, row, lane, n);
+}
+
+// The first smoothing step from x = 0, x0 = D^-1 b / theta, formed where it
+// is read (the degree-1 kernels below) instead of stored.
+template <class T>
+__device__ __forceinline__ T jacobi0(const AmgLevelDevT<T> &L, const T *__restrict__ b, int64_t i) {
+    return T(L.inv_theta) * (__ldg(L.dinv + i) * __ldg(b + i));
 }
 
 // x = d = D^-1 b / theta (first Chebyshev step from x = 0)
@@ -122,6 +134,52 @@ __global__ void __launch_bounds__(kT) k_resid(const AmgLevelDevT<T> L, const T *
     row_of<G>(L.n, i, lane, own);
     const T ax = mat_row_safe<T, G>(L.A, xin, i, lane, L.n);
     if (own) L.r[i] = b[i] - ax;
+}
+
+// Degree 1: r = b - A x0 with x0 = D^-1 b / theta formed at each column.
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_resid_j(const AmgLevelDevT<T> L, const T *__restrict__ b,
+                                                const PcgScalars *sc) {
+    if (done(sc)) return;
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(L.n, i, lane, own);
+    const T *dinv = L.dinv;
+    const T it = T(L.inv_theta);
+    const T ax = mat_row_safe_f<T, G>(
+        L.A, [dinv, b, it](int32_t c) { return it * (__ldg(dinv + c) * __ldg(b + c)); }, i, lane, L.n);
+    if (own) L.r[i] = b[i] - ax;
+}
+
+// Degree 1: x_out = x0 + P x_coarse (x0 as in k_resid_j)
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_prolong_j(const AmgLevelDevT<T> L, const T *__restrict__ b,
+                                                  const T *__restrict__ xc, T *__restrict__ xout,
+                                                  const PcgScalars *sc) {
+    if (done(sc)) return;
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(L.P.n, i, lane, own);
+    const T v = mat_row_safe<T, G>(L.P, xc, i, lane, L.P.n);
+    if (own) xout[i] = jacobi0(L, b, i) + v;
+}
+
+// Degree 1 post-smoothing: x_out = x_in + D^-1 (b - A x_in) / theta
+template <class T, int G>
+__global__ void __launch_bounds__(kT) k_jacobi_step(const AmgLevelDevT<T> L, const T *__restrict__ b,
+                                                    const T *__restrict__ xin, T *__restrict__ xout,
+                                                    const PcgScalars *sc) {
+    if (done(sc)) return;
+    int64_t i;
+    int lane;
+    bool own;
+    row_of<G>(L.n, i, lane, own);
+    const T ax = mat_row_safe<T, G>(L.A, xin, i, lane, L.n);
+    if (!own) return;
+    const T r = b[i] - ax;
+    xout[i] = xin[i] + T(L.inv_theta) * (L.dinv[i] * r);
 }
 
 // b_next = R r
@@ -189,13 +247,12 @@ void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalar
     T *xb = L.x[1];
     const int ga = L.A.g;
     const AmgLevelDevT<T> &N = a.lev[l + 1];
-    if (L.degree == 1) {  // x = D^-1 b / theta; residual; coarse correction; one damped Jacobi step
-        k_cheb0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
-        SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xa, sc)
+    if (L.degree == 1) {  // x0 = D^-1 b / theta; residual; coarse correction; one damped Jacobi step
+        SPG_AMG_DISPATCH(ga, k_resid_j, L.n, L, b, sc)
         SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
         vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
-        SPG_AMG_DISPATCH(L.P.g, k_prolong, L.P.n, L.P, xa, N.x[0], xb, sc)
-        SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xb, xa, 0.0, L.inv_theta, sc)
+        SPG_AMG_DISPATCH(L.P.g, k_prolong_j, L.P.n, L, b, N.x[0], xb, sc)
+        SPG_AMG_DISPATCH(ga, k_jacobi_step, L.n, L, b, xb, xa, sc)
         return;
     }
     k_cheb0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);

@@ -15,9 +15,11 @@ namespace spg {
 // loads issued before the gathers, then the remaining (< 8) entries the same
 // way, so a row costs two dependent load stages per eight entries and no
 // FMA is spent on padding beyond the slice width.
-template <class T>
-__device__ __forceinline__ T spmv_row_sell(const int64_t *__restrict__ slice_ptr, const int32_t *__restrict__ scol,
-                                           const T *__restrict__ sval, const T *__restrict__ x, int64_t i) {
+// xf(c) supplies x[c]: a plain gather, or a value formed from several
+// vectors at the gathered column (a fused vector update).
+template <class T, class X>
+__device__ __forceinline__ T spmv_row_sell_f(const int64_t *__restrict__ slice_ptr, const int32_t *__restrict__ scol,
+                                             const T *__restrict__ sval, X xf, int64_t i) {
     const int64_t s = i >> 5;
     const int64_t base = __ldg(slice_ptr + s) + (i & 31);
     const int w = int((__ldg(slice_ptr + s + 1) - __ldg(slice_ptr + s)) >> 5);
@@ -32,7 +34,7 @@ __device__ __forceinline__ T spmv_row_sell(const int64_t *__restrict__ slice_ptr
             v[u] = __ldg(sval + base + 32 * (j + u));
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) xv[u] = __ldg(x + c[u]);
+        for (int u = 0; u < 8; ++u) xv[u] = xf(c[u]);
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
             a0 = fma(v[u], xv[u], a0);
@@ -51,7 +53,7 @@ __device__ __forceinline__ T spmv_row_sell(const int64_t *__restrict__ slice_ptr
             }
 #pragma unroll
         for (int u = 0; u < 7; ++u)
-            if (u < rem) xv[u] = __ldg(x + c[u]);
+            if (u < rem) xv[u] = xf(c[u]);
 #pragma unroll
         for (int u = 0; u < 7; ++u)
             if (u < rem) {
@@ -62,6 +64,12 @@ __device__ __forceinline__ T spmv_row_sell(const int64_t *__restrict__ slice_ptr
             }
     }
     return a0 + a1;
+}
+
+template <class T>
+__device__ __forceinline__ T spmv_row_sell(const int64_t *__restrict__ slice_ptr, const int32_t *__restrict__ scol,
+                                           const T *__restrict__ sval, const T *__restrict__ x, int64_t i) {
+    return spmv_row_sell_f<T>(slice_ptr, scol, sval, [x](int32_t c) { return __ldg(x + c); }, i);
 }
 
 }  // namespace spg
