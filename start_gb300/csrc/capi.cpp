@@ -71,7 +71,7 @@ struct spg_handle {
 
     // fields
     double *node_q = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr, *r = nullptr, *z = nullptr,
-           *p = nullptr, *p2 = nullptr, *q = nullptr, *partials = nullptr;
+           *p = nullptr, *q = nullptr, *partials = nullptr;
     double *efield = nullptr;                 // 3 per tet
     unsigned long long *node_fix = nullptr;   // fixed-point deposit accumulators
     int fix_bits = 40;                        // deposit quantum 2^-fix_bits of one particle's charge
@@ -115,7 +115,6 @@ struct spg_handle {
     unsigned int *tri_count = nullptr;
     DevCounters *ctr = nullptr;
     WalkItem *walkq = nullptr;       // capacity cap (particles)
-    int32_t *collq = nullptr;        // collision queue of the FP64 step, capacity cap
     unsigned int *walkq_n = nullptr;
     int64_t *n_alive_dev = nullptr;
     int32_t *sort_scratch = nullptr;
@@ -219,8 +218,6 @@ void free_particles(spg_handle *h) {
     }
     cudaFree(h->walkq);
     h->walkq = nullptr;
-    cudaFree(h->collq);
-    h->collq = nullptr;
     h->cap = 0;
 }
 
@@ -352,11 +349,17 @@ int upload_amg(spg_handle *h, const AmgHost &ah, const T *sval0, AmgDevT<T> &a) 
                 // (nnz(P) + 2 n + nc); vector words
                 h->amg_bytes += wv * (4.0 * n + 18.0 * n + 3.0 * n + 3.0 * n + 2.0 * nc) + wm * (4.0 * nnzA + 2.0 * nnzP);
                 h->amg_launches += 7;
-            } else {
+            } else if (sizeof(T) == 4) {
                 // residual from x0 = D^-1 b / theta (nnz + 3 n); restriction (nnz(P) +
                 // n + nc); prolongation onto x0 (nnz(P) + 3 n + nc); Jacobi step (nnz + 4 n)
                 h->amg_bytes += wv * (3.0 * n + n + 3.0 * n + 4.0 * n + 2.0 * nc) + wm * (2.0 * nnzA + 2.0 * nnzP);
                 h->amg_launches += 4;
+            } else {
+                // x0 = D^-1 b / theta (3 n); residual (nnz + 3 n); restriction (nnz(P) +
+                // n + nc); prolongation (nnz(P) + 2 n + nc); Jacobi step (nnz + 4 n)
+                h->amg_bytes += wv * (3.0 * n + 3.0 * n + n + 2.0 * n + 4.0 * n + 2.0 * nc) +
+                                wm * (2.0 * nnzA + 2.0 * nnzP);
+                h->amg_launches += 5;
             }
         }
         if (l > 0 && (rc = vec(&D.b, D.n))) return rc;
@@ -397,14 +400,13 @@ void pcg_setup_any(spg_handle *h, const PcgDev &d, const double *b) {
     else
         launch_pcg_setup(d, b, h->stream);
 }
-void pcg_iteration_any(spg_handle *h, PcgDev &d, int parity) {
+void pcg_iteration_any(spg_handle *h, PcgDev &d) {
     if (h->amg)
-        launch_pcg_iteration_amg(d, h->amgd, parity, h->stream);
+        launch_pcg_iteration_amg(d, h->amgd, h->stream);
     else
         launch_pcg_iteration(d, h->stream);
 }
-int pcg_iter_launches(const spg_handle *h) { return (h->amg || h->amg32) ? 3 + h->amg_launches : 3; }
-// AMG iterations alternate two p buffers, so their chunk is even.
+int pcg_iter_launches(const spg_handle *h) { return (h->amg || h->amg32) ? 4 + h->amg_launches : 3; }
 int pcg_chunk(const spg_handle *h) { return (h->amg || h->amg32) ? 2 : kPcgChunk; }
 
 // Allocates both particle buffers (and the walk queue) for n particles.
@@ -435,7 +437,6 @@ int alloc_particles(spg_handle *h, int64_t n) {
         }
     }
     CK(dalloc(&h->walkq, n));
-    CK(dalloc(&h->collq, n));
     h->cap = n;
     return SPG_OK;
 }
@@ -528,7 +529,7 @@ PcgDev pcg_dev(spg_handle *h) {
     d.r = h->r;
     d.z = h->z;
     d.p = h->p;
-    d.p2 = h->p2;
+    d.p2 = nullptr;
     d.q = h->q;
     d.partials = h->partials;
     d.sc = h->sc;
@@ -697,7 +698,7 @@ int do_solve64(spg_handle *h) {
     if (!h->pcg_graph) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < chunk; ++k) pcg_iteration_any(h, d, k & 1);
+        for (int k = 0; k < chunk; ++k) pcg_iteration_any(h, d);
         CK(cudaStreamEndCapture(h->stream, &g));
         CK(cudaGraphInstantiate(&h->pcg_graph, g, 0));
         cudaGraphDestroy(g);
@@ -712,8 +713,8 @@ int do_solve64(spg_handle *h) {
     ev_end(h, h->ev_pcg);
     if (h->prof) {
         h->pcg_iters_prof += hs.iters;
-        if (h->amg)  // spmv_dot with the p update 12 nnz + 32 n, update 48 n, V-cycle, r.z 16 n
-            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 96.0 * double(n) + h->amg_bytes);
+        if (h->amg)  // spmv_dot 12 nnz + 24 n, update 48 n, V-cycle, r.z 16 n, p update 24 n
+            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 112.0 * double(n) + h->amg_bytes);
         else
             h->pcg_bytes += double(hs.iters) * (12.0 * double(h->nnz_kept) + 4.0 * double(n + 1) + 72.0 * double(n));
     }
@@ -738,8 +739,7 @@ int do_solve_mixed_amg(spg_handle *h) {
     if (!h->pcg32_graph) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < chunk; ++k)
-            launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, k & 1, h->stream);
+        for (int k = 0; k < chunk; ++k) launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream);
         CK(cudaStreamEndCapture(h->stream, &g));
         CK(cudaGraphInstantiate(&h->pcg32_graph, g, 0));
         cudaGraphDestroy(g);
@@ -753,9 +753,9 @@ int do_solve_mixed_amg(spg_handle *h) {
         if (hs.converged) break;
     }
     ev_end(h, h->ev_pcg);
-    if (h->prof) {  // spmv_dot with the p update 12 nnz + 28 n, update 52 n, FP32 V-cycle, r.z 12 n
+    if (h->prof) {  // spmv_dot 12 nnz + 24 n, update 52 n, FP32 V-cycle, r.z 12 n, p update 20 n
         h->pcg_iters_prof += hs.iters;
-        h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 92.0 * double(n) + h->amg_bytes);
+        h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 108.0 * double(n) + h->amg_bytes);
     }
     return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
 }
@@ -859,11 +859,10 @@ int do_process(spg_handle *h) {
         launch_step32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
                       h->stream);
     else
-        launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->collq, h->ctr,
+        launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
                       h->stream);
     ev_end(h, h->ev_step);
-    if (h->n_active > 0)  // step kernel + queued walks (+ queued collisions of the FP64 step)
-        h->launches += (!h->mixed && c.model != SPG_COLL_NONE) ? 3 : 2;
+    if (h->n_active > 0) h->launches += 2;  // step kernel + queued walks
     CK(cudaGetLastError());
     if (h->prof)
         h->step_bytes += (h->mixed ? 92.0 : 152.0) *
@@ -1105,7 +1104,6 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(dalloc(&h->r, n));
     CK(dalloc(&h->z, n));
     CK(dalloc(&h->p, n));
-    CK(dalloc(&h->p2, n));
     CK(dalloc(&h->q, n));
     h->pcg_blocks = pcg_blocks(n);
     h->grid64 = pcg_grid64(n);
@@ -1119,7 +1117,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(cudaMemsetAsync(h->sc, 0, sizeof(PcgScalars), s));
     CK(dalloc(&h->tri_count, std::max<int64_t>(h->n_tris, 1)));
     CK(dalloc(&h->ctr, 1));
-    CK(dalloc(&h->walkq_n, 2));
+    CK(dalloc(&h->walkq_n, 1));
     CK(dalloc(&h->n_alive_dev, 1));
     CK(dalloc(&h->sort_scratch, size_t(sort_scratch_words(h->n_tets))));
     rc = reset_run_state(h);
@@ -1135,7 +1133,7 @@ int spg_destroy(spg_handle *h) {
     free_particles(h);
     void *ptrs[] = {h->rec,      h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
-                    h->node_q,   h->rho,      h->phi,      h->b,         h->r,        h->z,         h->p,         h->p2,
+                    h->node_q,   h->rho,      h->phi,      h->b,         h->r,        h->z,         h->p,
                     h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
@@ -1801,7 +1799,7 @@ int solve_into(spg_handle *h, double *b, double *x, int32_t *iters) {
     pcg_setup_any(h, d, b);
     PcgScalars hs{};
     for (int chunk = 0;; ++chunk) {
-        for (int k = 0; k < pcg_chunk(h); ++k) pcg_iteration_any(h, d, k & 1);
+        for (int k = 0; k < pcg_chunk(h); ++k) pcg_iteration_any(h, d);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
@@ -1895,7 +1893,7 @@ int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, co
             launch_step32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
                           h->stream, h->land);
         else
-            launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->collq, h->ctr,
+            launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
                           h->stream, h->land);
         CK(cudaGetLastError());
         h->step++;
@@ -1955,7 +1953,7 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
                 launch_step32(work32, n, mesh_dev32(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
             } else {
                 launch_record(work, n, h->hist, k - k0, s);
-                launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->collq, h->ctr_scratch, s);
+                launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
             }
         }
         StepConst c = step_const(h);

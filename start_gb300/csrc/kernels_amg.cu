@@ -87,11 +87,22 @@ __device__ __forceinline__ T mat_row_safe(const DevSellT<T> &M, const T *__restr
     return mat_row_safe_f<T, G>(M, [x](int32_t c) { return __ldg(x + c); }, row, lane, n);
 }
 
-// The first smoothing step from x = 0, x0 = D^-1 b / theta, formed where it
-// is read (the degree-1 kernels below) instead of stored.
+// The first smoothing step from x = 0, x0 = D^-1 b / theta. The FP32
+// V-cycle forms it where it is read (k_resid_j, k_prolong_j) instead of
+// storing it; the FP64 V-cycle stores it (k_jacobi0), because forming it at
+// every gathered column would triple the FP64 work of the residual.
 template <class T>
 __device__ __forceinline__ T jacobi0(const AmgLevelDevT<T> &L, const T *__restrict__ b, int64_t i) {
     return T(L.inv_theta) * (__ldg(L.dinv + i) * __ldg(b + i));
+}
+
+// x = D^-1 b / theta (degree 1, FP64 V-cycle)
+template <class T>
+__global__ void __launch_bounds__(kT) k_jacobi0(const AmgLevelDevT<T> L, const T *__restrict__ b, T *__restrict__ x,
+                                                const PcgScalars *sc) {
+    if (done(sc)) return;
+    const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+    if (i < L.n) x[i] = jacobi0(L, b, i);
 }
 
 // x = d = D^-1 b / theta (first Chebyshev step from x = 0)
@@ -247,11 +258,20 @@ void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalar
     T *xb = L.x[1];
     const int ga = L.A.g;
     const AmgLevelDevT<T> &N = a.lev[l + 1];
-    if (L.degree == 1) {  // x0 = D^-1 b / theta; residual; coarse correction; one damped Jacobi step
+    if (L.degree == 1 && sizeof(T) == 4) {  // x0 = D^-1 b / theta; residual; coarse correction; damped Jacobi
         SPG_AMG_DISPATCH(ga, k_resid_j, L.n, L, b, sc)
         SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
         vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
         SPG_AMG_DISPATCH(L.P.g, k_prolong_j, L.P.n, L, b, N.x[0], xb, sc)
+        SPG_AMG_DISPATCH(ga, k_jacobi_step, L.n, L, b, xb, xa, sc)
+        return;
+    }
+    if (L.degree == 1) {
+        k_jacobi0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
+        SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xa, sc)
+        SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
+        vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
+        SPG_AMG_DISPATCH(L.P.g, k_prolong, L.P.n, L.P, xa, N.x[0], xb, sc)
         SPG_AMG_DISPATCH(ga, k_jacobi_step, L.n, L, b, xb, xa, sc)
         return;
     }

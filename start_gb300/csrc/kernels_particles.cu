@@ -265,29 +265,29 @@ __device__ __noinline__ void scatter64(const StepConst c, double u1, double u2, 
     vz = ez + cmz;
 }
 
-// Gas collision decision. Draw u0 (53-bit) decides; the FP32 screen compares
-// the interval of u0 known from its top 24 bits with P_f (1 -+ 1e-4).
-// P_f = kp (v^2)^pexp from 20-bit velocity components has a relative error
-// below 2e-5, so a decided screen agrees with u0 < P in FP64.
-__device__ __forceinline__ bool collide_hit(const StepConst &c, uint32_t id, double vx, double vy, double vz) {
+// Gas collision decision and scattering. Draw u0 (53-bit) decides; the FP32
+// screen compares the interval of u0 known from its top 24 bits with
+// P_f (1 -+ 1e-4). P_f = kp (v^2)^pexp from 20-bit velocity components has a
+// relative error below 2e-5, so a decided screen agrees with u0 < P in FP64.
+__device__ __forceinline__ bool collide(const StepConst &c, uint32_t id, double &vx, double &vy, double &vz) {
     const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
     const float fx = hi_float(vx), fy = hi_float(vy), fz = hi_float(vz);
     const float v2 = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
     const float pf = c.kp_f * exp2f(c.pexp_f * log2f(v2));
     const float ulo = float(r.v[0] >> 8) * 5.9604644775390625e-8f;  // 2^-24
     const float uhi = ulo + 5.9604644775390625e-8f;
-    if (uhi < pf * (1.0f - 1e-4f)) return true;
-    if (ulo > pf * (1.0f + 1e-4f)) return false;
-    return u01_from(r.v[0], r.v[1]) < probability64(c, vx, vy, vz);
-}
-
-// Scattering of a particle whose collision collide_hit decided, from the
-// same draws (u1 from the first Philox block, u2 from the second).
-__device__ __forceinline__ void collide_scatter(const StepConst &c, uint32_t id, double &vx, double &vy, double &vz) {
-    const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
+    bool hit;
+    if (uhi < pf * (1.0f - 1e-4f))
+        hit = true;
+    else if (ulo > pf * (1.0f + 1e-4f))
+        hit = false;
+    else
+        hit = u01_from(r.v[0], r.v[1]) < probability64(c, vx, vy, vz);
+    if (!hit) return false;
     const double u1 = u01_from(r.v[2], r.v[3]);
     const Philox4 r2 = collision_draw(uint64_t(c.step), 1u, id, c.seed_lo, c.seed_hi);
     scatter64(c, u1, u01_from(r2.v[0], r2.v[1]), vx, vy, vz);
+    return true;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(unsigned v) { return __reduce_add_sync(kFull, v); }
@@ -295,19 +295,6 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned v) { return __re
 // Finite test from the exponent bits (no FP64 compare).
 __device__ __forceinline__ bool finite_bits(double x) {
     return ((__double2hiint(x) >> 20) & 0x7ff) != 0x7ff;
-}
-
-// Warp-aggregated append of this lane's index to the collision queue.
-__device__ __forceinline__ void queue_collision(int32_t *__restrict__ q, unsigned int *__restrict__ qn, bool want,
-                                                int64_t i) {
-    const unsigned ballot = __ballot_sync(kFull, want);
-    if (!ballot) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(qn, unsigned(__popc(ballot)));
-    base = __shfl_sync(kFull, base, leader);
-    if (want) q[base + __popc(ballot & ((1u << lane) - 1u))] = int32_t(i);
 }
 
 // Warp-aggregated append of this lane's item to the walk queue.
@@ -336,17 +323,13 @@ __device__ __forceinline__ void queue_walk(WalkItem *__restrict__ q, unsigned in
 // end point is not certainly inside its tet is appended to the walk queue
 // with its start point; k_walk_queue64 then walks it in full warps (FP64
 // instructions issue per warp on GB300, so a walk taken by a few lanes of
-// every warp would cost the whole warp its FP64 throughput). For the same
-// reason a colliding particle stores its pre-collision velocity and is
-// appended to the collision queue, whose FP64 scattering k_scatter_queue64
-// runs in full warps before the next step reads the velocity (the walk of
-// this step uses the position only, as in the reference order).
+// every warp would cost the whole warp its FP64 throughput).
 __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, MeshDev m, StepConst c,
                                                 WalkItem *__restrict__ wq, unsigned int *__restrict__ wq_n,
-                                                int32_t *__restrict__ cq, DevCounters *ctr) {
+                                                DevCounters *ctr) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     unsigned processed = 0, coll = 0, cross = 0, settled = 0, lost = 0, capped = 0;
-    bool want_walk = false, want_scatter = false;
+    bool want_walk = false;
     double x = 0.0, y = 0.0, z = 0.0;
     if (i < n) {
         uint32_t idf = p.idf[i];
@@ -382,10 +365,7 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
                 const double nx = x + vx * c.dt, ny = y + vy * c.dt, nz = z + vz * c.dt;
                 if (!(same_value(nx, x) && same_value(ny, y) && same_value(nz, z))) {
                     const uint32_t id = idf & kIdMask;
-                    if (c.model != SPG_COLL_NONE) {
-                        want_scatter = collide_hit(c, id, vx, vy, vz);
-                        coll = want_scatter ? 1u : 0u;
-                    }
+                    if (c.model != SPG_COLL_NONE) coll = collide(c, id, vx, vy, vz) ? 1u : 0u;
                     if (!(finite_bits(nx) && finite_bits(ny) && finite_bits(nz))) {
                         idf |= kLost;
                         lost = 1;
@@ -406,7 +386,6 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
         }
     }
     queue_walk(wq, wq_n, want_walk, i, x, y, z);
-    queue_collision(cq, wq_n + 1, want_scatter, i);
     // Block-level counter reduction, one atomic per counter per block.
     __shared__ unsigned long long sh[8][6];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -430,20 +409,6 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
                                                          : &ctr->capped;
             atomicAdd(dst, s);
         }
-    }
-}
-
-// Post-collision velocities of the queued particles, one particle per lane.
-__global__ void __launch_bounds__(128) k_scatter_queue64(DevParticles p, StepConst c, const int32_t *__restrict__ cq,
-                                                         const unsigned int *__restrict__ cq_n) {
-    const unsigned nq = *cq_n;
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
-        const int32_t i = cq[q];
-        double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
-        collide_scatter(c, p.idf[i] & kIdMask, vx, vy, vz);
-        p.vx[i] = vx;
-        p.vy[i] = vy;
-        p.vz[i] = vz;
     }
 }
 
@@ -797,12 +762,11 @@ inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1)
 }  // namespace
 
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c, unsigned int *tri_count,
-                   WalkItem *wq, unsigned int *wq_n, int32_t *cq, DevCounters *ctr, cudaStream_t s, LandRec *land) {
+                   WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s, LandRec *land) {
     if (n <= 0) return;
-    cudaMemsetAsync(wq_n, 0, 2 * sizeof(unsigned int), s);
-    k_step64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, c, wq, wq_n, cq, ctr);
+    cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
+    k_step64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, c, wq, wq_n, ctr);
     k_walk_queue64<<<152 * 8, 128, 0, s>>>(p, m, c.max_cross, wq, wq_n, tri_count, ctr, land, c.step);
-    if (c.model != SPG_COLL_NONE) k_scatter_queue64<<<152 * 4, 128, 0, s>>>(p, c, cq, wq_n + 1);
 }
 
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,

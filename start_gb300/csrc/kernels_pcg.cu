@@ -277,43 +277,12 @@ __global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, const float *__re
     }
 }
 
-// The p update fused into the SpMV: p_new = z + beta p_old is formed at every
-// gathered column (the same expression in every thread, so the same value)
-// and stored for the thread's own row in the other p buffer; q = A p_new,
-// pq = p_new.q, alpha = rz / pq. M: z is the FP32 V-cycle output.
-template <bool M>
-__global__ void __launch_bounds__(kThreads) k_spmv_dot_p(PcgDev d, const float *__restrict__ z32,
-                                                         const double *__restrict__ pold, double *__restrict__ pnew) {
+// p = z32 + beta p (mixed form)
+__global__ void __launch_bounds__(kThreads) k_pupdate_m(PcgDev d, const float *__restrict__ z32) {
     if (d.sc->converged) return;
     const double beta = d.sc->beta;
-    const double *z = d.z;
-    auto pv = [beta, z, z32, pold](int32_t c) {
-        double zc;
-        if constexpr (M)
-            zc = double(__ldg(z32 + c));
-        else
-            zc = __ldg(z + c);
-        return fma(beta, __ldg(pold + c), zc);
-    };
-    double pq = 0.0;
-    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
-        const double qi = spmv_row_sell_f<double>(d.slice_ptr, d.scol, d.sval, pv, i);
-        const double pi = pv(int32_t(i));
-        pnew[i] = pi;
-        d.q[i] = qi;
-        pq += pi * qi;
-    }
-    double tot[2];
-    if (block_reduce2(pq, 0.0, d.partials, d.sc, tot)) {
-        PcgScalars *sc = d.sc;
-        sc->pq = tot[0];
-        if (tot[0] > 0.0) {
-            sc->alpha = sc->rz / tot[0];
-        } else {
-            sc->alpha = 0.0;
-            sc->converged = 2;  // breakdown: A not SPD on this subspace
-        }
-    }
+    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads)
+        d.p[i] = fma(beta, d.p[i], double(z32[i]));
 }
 
 // ------------------------------------------------- mixed precision (SPG_MIXED)
@@ -487,7 +456,6 @@ PcgGrid pcg_grid64(int64_t n) {
     PcgGrid g;
     g.setup = wave(k_setup, n);
     g.spmv = wave(k_spmv_dot, n);
-    g.spmv_p = std::min(wave(k_spmv_dot_p<false>, n), wave(k_spmv_dot_p<true>, n));
     g.update = wave(k_update, n);
     g.pupdate = wave(k_pupdate, n);
     return g;
@@ -512,16 +480,12 @@ void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cud
     k_rz_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr, 1);
 }
 
-// Iterations alternate the two p buffers: parity 0 reads p and writes p2,
-// parity 1 the reverse; the setup leaves p_0 = z_0 in p with beta = 0.
-void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, int parity, cudaStream_t s) {
-    double *pold = parity ? d.p2 : d.p, *pnew = parity ? d.p : d.p2;
-    PcgDev du = d;
-    du.p = pnew;
-    k_spmv_dot_p<false><<<d.grid.spmv_p, kThreads, 0, s>>>(d, nullptr, pold, pnew);
-    k_update_amg<false><<<d.grid.update, kThreads, 0, s>>>(du, nullptr);
+void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s) {
+    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
+    k_update_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr);
     launch_amg_vcycle(a, d.r, d.z, d.sc, s);
     k_rz_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr, 0);
+    k_pupdate<<<d.grid.pupdate, kThreads, 0, s>>>(d);
 }
 
 void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
@@ -531,15 +495,12 @@ void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double
     k_rz_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, z32, 1);
 }
 
-void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, int parity,
-                                    cudaStream_t s) {
-    double *pold = parity ? d.p2 : d.p, *pnew = parity ? d.p : d.p2;
-    PcgDev du = d;
-    du.p = pnew;
-    k_spmv_dot_p<true><<<d.grid.spmv_p, kThreads, 0, s>>>(d, z32, pold, pnew);
-    k_update_amg<true><<<d.grid.update, kThreads, 0, s>>>(du, r32);
+void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {
+    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
+    k_update_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, r32);
     launch_amg_vcycle(a, r32, z32, d.sc, s);
     k_rz_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, z32, 0);
+    k_pupdate_m<<<d.grid.pupdate, kThreads, 0, s>>>(d, z32);
 }
 
 void launch_pcg_iteration(PcgDev &d, cudaStream_t s) {

@@ -184,11 +184,9 @@ void launch_gather_adj(const DevParticles &p, int64_t n, const double *ax, const
 // Kernel launchers (kernels_particles.cu).
 // Step kernel plus the exact walk of the queued particles (wq holds up to n
 // items); land (nullable) receives the landing records.
-// wq_n: two counters (walk queue, collision queue); cq: collision queue of
-// n indices.
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c,
-                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, int32_t *cq, DevCounters *ctr,
-                   cudaStream_t s, LandRec *land = nullptr);
+                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
+                   LandRec *land = nullptr);
 // Fixed-point P1 deposit: node_fix[n] += round(lambda_n * 2^k) per alive
 // particle (lambda_0 takes the remainder so each particle adds exactly 2^k).
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,
@@ -285,7 +283,7 @@ struct PcgScalars {
 // Grid of each PCG kernel: SMs x resident blocks per SM (occupancy of that
 // kernel), capped by the rows; every kernel loops over rows grid-stride.
 struct PcgGrid {
-    int setup = 1, spmv = 1, spmv_p = 1, update = 1, pupdate = 1;
+    int setup = 1, spmv = 1, update = 1, pupdate = 1;
 };
 struct PcgDev {
     int64_t n;
@@ -422,16 +420,15 @@ using AmgDev32 = AmgDevT<float>;
 // the inner cap of the mixed form, also stops it).
 void launch_amg_vcycle(const AmgDev &a, const double *r, double *z, const PcgScalars *sc, cudaStream_t s);
 void launch_amg_vcycle(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s);
-// PCG with the V-cycle: setup and one iteration (p update fused into
-// spmv_dot, update, V-cycle, r.z and beta); d.p2 is the second p buffer.
+// PCG with the V-cycle: setup and one iteration (spmv_dot, update, V-cycle,
+// r.z and beta, p update).
 void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s);
-void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, int parity, cudaStream_t s);
+void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s);
 // The mixed form's PCG: FP64 SpMV, vectors and sums with the FP32 V-cycle as
 // the preconditioner (r32 = float(r) in, z32 out).
 void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
                                 cudaStream_t s);
-void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, int parity,
-                                    cudaStream_t s);
+void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
                     const double *dir_value, double *b, int64_t n, cudaStream_t s);
