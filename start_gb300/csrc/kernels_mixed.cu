@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned 
         v[3] = fix_round32(l[3], k);
         v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
-    deposit_block_flush<256>(key, v, a.tet_nodes, node_fix);
+    deposit_block_flush<256>(key, v, 1LL << k, a.tet_nodes, node_fix);
 }
 
 // Push increment in FP32 from the FP64 field of the plain form's kernel.

@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, Me
         v[3] = fix_round(l3, k);
         v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
-    deposit_block_flush<256>(key, v, m.tet_nodes, node_fix);
+    deposit_block_flush<256>(key, v, 1LL << k, m.tet_nodes, node_fix);
 }
 
 __global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix, double scale,
