@@ -132,7 +132,7 @@ def build_workload(args):
     else:
         w = workload1(n_particles=args.particles, cells=args.cells, seed=0, steps=args.warmup + args.steps)
     w.params["precision"] = 1 if args.precision == "mixed" else 0
-    w.params["preconditioner"] = 1 if args.precond == "amg" else 0
+    w.params["preconditioner"] = {"jacobi": 0, "amg": 1, "amg32": 2}[args.precond]
     return w
 
 
@@ -312,7 +312,7 @@ def run_gpu(args):
         "step": (f"k_step{sfx} + k_walk_queue{sfx} (push, move, collide, walk, settle)", prof["step_ms"],
                  prof["step_bytes"], prof["step_launches"]),
         "pcg": ("PCG iterations (SELL-32 SpMV + dots, updates"
-                + (", AMG V-cycle)" if args.precond == "amg" else ")"), prof["pcg_ms"], prof["pcg_bytes"],
+                + (", AMG V-cycle)" if args.precond != "jacobi" else ")"), prof["pcg_ms"], prof["pcg_bytes"],
                 prof["pcg_iters"]),
         "deposit": (f"k_deposit{sfx} (fixed-point P1 deposit)", prof["deposit_ms"], prof["deposit_bytes"],
                     prof["deposit_launches"]),
@@ -417,7 +417,7 @@ def run_gpu(args):
                  "step_GBps": mp["step_bytes"] / (mp["step_ms"] / 1e3) / 1e9 if mp["step_ms"] > 0 else None,
                  "pcg_GBps": mp["pcg_bytes"] / (mp["pcg_ms"] / 1e3) / 1e9 if mp["pcg_ms"] > 0 else None,
                  "gpu_launches": mp["kernel_launches"],
-                 "dtype": ("f32 state/push/V-cycle, f64 PCG SpMV + vectors + sums" if args.precond == "amg"
+                 "dtype": ("f32 state/push/V-cycle, f64 PCG SpMV + vectors + sums" if args.precond != "jacobi"
                            else "f32 state/push/SpMV, f64 refinement + sums")}
         em.close()
     grad = None
@@ -451,7 +451,7 @@ def main():
     ap.add_argument("--particles", type=int, default=10_000_000)
     ap.add_argument("--cells", type=int, default=100)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--precond", default="amg", choices=["jacobi", "amg"],
+    ap.add_argument("--precond", default="amg32", choices=["jacobi", "amg", "amg32"],
                     help="Poisson PCG preconditioner (both forms)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU sample (0: all)")
     ap.add_argument("--cpu-steps", type=int, default=0, help="timed CPU steps (0: --steps)")

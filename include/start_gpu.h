@@ -73,9 +73,12 @@ typedef enum spg_precision {
  * with MueLu (src/FiniteElementMethod/Solvers/MatrixEquationSolver.cpp:359-427),
  * whose default is smoothed aggregation with Chebyshev smoothing. */
 typedef enum spg_preconditioner {
-    SPG_PRECOND_JACOBI = 0, /* diagonal scaling */
-    SPG_PRECOND_AMG = 1     /* smoothed-aggregation AMG V-cycle, degree-2 Jacobi-Chebyshev smoothing
-                               (FP64 in the plain form, FP32 in the mixed form's inner solve) */
+    SPG_PRECOND_JACOBI = 0,  /* diagonal scaling */
+    SPG_PRECOND_AMG = 1,     /* smoothed-aggregation AMG V-cycle with damped-Jacobi smoothing; the
+                                V-cycle runs in FP64 in the plain form, in FP32 in the mixed form */
+    SPG_PRECOND_AMG_F32 = 2  /* the same V-cycle in FP32 in both forms. The PCG itself (SpMV, vectors,
+                                dot products, stop test) stays FP64, so the solve reaches the same
+                                FP64 residual target; only M^-1 is rounded to FP32 */
 } spg_preconditioner;
 
 /* Particle flag bits returned by spg_get_particles. */

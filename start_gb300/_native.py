@@ -24,7 +24,7 @@ SPG_E_STATE = -8
 
 SPG_COLL_NONE, SPG_COLL_HS, SPG_COLL_VHS, SPG_COLL_VSS = 0, 1, 2, 3
 SPG_FP64, SPG_MIXED = 0, 1
-SPG_PRECOND_JACOBI, SPG_PRECOND_AMG = 0, 1
+SPG_PRECOND_JACOBI, SPG_PRECOND_AMG, SPG_PRECOND_AMG_F32 = 0, 1, 2
 SPG_FLAG_SETTLED, SPG_FLAG_LOST = 1, 2
 
 _pd = C.POINTER(C.c_double)

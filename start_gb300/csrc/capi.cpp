@@ -383,9 +383,13 @@ int setup_amg(spg_handle *h, const HostMesh &hm) {
     std::string err;
     int rc = amg_setup(hm.n_nodes, hm.row_ptr.data(), hm.col.data(), hm.val.data(), ah, err);
     if (rc) return fail(h, rc, err);
-    if (h->mixed) {
+    if (h->mixed || h->prm.preconditioner == SPG_PRECOND_AMG_F32) {
         if ((rc = upload_amg<float>(h, ah, h->sval32, h->amgd32))) return rc;
         h->amg32 = true;
+        if (!h->mixed) {  // the FP32 V-cycle's input and output vectors (the mixed form allocates them anyway)
+            CK(dalloc(&h->r32, hm.n_nodes));
+            CK(dalloc(&h->z32, hm.n_nodes));
+        }
     } else {
         if ((rc = upload_amg<double>(h, ah, h->sval, h->amgd))) return rc;
         h->amg = true;
@@ -395,13 +399,17 @@ int setup_amg(spg_handle *h, const HostMesh &hm) {
 
 // PCG setup and one iteration with the handle's preconditioner.
 void pcg_setup_any(spg_handle *h, const PcgDev &d, const double *b) {
-    if (h->amg)
+    if (h->amg32)
+        launch_pcg_setup_amg_mixed(d, h->amgd32, b, h->r32, h->z32, h->stream);
+    else if (h->amg)
         launch_pcg_setup_amg(d, h->amgd, b, h->stream);
     else
         launch_pcg_setup(d, b, h->stream);
 }
 void pcg_iteration_any(spg_handle *h, PcgDev &d) {
-    if (h->amg)
+    if (h->amg32)
+        launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream);
+    else if (h->amg)
         launch_pcg_iteration_amg(d, h->amgd, h->stream);
     else
         launch_pcg_iteration(d, h->stream);
@@ -818,6 +826,7 @@ int do_solve_mixed(spg_handle *h) {
 int do_solve(spg_handle *h) {
     launch_pcg_rhs(h->node_q, 1.0 / h->prm.epsilon0, h->lift, h->is_dir, h->dir_value, h->b, h->n_nodes, h->stream);
     h->launches += 1;
+    if (h->amg32) return do_solve_mixed_amg(h);
     return h->mixed ? do_solve_mixed(h) : do_solve64(h);
 }
 
@@ -922,7 +931,9 @@ int validate_params(const spg_params *p, std::string &msg) {
     else if (!(p->epsilon0 > 0.0)) msg = "epsilon0 must be > 0";
     else if (p->collision_model < SPG_COLL_NONE || p->collision_model > SPG_COLL_VSS) msg = "bad collision_model";
     else if (p->precision != SPG_FP64 && p->precision != SPG_MIXED) msg = "bad precision";
-    else if (p->preconditioner != SPG_PRECOND_JACOBI && p->preconditioner != SPG_PRECOND_AMG) msg = "bad preconditioner";
+    else if (p->preconditioner != SPG_PRECOND_JACOBI && p->preconditioner != SPG_PRECOND_AMG &&
+             p->preconditioner != SPG_PRECOND_AMG_F32)
+        msg = "bad preconditioner";
     else if (p->collision_model != SPG_COLL_NONE && !(p->gas_mass > 0.0)) msg = "gas_mass must be > 0";
     else if (p->collision_model != SPG_COLL_NONE && !(p->gas_concentration >= 0.0)) msg = "gas_concentration < 0";
     else if (p->collision_model == SPG_COLL_VSS && !(p->alpha > 0.0)) msg = "alpha must be > 0";
@@ -1037,12 +1048,12 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         CK(upload(&h->slice_ptr, sp, s));
         CK(upload(&h->scol, sc, s));
         CK(upload(&h->sval, sv, s));
-        if (h->mixed) {
+        if (h->mixed || h->prm.preconditioner == SPG_PRECOND_AMG_F32) {
             std::vector<float> sv32(sv.begin(), sv.end());
             CK(upload(&h->sval32, sv32, s));
         }
     }
-    if (h->prm.preconditioner == SPG_PRECOND_AMG) {
+    if (h->prm.preconditioner == SPG_PRECOND_AMG || h->prm.preconditioner == SPG_PRECOND_AMG_F32) {
         int rc = setup_amg(h, hm);
         if (rc) return rc;
     }

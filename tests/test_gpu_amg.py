@@ -153,3 +153,21 @@ def test_mixed_run_with_fp32_vcycle_matches_jacobi(built):
     assert (pa["tet"] == pb["tet"]).mean() >= 0.999
     assert np.abs(pa["pos"] - pb["pos"]).max() <= 1e-6
     assert np.abs(ca.astype(np.int64) - cb.astype(np.int64)).sum() <= 2
+
+
+def test_fp32_vcycle_in_the_fp64_form(built):
+    """SPG_PRECOND_AMG_F32 in the FP64 form: the FP64 PCG with the FP32
+    V-cycle reaches the same FP64 residual target as with the FP64 V-cycle,
+    in at most two more iterations, and the potentials agree within 1e-8 of
+    max|phi| (both solves stop at ||r|| <= 1e-13 ||b||). Its adjoint solves
+    use the same preconditioner."""
+    out = {}
+    for precond in (1, 2):
+        w = _w(40, 20000, precond=precond)
+        e, phi, st = _solve_after_gather(w)
+        out[precond] = (phi, st)
+        e.close()
+    (p1, s1), (p2, s2) = out[1], out[2]
+    assert s2["cg_relres_last"] <= 1e-13
+    assert s2["cg_iters_last"] <= s1["cg_iters_last"] + 2
+    assert np.abs(p2 - p1).max() <= 1e-8 * np.abs(p1).max()
