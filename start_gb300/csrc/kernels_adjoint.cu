@@ -98,9 +98,10 @@ __device__ bool collided(const StepConst &c, uint32_t id, int64_t k, double vx, 
     const double u2 = u01_from(r2.v[0], r2.v[1]);
     const double xc = c.model == SPG_COLL_HS ? -1.0 + 2.0 * u1 : u1;
     const double xs = sqrt(1.0 - xc * xc);
-    const double ph = (2.0 * kPi) * u2;
-    nh[0] = xs * cos(ph);
-    nh[1] = xs * sin(ph);
+    double sph, cph;  // the forward's azimuth, cospi / sinpi (2 u2)
+    sincospi(2.0 * u2, &sph, &cph);
+    nh[0] = xs * cph;
+    nh[1] = xs * sph;
     nh[2] = xc;
     return true;
 }
