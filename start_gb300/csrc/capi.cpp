@@ -56,6 +56,7 @@ struct spg_handle {
     double vox_oi[6];
     int32_t vox_dims[3];
     TetRec *rec = nullptr;
+    TetScreen *screen = nullptr;  // hi_float of rec's M and x0, the FP64 step's inside screen
     int4 *nbr = nullptr, *ftri = nullptr, *tet_nodes = nullptr;
     double *node_xyz = nullptr;
     int32_t *row_ptr = nullptr, *col = nullptr;
@@ -452,6 +453,7 @@ int alloc_particles(spg_handle *h, int64_t n) {
 MeshDev mesh_dev(const spg_handle *h) {
     MeshDev m;
     m.rec = h->rec;
+    m.screen = h->screen;
     m.nbr = h->nbr;
     m.ftri = h->ftri;
     m.tet_nodes = h->tet_nodes;
@@ -1031,6 +1033,14 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     for (size_t i = 0; i < hm.diag.size(); ++i) inv_diag[i] = 1.0 / hm.diag[i];
     cudaStream_t s = h->stream;
     CK(upload(&h->rec, hm.rec, s));
+    {
+        std::vector<TetScreen> scr(hm.n_tets);
+        for (int64_t t = 0; t < hm.n_tets; ++t) {
+            for (int k = 0; k < 9; ++k) scr[t].M[k] = hi_float(hm.rec[t].M[k]);
+            for (int k = 0; k < 3; ++k) scr[t].x0[k] = hi_float(hm.rec[t].x0[k]);
+        }
+        CK(upload(&h->screen, scr, s));
+    }
     CK(upload(reinterpret_cast<int32_t **>(&h->nbr), hm.nbr, s));
     CK(upload(reinterpret_cast<int32_t **>(&h->ftri), hm.ftri, s));
     CK(upload(reinterpret_cast<int32_t **>(&h->tet_nodes), hm.tet_nodes, s));
@@ -1142,7 +1152,7 @@ int spg_destroy(spg_handle *h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_particles(h);
-    void *ptrs[] = {h->rec,      h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
+    void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
                     h->node_q,   h->rho,      h->phi,      h->b,         h->r,        h->z,         h->p,
                     h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,

@@ -20,6 +20,7 @@
 #include "philox.h"
 #include "deposit.cuh"
 #include "exact_div.h"
+#include "screen.h"
 #include "spg_internal.h"
 
 namespace spg {
@@ -59,16 +60,6 @@ __device__ __forceinline__ int comp(const int4 &v, int f) {
 }
 
 // ---------------------------------------------------------------- screens
-// Float from the high word of a double (sign, exponent, top 20 mantissa
-// bits), integer ops only: |f - x| <= 2^-20 |x| for 2^-126 <= |x| < 2^128;
-// 0 below that range, +-inf above.
-__device__ __forceinline__ float hi_float(double x) {
-    const int hi = __double2hiint(x);
-    const int a = hi & 0x7fffffff;
-    const int r = a < (897 << 20) ? 0 : (a >= (1151 << 20) ? 0x7f800000 : ((a - (896 << 20)) << 3));
-    return __int_as_float(r | (hi & int(0x80000000)));
-}
-
 // Order-preserving integer key of a double (see order_key_host).
 __device__ __forceinline__ long long order_key(double x) {
     long long b = __double_as_longlong(x);
@@ -108,6 +99,35 @@ __device__ __forceinline__ bool inside_sure_pos(const TetGeo &g, double px, doub
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
         const float m0 = hi_float(g.M[3 * r]), m1 = hi_float(g.M[3 * r + 1]), m2 = hi_float(g.M[3 * r + 2]);
+        l[r] = fmaf(m2, e[2], fmaf(m1, e[1], m0 * e[0]));
+        const float s = fmaf(fabsf(m2), fabsf(e[2]), fmaf(fabsf(m1), fabsf(e[1]), fabsf(m0) * fabsf(e[0])));
+        const float pd = fmaf(fabsf(m2), dl[2], fmaf(fabsf(m1), dl[1], fabsf(m0) * dl[0]));
+        b[r] = fmaf(4e-6f, s, fmaf(1.01f, pd, 1e-30f));
+    }
+    const float l0 = 1.0f - l[0] - l[1] - l[2];
+    const float b0 = b[0] + b[1] + b[2] + 1e-6f;
+    return l[0] > b[0] && l[1] > b[1] && l[2] > b[2] && l0 > b0;
+}
+
+// inside_sure_pos from the tet's TetScreen record (the same truncated floats,
+// so the same decision), without holding the FP64 map in registers.
+__device__ __forceinline__ bool inside_sure_scr(const TetScreen *__restrict__ scr, double px, double py, double pz) {
+    const float4 *sp = reinterpret_cast<const float4 *>(scr);
+    const float4 q0 = __ldg(sp), q1 = __ldg(sp + 1), q2 = __ldg(sp + 2);
+    const float M[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+    const float X0[3] = {q2.y, q2.z, q2.w};
+    const float pf[3] = {hi_float(px), hi_float(py), hi_float(pz)};
+    float e[3], dl[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float x0 = X0[k];
+        e[k] = pf[k] - x0;
+        dl[k] = fmaf(9.6e-7f, fabsf(pf[k]) + fabsf(x0), fmaf(6e-8f, fabsf(e[k]), 1e-30f));
+    }
+    float l[3], b[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float m0 = M[3 * r], m1 = M[3 * r + 1], m2 = M[3 * r + 2];
         l[r] = fmaf(m2, e[2], fmaf(m1, e[1], m0 * e[0]));
         const float s = fmaf(fabsf(m2), fabsf(e[2]), fmaf(fabsf(m1), fabsf(e[1]), fabsf(m0) * fabsf(e[0])));
         const float pd = fmaf(fabsf(m2), dl[2], fmaf(fabsf(m1), dl[1], fabsf(m0) * dl[0]));
@@ -303,23 +323,22 @@ __device__ __forceinline__ bool finite_bits(double x) {
     return ((__double2hiint(x) >> 20) & 0x7ff) != 0x7ff;
 }
 
-// Warp-aggregated append of this lane's item to the walk queue.
-__device__ __forceinline__ void queue_walk(WalkItem *__restrict__ q, unsigned int *__restrict__ qn, bool want,
-                                           int64_t i, double x, double y, double z) {
-    const unsigned ballot = __ballot_sync(kFull, want);
-    if (!ballot) return;
+// Append of this lane's item to the walk queue, called where the lane decides
+// to queue: the lanes converged there share one atomic (their slots follow
+// their lane order; the order of the queue does not matter).
+__device__ __forceinline__ void queue_walk(WalkItem *__restrict__ q, unsigned int *__restrict__ qn, int64_t i,
+                                           double x, double y, double z) {
+    const unsigned act = __activemask();
     const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
+    const int leader = __ffs(act) - 1;
     unsigned base = 0;
-    if (lane == leader) base = atomicAdd(qn, unsigned(__popc(ballot)));
-    base = __shfl_sync(kFull, base, leader);
-    if (want) {
-        WalkItem &w = q[base + __popc(ballot & ((1u << lane) - 1u))];
-        w.i = int32_t(i);
-        w.x0 = x;
-        w.y0 = y;
-        w.z0 = z;
-    }
+    if (lane == leader) base = atomicAdd(qn, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    WalkItem &w = q[base + __popc(act & ((1u << lane) - 1u))];
+    w.i = int32_t(i);
+    w.x0 = x;
+    w.y0 = y;
+    w.z0 = z;
 }
 
 // One particle step (ParticleDynamicsProcessor.cpp:161-200 order):
@@ -334,17 +353,13 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
                                                 WalkItem *__restrict__ wq, unsigned int *__restrict__ wq_n,
                                                 DevCounters *ctr) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    unsigned processed = 0, coll = 0, cross = 0, settled = 0, lost = 0, capped = 0;
-    bool want_walk = false;
-    double x = 0.0, y = 0.0, z = 0.0;
+    unsigned processed = 0, coll = 0, lost = 0;
     if (i < n) {
         uint32_t idf = p.idf[i];
         if (!(idf & kDead)) {
             processed = 1;
             const int t = p.tet[i];
-            x = p.x[i];
-            y = p.y[i];
-            z = p.z[i];
+            const double x = p.x[i], y = p.y[i], z = p.z[i];
             double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
             // |v| < vmin: certainly false when some |v_k| >= 2 vmin (bit compare of
             // non-negative doubles); otherwise the exact FP64 test.
@@ -377,9 +392,7 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
                         lost = 1;
                         p.idf[i] = idf;
                     } else {
-                        TetGeo g;
-                        load_geo(m.rec, t, g);
-                        want_walk = !inside_sure_pos(g, nx, ny, nz);
+                        if (!inside_sure_scr(m.screen + t, nx, ny, nz)) queue_walk(wq, wq_n, i, x, y, z);
                         p.x[i] = nx;
                         p.y[i] = ny;
                         p.z[i] = nz;
@@ -391,28 +404,25 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
             }
         }
     }
-    queue_walk(wq, wq_n, want_walk, i, x, y, z);
-    // Block-level counter reduction, one atomic per counter per block.
-    __shared__ unsigned long long sh[8][6];
+    // Block-level counter reduction, one atomic per counter per block (the
+    // walk kernel counts crossings, settled and capped particles).
+    __shared__ unsigned long long sh[8][3];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned long long a0 = warp_sum(processed), a1 = warp_sum(coll), a2 = warp_sum(cross);
-    unsigned long long a3 = warp_sum(settled), a4 = warp_sum(lost), a5 = warp_sum(capped);
+    const unsigned long long a0 = warp_sum(processed), a1 = warp_sum(coll), a2 = warp_sum(lost);
     if (lane == 0) {
-        sh[wid][0] = a0; sh[wid][1] = a1; sh[wid][2] = a2;
-        sh[wid][3] = a3; sh[wid][4] = a4; sh[wid][5] = a5;
+        sh[wid][0] = a0;
+        sh[wid][1] = a1;
+        sh[wid][2] = a2;
     }
     __syncthreads();
-    if (threadIdx.x < 6) {
+    if (threadIdx.x < 3) {
         unsigned long long s = 0;
         const int nw = blockDim.x >> 5;
         for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
         if (s) {
             unsigned long long *dst = threadIdx.x == 0   ? &ctr->processed
                                       : threadIdx.x == 1 ? &ctr->collisions
-                                      : threadIdx.x == 2 ? &ctr->crossings
-                                      : threadIdx.x == 3 ? &ctr->settled
-                                      : threadIdx.x == 4 ? &ctr->lost
-                                                         : &ctr->capped;
+                                                         : &ctr->lost;
             atomicAdd(dst, s);
         }
     }

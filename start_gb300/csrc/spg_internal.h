@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/start_gpu.h"
+#include "screen.h"
 
 namespace spg {
 
@@ -130,6 +131,7 @@ struct StepConst {
 
 struct MeshDev {
     const TetRec *rec;
+    const TetScreen *screen;  // hi_float of rec's M and x0 (inside screen of the FP64 step)
     const int4 *nbr;
     const int4 *ftri;
     const int4 *tet_nodes;
