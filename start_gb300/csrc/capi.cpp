@@ -73,6 +73,10 @@ struct spg_handle {
     // fields
     double *node_q = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr, *r = nullptr, *z = nullptr,
            *p = nullptr, *q = nullptr, *partials = nullptr;
+    // phi of the previous solve of spg_run and the number of run solves it
+    // has seen (the AMG solves start from 2 phi - phi_prev once there are two)
+    double *phi_prev = nullptr;
+    int32_t phi_hist = 0;
     double *efield = nullptr;                 // 3 per tet
     unsigned long long *node_fix = nullptr;   // fixed-point deposit accumulators
     int fix_bits = 40;                        // deposit quantum 2^-fix_bits of one particle's charge
@@ -1121,6 +1125,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(dalloc(&h->efield, 3 * size_t(h->n_tets)));
     CK(dalloc(&h->rho, n));
     CK(dalloc(&h->phi, n));
+    CK(dalloc(&h->phi_prev, n));
     CK(dalloc(&h->b, n));
     CK(dalloc(&h->r, n));
     CK(dalloc(&h->z, n));
@@ -1154,7 +1159,7 @@ int spg_destroy(spg_handle *h) {
     free_particles(h);
     void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
-                    h->node_q,   h->rho,      h->phi,      h->b,         h->r,        h->z,         h->p,
+                    h->node_q,   h->rho,      h->phi,      h->phi_prev,      h->b,         h->r,        h->z,         h->p,
                     h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
@@ -1197,6 +1202,7 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
     if (n < 0 || n > kMaxParticles) return fail(h, SPG_E_INVALID, "set_particles: n out of range");
     if (n > 0 && (!pos || !vel)) return fail(h, SPG_E_INVALID, "set_particles: null pos/vel");
     CK(cudaSetDevice(h->device));
+    h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
     free_tracks(h);  // a new particle set ends any tracking
     cudaStream_t s = h->stream;
     {
@@ -1312,6 +1318,7 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
     c.seed_lo = uint32_t(src->seed);
     c.seed_hi = uint32_t(src->seed >> 32);
     CK(cudaSetDevice(h->device));
+    h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
     free_tracks(h);  // a new particle set ends any tracking
     cudaStream_t s = h->stream;
     {
@@ -1462,6 +1469,7 @@ __attribute__((unused)) void node_q_from_rho_host(const std::vector<double> &rho
 int spg_solve(spg_handle *h, const double *rho_or_null, double *phi_out, int32_t *iters, double *relres) {
     if (!h) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
+    h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
     if (rho_or_null) {
         std::vector<double> dv(h->n_nodes), q;
         CK(cudaMemcpy(dv.data(), h->dual_vol, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost));
@@ -1508,6 +1516,12 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
         if (h->step % h->prm.poisson_every == 0) {
             rc = do_gather(h);
             if (rc) return rc;
+            if (h->amg || h->amg32) {
+                // initial guess: linear extrapolation of the last two run solves
+                launch_extrapolate(h->phi, h->phi_prev, h->n_nodes, h->phi_hist >= 2, h->stream);
+                h->launches += 1;
+                h->phi_hist++;
+            }
             rc = do_solve(h);
             if (rc == SPG_E_NOT_CONVERGED)
                 status = rc;
@@ -1555,6 +1569,7 @@ int spg_get_potential(spg_handle *h, double *phi) {
 int spg_set_potential(spg_handle *h, const double *phi) {
     if (!h || !phi) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
+    h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
     CK(cudaMemcpyAsync(h->phi, phi, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
     {
         const int rc = update_field(h);
@@ -1600,12 +1615,12 @@ struct CkptHeader {
     int64_t cg_iters_total;
     int32_t cg_iters_last, cg_solves;
     double cg_relres_last;
-    int32_t precision, pad;
+    int32_t precision, phi_hist;
 };
 constexpr uint64_t kMagic = 0x5350474B50543032ull;  // "SPGKPT02"
 size_t particle_bytes(const spg_handle *h) { return h->mixed ? 32 : 56; }
 size_t ckpt_bytes_for(const spg_handle *h, int64_t np) {
-    return sizeof(CkptHeader) + size_t(np) * particle_bytes(h) + size_t(h->n_nodes) * 8 + size_t(h->n_tris) * 4 +
+    return sizeof(CkptHeader) + size_t(np) * particle_bytes(h) + size_t(h->n_nodes) * 16 + size_t(h->n_tris) * 4 +
            sizeof(DevCounters);
 }
 size_t ckpt_bytes(const spg_handle *h) { return ckpt_bytes_for(h, h->np); }
@@ -1638,7 +1653,7 @@ int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
     CK(cudaSetDevice(h->device));
     CkptHeader hd{};
     hd.magic = kMagic;
-    hd.version = 2;
+    hd.version = 3;
     hd.np = h->np;
     hd.n_active = h->n_active;
     hd.step = h->step;
@@ -1651,6 +1666,7 @@ int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
     hd.cg_solves = h->cg_solves;
     hd.cg_relres_last = h->cg_relres_last;
     hd.precision = h->prm.precision;
+    hd.phi_hist = h->phi_hist;
     char *o = static_cast<char *>(buf);
     std::memcpy(o, &hd, sizeof(hd));
     o += sizeof(hd);
@@ -1665,6 +1681,8 @@ int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
     }
     CK(cudaMemcpyAsync(o, h->phi, 8 * h->n_nodes, cudaMemcpyDeviceToHost, s));
     o += 8 * h->n_nodes;
+    CK(cudaMemcpyAsync(o, h->phi_prev, 8 * h->n_nodes, cudaMemcpyDeviceToHost, s));
+    o += 8 * h->n_nodes;
     if (h->n_tris) CK(cudaMemcpyAsync(o, h->tri_count, 4 * h->n_tris, cudaMemcpyDeviceToHost, s));
     o += 4 * h->n_tris;
     CK(cudaMemcpyAsync(o, h->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
@@ -1677,7 +1695,7 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     if (bytes < sizeof(CkptHeader)) return fail(h, SPG_E_INVALID, "restore: buffer too small");
     CkptHeader hd;
     std::memcpy(&hd, buf, sizeof(hd));
-    if (hd.magic != kMagic || hd.version != 2) return fail(h, SPG_E_INVALID, "restore: not a checkpoint");
+    if (hd.magic != kMagic || hd.version != 3) return fail(h, SPG_E_INVALID, "restore: not a checkpoint");
     if (hd.n_nodes != h->n_nodes || hd.n_tris != h->n_tris)
         return fail(h, SPG_E_INVALID, "restore: checkpoint is for a different mesh");
     if (hd.precision != h->prm.precision)
@@ -1704,6 +1722,9 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     }
     CK(cudaMemcpyAsync(h->phi, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
     o += 8 * h->n_nodes;
+    CK(cudaMemcpyAsync(h->phi_prev, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
+    o += 8 * h->n_nodes;
+    h->phi_hist = hd.phi_hist;
     if (h->n_tris) CK(cudaMemcpyAsync(h->tri_count, o, 4 * h->n_tris, cudaMemcpyHostToDevice, s));
     o += 4 * h->n_tris;
     CK(cudaMemcpyAsync(h->ctr, o, sizeof(DevCounters), cudaMemcpyHostToDevice, s));
@@ -1838,6 +1859,7 @@ extern "C" {
 int spg_set_dirichlet(spg_handle *h, const double *g) {
     if (!h || !g) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
+    h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
     double *dg = nullptr;
     CK(dalloc(&dg, h->n_nodes));
     CK(cudaMemcpyAsync(dg, g, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));

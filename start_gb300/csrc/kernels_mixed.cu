@@ -240,14 +240,15 @@ __global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkIt
     bool want_walk = false;
     float x = 0.f, y = 0.f, z = 0.f;
     if (i < a.n) {
-        uint32_t idf = a.p.idf[i];
+        // all of the particle's words in one round trip (the flags gate their use)
+        const uint32_t idf = a.p.idf[i];
+        const int t = a.p.tet[i];
+        x = a.p.x[i];
+        y = a.p.y[i];
+        z = a.p.z[i];
+        float vx = a.p.vx[i], vy = a.p.vy[i], vz = a.p.vz[i];
         if (!(idf & kDead)) {
             processed = 1;
-            const int t = a.p.tet[i];
-            x = a.p.x[i];
-            y = a.p.y[i];
-            z = a.p.z[i];
-            float vx = a.p.vx[i], vy = a.p.vy[i], vz = a.p.vz[i];
             const float vmin = c.vmin_f;
             const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
             const TetRec32 &R = a.rec[t];

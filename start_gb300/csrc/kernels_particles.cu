@@ -355,12 +355,13 @@ __global__ void __launch_bounds__(256, 6) k_step64(DevParticles p, int64_t n, Me
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     unsigned processed = 0, coll = 0, lost = 0;
     if (i < n) {
+        // all of the particle's words in one round trip (the flags gate their use)
         uint32_t idf = p.idf[i];
+        const int t = p.tet[i];
+        const double x = p.x[i], y = p.y[i], z = p.z[i];
+        double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
         if (!(idf & kDead)) {
             processed = 1;
-            const int t = p.tet[i];
-            const double x = p.x[i], y = p.y[i], z = p.z[i];
-            double vx = p.vx[i], vy = p.vy[i], vz = p.vz[i];
             // |v| < vmin: certainly false when some |v_k| >= 2 vmin (bit compare of
             // non-negative doubles); otherwise the exact FP64 test.
             const long long ax = __double_as_longlong(vx) & 0x7fffffffffffffffLL;

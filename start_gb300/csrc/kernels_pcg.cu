@@ -592,3 +592,22 @@ void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s) {
 }
 
 }  // namespace spg
+
+namespace spg {
+
+namespace {
+// phi_prev <- phi; with `extrapolate`: phi <- 2 phi - phi_prev (old values)
+__global__ void k_extrapolate(double *__restrict__ phi, double *__restrict__ phi_prev, int64_t n, int extrapolate) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double t = phi[i];
+    if (extrapolate) phi[i] = fma(2.0, t, -phi_prev[i]);
+    phi_prev[i] = t;
+}
+}  // namespace
+
+void launch_extrapolate(double *phi, double *phi_prev, int64_t n, bool extrapolate, cudaStream_t s) {
+    k_extrapolate<<<unsigned((n + 255) / 256), 256, 0, s>>>(phi, phi_prev, n, extrapolate ? 1 : 0);
+}
+
+}  // namespace spg
