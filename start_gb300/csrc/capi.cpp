@@ -24,6 +24,9 @@ thread_local std::string g_create_error;
 
 constexpr int kEventPool = 8192;
 constexpr int kPcgChunk = 8;
+// Order of the extrapolated initial guess of the AMG run solves (1: linear
+// in the last two potentials, 2: quadratic in the last three).
+constexpr int kExtrapOrder = 2;
 // Mixed form: FP32 inner PCG to 1e-4 of the outer residual (about what an
 // FP32 matrix can resolve for kappa ~ 1e4), at most this many inner
 // iterations per correction and outer refinement steps per solve.
@@ -73,9 +76,10 @@ struct spg_handle {
     // fields
     double *node_q = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr, *r = nullptr, *z = nullptr,
            *p = nullptr, *q = nullptr, *partials = nullptr;
-    // phi of the previous solve of spg_run and the number of run solves it
-    // has seen (the AMG solves start from 2 phi - phi_prev once there are two)
-    double *phi_prev = nullptr;
+    // phi of the two previous solves of spg_run and the number of run solves
+    // they have seen (the AMG solves start from an extrapolation of the last
+    // kExtrapOrder + 1 solutions once there are that many)
+    double *phi_prev = nullptr, *phi_prev2 = nullptr;
     int32_t phi_hist = 0;
     double *efield = nullptr;                 // 3 per tet
     unsigned long long *node_fix = nullptr;   // fixed-point deposit accumulators
@@ -1126,6 +1130,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(dalloc(&h->rho, n));
     CK(dalloc(&h->phi, n));
     CK(dalloc(&h->phi_prev, n));
+    CK(dalloc(&h->phi_prev2, n));
     CK(dalloc(&h->b, n));
     CK(dalloc(&h->r, n));
     CK(dalloc(&h->z, n));
@@ -1159,7 +1164,7 @@ int spg_destroy(spg_handle *h) {
     free_particles(h);
     void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
-                    h->node_q,   h->rho,      h->phi,      h->phi_prev,      h->b,         h->r,        h->z,         h->p,
+                    h->node_q,   h->rho,      h->phi,      h->phi_prev,  h->phi_prev2,      h->b,         h->r,        h->z,         h->p,
                     h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
@@ -1517,8 +1522,9 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
             rc = do_gather(h);
             if (rc) return rc;
             if (h->amg || h->amg32) {
-                // initial guess: linear extrapolation of the last two run solves
-                launch_extrapolate(h->phi, h->phi_prev, h->n_nodes, h->phi_hist >= 2, h->stream);
+                // initial guess: extrapolation of the last run solves
+                launch_extrapolate(h->phi, h->phi_prev, h->phi_prev2, h->n_nodes,
+                                   std::min(kExtrapOrder, h->phi_hist - 1), h->stream);
                 h->launches += 1;
                 h->phi_hist++;
             }
@@ -1620,7 +1626,7 @@ struct CkptHeader {
 constexpr uint64_t kMagic = 0x5350474B50543032ull;  // "SPGKPT02"
 size_t particle_bytes(const spg_handle *h) { return h->mixed ? 32 : 56; }
 size_t ckpt_bytes_for(const spg_handle *h, int64_t np) {
-    return sizeof(CkptHeader) + size_t(np) * particle_bytes(h) + size_t(h->n_nodes) * 16 + size_t(h->n_tris) * 4 +
+    return sizeof(CkptHeader) + size_t(np) * particle_bytes(h) + size_t(h->n_nodes) * 24 + size_t(h->n_tris) * 4 +
            sizeof(DevCounters);
 }
 size_t ckpt_bytes(const spg_handle *h) { return ckpt_bytes_for(h, h->np); }
@@ -1683,6 +1689,8 @@ int spg_checkpoint(spg_handle *h, void *buf, size_t bytes) {
     o += 8 * h->n_nodes;
     CK(cudaMemcpyAsync(o, h->phi_prev, 8 * h->n_nodes, cudaMemcpyDeviceToHost, s));
     o += 8 * h->n_nodes;
+    CK(cudaMemcpyAsync(o, h->phi_prev2, 8 * h->n_nodes, cudaMemcpyDeviceToHost, s));
+    o += 8 * h->n_nodes;
     if (h->n_tris) CK(cudaMemcpyAsync(o, h->tri_count, 4 * h->n_tris, cudaMemcpyDeviceToHost, s));
     o += 4 * h->n_tris;
     CK(cudaMemcpyAsync(o, h->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
@@ -1723,6 +1731,8 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     CK(cudaMemcpyAsync(h->phi, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
     o += 8 * h->n_nodes;
     CK(cudaMemcpyAsync(h->phi_prev, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
+    o += 8 * h->n_nodes;
+    CK(cudaMemcpyAsync(h->phi_prev2, o, 8 * h->n_nodes, cudaMemcpyHostToDevice, s));
     o += 8 * h->n_nodes;
     h->phi_hist = hd.phi_hist;
     if (h->n_tris) CK(cudaMemcpyAsync(h->tri_count, o, 4 * h->n_tris, cudaMemcpyHostToDevice, s));

@@ -596,18 +596,25 @@ void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s) {
 namespace spg {
 
 namespace {
-// phi_prev <- phi; with `extrapolate`: phi <- 2 phi - phi_prev (old values)
-__global__ void k_extrapolate(double *__restrict__ phi, double *__restrict__ phi_prev, int64_t n, int extrapolate) {
+// Shifts the history (prev2 <- prev, prev <- phi) and sets phi to the
+// extrapolation of order `order` (0: phi itself, 1: 2 phi - prev, 2: 3 phi
+// - 3 prev + prev2).
+__global__ void k_extrapolate(double *__restrict__ phi, double *__restrict__ prev, double *__restrict__ prev2,
+                              int64_t n, int order) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double t = phi[i];
-    if (extrapolate) phi[i] = fma(2.0, t, -phi_prev[i]);
-    phi_prev[i] = t;
+    const double t = phi[i], p1 = prev[i];
+    if (order == 1)
+        phi[i] = fma(2.0, t, -p1);
+    else if (order == 2)
+        phi[i] = fma(3.0, t - p1, prev2[i]);
+    prev2[i] = p1;
+    prev[i] = t;
 }
 }  // namespace
 
-void launch_extrapolate(double *phi, double *phi_prev, int64_t n, bool extrapolate, cudaStream_t s) {
-    k_extrapolate<<<unsigned((n + 255) / 256), 256, 0, s>>>(phi, phi_prev, n, extrapolate ? 1 : 0);
+void launch_extrapolate(double *phi, double *prev, double *prev2, int64_t n, int order, cudaStream_t s) {
+    k_extrapolate<<<unsigned((n + 255) / 256), 256, 0, s>>>(phi, prev, prev2, n, order < 0 ? 0 : order);
 }
 
 }  // namespace spg

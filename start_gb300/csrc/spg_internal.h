@@ -318,9 +318,10 @@ PcgGrid pcg_grid32(int64_t n);
 void launch_refine_setup(const PcgDev &d, const PcgDev32 &f, const double *b, cudaStream_t s);
 void launch_pcg32_iteration(PcgDev32 &f, cudaStream_t s);
 void launch_refine_apply(double *x, const float *e, int64_t n, cudaStream_t s);
-// Initial guess of a run solve: phi_prev <- phi, and with `extrapolate`
-// phi <- 2 phi - phi_prev (linear extrapolation of the last two solutions).
-void launch_extrapolate(double *phi, double *phi_prev, int64_t n, bool extrapolate, cudaStream_t s);
+// Initial guess of a run solve: the history shifts (prev2 <- prev <- phi) and
+// phi becomes the polynomial extrapolation of order `order` (0: unchanged,
+// 1: 2 phi - prev, 2: 3 phi - 3 prev + prev2).
+void launch_extrapolate(double *phi, double *prev, double *prev2, int64_t n, int order, cudaStream_t s);
 // CSR -> SELL-32 (slices of 32 rows, column-major, zero padding).
 void build_sell32(int64_t n, const int32_t *row_ptr, const int32_t *col, const double *val,
                   std::vector<int64_t> &slice_ptr, std::vector<int32_t> &scol, std::vector<double> &sval);
