@@ -82,6 +82,15 @@ struct spg_handle {
     double *phi_prev = nullptr, *phi_prev2 = nullptr;
     int32_t phi_hist = 0;
     double *efield = nullptr;                 // 3 per tet
+    uint32_t *tet_stamp = nullptr;            // per tet: epoch of its field (E, H)
+    uint32_t field_epoch = 0;                 // epoch of the current potential's field
+    bool field_full = true;                   // every tet's field is of field_epoch
+    bool in_run = false;                      // inside spg_run: solves refresh the occupied tets only
+    int32_t *occ_list = nullptr;              // tets holding particles at the last deposit
+    unsigned int *occ_n = nullptr;
+    uint32_t *occ_gen = nullptr;              // per tet: generation of the list that holds it
+    uint32_t occ_epoch = 0;                   // field epoch the list was made for
+    uint32_t occ_count = 0;                   // deposits so far (the list generation)
     unsigned long long *node_fix = nullptr;   // fixed-point deposit accumulators
     int fix_bits = 40;                        // deposit quantum 2^-fix_bits of one particle's charge
     PcgScalars *sc = nullptr;
@@ -653,11 +662,15 @@ int do_resort(spg_handle *h) {
 int do_gather(spg_handle *h) {
     if (!h->have_particles) return fail(h, SPG_E_STATE, "gather: no particles set");
     CK(cudaMemsetAsync(h->node_fix, 0, sizeof(unsigned long long) * h->n_nodes, h->stream));
+    // the deposit also lists the occupied tets, for the field of the next solve
+    CK(cudaMemsetAsync(h->occ_n, 0, sizeof(unsigned int), h->stream));
+    h->occ_epoch = h->field_epoch + 1;
+    const OccList occ{h->occ_list, h->occ_n, h->occ_gen, ++h->occ_count};
     ev_begin(h, h->ev_dep);
     if (h->mixed)
-        launch_deposit32(h->Q[h->cur], h->n_active, mesh_dev32(h), h->fix_bits, h->node_fix, h->stream);
+        launch_deposit32(h->Q[h->cur], h->n_active, mesh_dev32(h), h->fix_bits, h->node_fix, occ, h->stream);
     else
-        launch_deposit64(h->P[h->cur], h->n_active, mesh_dev(h), h->fix_bits, h->node_fix, h->stream);
+        launch_deposit64(h->P[h->cur], h->n_active, mesh_dev(h), h->fix_bits, h->node_fix, occ, h->stream);
     ev_end(h, h->ev_dep);
     launch_fix_to_charge(h->node_fix, std::ldexp(h->prm.weight * h->prm.charge, -h->fix_bits), h->node_q,
                          h->n_nodes, h->stream);
@@ -672,22 +685,61 @@ int do_gather(spg_handle *h) {
     return SPG_OK;
 }
 
-// E from phi for both forms (and the FP32 push increment of the mixed form).
-int update_field(spg_handle *h) {
+FieldArgs field_args(const spg_handle *h) {
+    FieldArgs f{};
+    f.tet_nodes = h->tet_nodes;
+    f.phi = h->phi;
+    f.efield = h->efield;
+    f.rec = h->rec;
+    f.rec32 = h->mixed ? h->rec32 : nullptr;
+    f.stamp = h->tet_stamp;
+    f.epoch = h->field_epoch;
+    f.charge = h->prm.charge;
+    f.mass = h->prm.mass;
+    f.inv_mass = 1.0 / h->prm.mass;
+    f.dt = h->prm.dt;
+    f.c32 = ((h->prm.charge / h->prm.mass) * h->prm.dt) / 2.0;
+    return f;
+}
+
+// E from phi for both forms (and the FP32 push increment of the mixed form):
+// every tet, or (sparse, the solves of spg_run) only the tets holding
+// particles; the walks compute the others as particles enter them.
+int update_field(spg_handle *h, bool sparse) {
     ev_begin(h, h->ev_ef);
-    if (h->mixed)
-        launch_efield_mixed(h->tet_nodes, h->rec, h->rec32, h->efield, h->phi, h->n_tets, h->prm.charge, h->prm.mass,
-                            h->prm.dt, h->stream);
-    else
-        launch_efield64(mesh_dev(h), h->rec, h->efield, h->phi, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
+    h->field_epoch++;
+    const FieldArgs f = field_args(h);
+    if (sparse && h->occ_epoch == h->field_epoch) {  // the deposit before this solve listed the tets
+        if (h->mixed)
+            launch_field32_list(f, h->occ_list, h->occ_n, h->stream);
+        else
+            launch_field64_list(f, h->occ_list, h->occ_n, h->stream);
+    } else if (sparse) {
+        if (h->mixed)
+            launch_refresh32(h->Q[h->cur], h->n_active, f, h->stream);
+        else
+            launch_refresh64(h->P[h->cur], h->n_active, f, h->stream);
+    } else if (h->mixed) {
+        launch_field32_full(f, h->n_tets, h->stream);
+    } else {
+        launch_field64_full(f, h->n_tets, h->stream);
+    }
+    h->field_full = !sparse;
     h->launches += 1;
     ev_end(h, h->ev_ef);
     CK(cudaGetLastError());
     return SPG_OK;
 }
 
+// E = 0 everywhere (no solve yet).
+void zero_field(spg_handle *h) {
+    h->field_epoch++;
+    h->field_full = true;
+    launch_zero_field(field_args(h), h->n_tets, h->stream);
+}
+
 int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped) {
-    int rc = update_field(h);
+    int rc = update_field(h, h->in_run);
     if (rc) return rc;
     h->cg_iters_last = iters;
     h->cg_iters_total += iters;
@@ -876,10 +928,10 @@ int do_process(spg_handle *h) {
     ev_begin(h, h->ev_step);
     if (h->mixed)
         launch_step32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
-                      h->stream);
+                      field_args(h), h->stream);
     else
         launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
-                      h->stream);
+                      field_args(h), h->stream);
     ev_end(h, h->ev_step);
     if (h->n_active > 0) h->launches += 2;  // step kernel + queued walks
     CK(cudaGetLastError());
@@ -927,8 +979,8 @@ int reset_run_state(spg_handle *h) {
     CK(cudaMemsetAsync(h->tri_count, 0, sizeof(unsigned int) * std::max<int64_t>(h->n_tris, 1), h->stream));
     CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * h->n_nodes, h->stream));
-    launch_zero_efield(h->rec, h->efield, h->n_tets, h->stream);
-    if (h->mixed) launch_push32(h->rec32, h->efield, h->n_tets, h->prm.charge, h->prm.mass, h->prm.dt, h->stream);
+    zero_field(h);
+    h->phi_hist = 0;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return SPG_OK;
@@ -1127,6 +1179,12 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(dalloc(&h->node_q, n));
     CK(dalloc(&h->node_fix, n));
     CK(dalloc(&h->efield, 3 * size_t(h->n_tets)));
+    CK(dalloc(&h->tet_stamp, size_t(h->n_tets)));
+    CK(dalloc(&h->occ_list, size_t(h->n_tets)));
+    CK(dalloc(&h->occ_n, 1));
+    CK(dalloc(&h->occ_gen, size_t(h->n_tets)));
+    CK(cudaMemsetAsync(h->occ_gen, 0, sizeof(uint32_t) * size_t(h->n_tets), s));
+    CK(cudaMemsetAsync(h->tet_stamp, 0, sizeof(uint32_t) * size_t(h->n_tets), s));
     CK(dalloc(&h->rho, n));
     CK(dalloc(&h->phi, n));
     CK(dalloc(&h->phi_prev, n));
@@ -1165,7 +1223,7 @@ int spg_destroy(spg_handle *h) {
     void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
                     h->node_q,   h->rho,      h->phi,      h->phi_prev,  h->phi_prev2,      h->b,         h->r,        h->z,         h->p,
-                    h->node_fix, h->efield,   h->slice_ptr, h->scol,   h->sval,
+                    h->node_fix, h->efield,   h->tet_stamp, h->occ_list, h->occ_n, h->occ_gen,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
                     h->elim_rp,  h->elim_row, h->elim_col, h->elim_val, h->land, h->gr, h->adj_x, h->adj_v,
@@ -1511,6 +1569,11 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
     if (!h->have_particles) return fail(h, SPG_E_STATE, "run: no particles set");
     if (nsteps < 0) return fail(h, SPG_E_INVALID, "run: nsteps < 0");
     CK(cudaSetDevice(h->device));
+    struct InRun {  // solves of the run refresh the occupied tets only
+        spg_handle *h;
+        explicit InRun(spg_handle *hh) : h(hh) { h->in_run = true; }
+        ~InRun() { h->in_run = false; }
+    } in_run(h);
     int status = SPG_OK;
     for (int32_t k = 0; k < nsteps; ++k) {
         int rc;
@@ -1578,7 +1641,7 @@ int spg_set_potential(spg_handle *h, const double *phi) {
     h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
     CK(cudaMemcpyAsync(h->phi, phi, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
     {
-        const int rc = update_field(h);
+        const int rc = update_field(h, false);
         if (rc) return rc;
     }
     CK(cudaStreamSynchronize(h->stream));
@@ -1588,6 +1651,15 @@ int spg_set_potential(spg_handle *h, const double *phi) {
 int spg_get_efield(spg_handle *h, double *E) {
     if (!h || !E) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
+    if (!h->field_full) {  // the last run solve computed the occupied tets only: complete the field
+        const FieldArgs f = field_args(h);
+        if (h->mixed)
+            launch_field32_full(f, h->n_tets, h->stream);
+        else
+            launch_field64_full(f, h->n_tets, h->stream);
+        CK(cudaGetLastError());
+        h->field_full = true;
+    }
     CK(cudaMemcpyAsync(E, h->efield, sizeof(double) * 3 * h->n_tets, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return SPG_OK;
@@ -1749,10 +1821,9 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     h->cg_relres_last = hd.cg_relres_last;
     h->have_particles = true;
     if (h->cg_solves == 0) {
-        launch_zero_efield(h->rec, h->efield, h->n_tets, s);
-        if (h->mixed) launch_push32(h->rec32, h->efield, h->n_tets, h->prm.charge, h->prm.mass, h->prm.dt, s);
+        zero_field(h);
     } else {
-        const int rc = update_field(h);
+        const int rc = update_field(h, false);
         if (rc) return rc;
     }
     h->fix_bits = fix_bits_for(h->np);
@@ -1944,10 +2015,10 @@ int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, co
         StepConst c = step_const(h);
         if (h->mixed)
             launch_step32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
-                          h->stream, h->land);
+                          field_args(h), h->stream, h->land);
         else
             launch_step64(h->P[h->cur], h->n_active, mesh_dev(h), c, h->tri_count, h->walkq, h->walkq_n, h->ctr,
-                          h->stream, h->land);
+                          field_args(h), h->stream, h->land);
         CK(cudaGetLastError());
         h->step++;
     }
@@ -2003,10 +2074,12 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
             c.step = h->grad_step0 + k;
             if (h->mixed) {
                 launch_record32(work32, n, h->hist, k - k0, s);
-                launch_step32(work32, n, mesh_dev32(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
+                launch_step32(work32, n, mesh_dev32(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch,
+                              field_args(h), s);
             } else {
                 launch_record(work, n, h->hist, k - k0, s);
-                launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch, s);
+                launch_step64(work, n, mesh_dev(h), c, h->tri_scratch, h->walkq, h->walkq_n, h->ctr_scratch,
+                              field_args(h), s);
             }
         }
         StepConst c = step_const(h);

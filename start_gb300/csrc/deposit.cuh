@@ -16,12 +16,14 @@
 
 #include <cstdint>
 
+#include "spg_internal.h"
+
 namespace spg {
 
 template <int NT>
 __device__ __forceinline__ void deposit_block_flush(int key, const long long v[4], long long one,
                                                     const int4 *__restrict__ tet_nodes,
-                                                    unsigned long long *__restrict__ node_fix) {
+                                                    unsigned long long *__restrict__ node_fix, const OccList &occ) {
     constexpr unsigned kAll = 0xffffffffu;
     constexpr int HS = 2 * NT;  // hash slots: node -> block sum
     __shared__ int s_node[HS];
@@ -50,6 +52,8 @@ __device__ __forceinline__ void deposit_block_flush(int key, const long long v[4
     // table (open addressing, linear probing); a full table falls back to a
     // global atomic.
     if (key >= 0 && lane == __ffs(grp) - 1) {
+        if (occ.list && __ldcg(occ.gen_of + key) != occ.gen && atomicExch(occ.gen_of + key, occ.gen) != occ.gen)
+            occ.list[atomicAdd(occ.n, 1u)] = key;
         const int4 tn = __ldg(tet_nodes + key);
         const int nodes[4] = {tn.x, tn.y, tn.z, tn.w};
 #pragma unroll

@@ -17,6 +17,7 @@
 
 #include "philox.h"
 #include "deposit.cuh"
+#include "field.cuh"
 #include "spg_internal.h"
 
 namespace spg {
@@ -311,12 +312,33 @@ __global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkIt
     }
 }
 
+// Mixed form: E per tet in FP64 from phi (the FP32 potential differences
+// across a tet would lose the field), then the FP32 push increment
+// H = float(E c) with c = q dt / (2 m) formed once on the host, so no FP64
+// division runs per tet. The FP64 record of the plain form is not touched.
+__device__ __forceinline__ void field_of_tet32(const FieldArgs &f, int64_t t) {
+    const int4 tn = __ldg(f.tet_nodes + t);
+    const double f0 = f.phi[tn.x], f1 = f.phi[tn.y], f2 = f.phi[tn.z], f3 = f.phi[tn.w];
+    const double d1 = f1 - f0, d2 = f2 - f0, d3 = f3 - f0;
+    const TetRec &r = f.rec[t];
+    double E[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f.efield[3 * t + k] = E[k];
+        f.rec32[t].H[k] = float(E[k] * f.c32);
+    }
+    f.rec32[t].ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
+}
+
 // With land != nullptr a particle that settles records the step, the exit
 // face, its tet and the hit fraction (adjoint).
 __global__ void __launch_bounds__(128) k_walk_queue32(MixedArgs a, int max_cross, const WalkItem32 *__restrict__ wq,
                                                       const unsigned int *__restrict__ wq_n,
                                                       unsigned int *__restrict__ tri_count, DevCounters *ctr,
-                                                      LandRec *__restrict__ land, int64_t step) {
+                                                      LandRec *__restrict__ land, int64_t step,
+                                                      const __grid_constant__ FieldArgs f) {
     const unsigned nq = *wq_n;
     unsigned cross = 0, settled = 0, lost = 0, capped = 0;
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
@@ -344,7 +366,10 @@ __global__ void __launch_bounds__(128) k_walk_queue32(MixedArgs a, int max_cross
             lost++;
             if (w.status == W_CAP) capped++;
         }
-        if (w.tet != t) a.p.tet[i] = w.tet;
+        if (w.tet != t) {
+            a.p.tet[i] = w.tet;
+            if (w.status == W_INSIDE) refresh_tet(f.stamp, f.epoch, w.tet, [&f](int tt) { field_of_tet32(f, tt); });
+        }
     }
     const unsigned long long s0 = __reduce_add_sync(kFull, cross), s1 = __reduce_add_sync(kFull, settled);
     const unsigned long long s2 = __reduce_add_sync(kFull, lost), s3 = __reduce_add_sync(kFull, capped);
@@ -373,7 +398,8 @@ __device__ __forceinline__ long long fix_round32(float x, int k) {
     return b < 0 ? -r : r;
 }
 
-__global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned long long *__restrict__ node_fix) {
+__global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned long long *__restrict__ node_fix,
+                                                   const OccList occ) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int key = -1;
     long long v[4] = {0, 0, 0, 0};
@@ -388,43 +414,36 @@ __global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned 
         v[3] = fix_round32(l[3], k);
         v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
-    deposit_block_flush<256>(key, v, 1LL << k, a.tet_nodes, node_fix);
+    deposit_block_flush<256>(key, v, 1LL << k, a.tet_nodes, node_fix, occ);
 }
 
-// Push increment in FP32 from the FP64 field of the plain form's kernel.
-__global__ void k_push32(TetRec32 *__restrict__ rec, const double *__restrict__ efield, int64_t n, double charge,
-                         double mass, double dt) {
-    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const double E0 = efield[3 * t], E1 = efield[3 * t + 1], E2 = efield[3 * t + 2];
-    rec[t].H[0] = float(((charge * E0) / mass * dt) / 2.0);
-    rec[t].H[1] = float(((charge * E1) / mass * dt) / 2.0);
-    rec[t].H[2] = float(((charge * E2) / mass * dt) / 2.0);
-    rec[t].ezero = (E0 == 0.0 && E1 == 0.0 && E2 == 0.0) ? 1u : 0u;
-}
-
-// Mixed form: E per tet in FP64 from phi (the FP32 potential differences
-// across a tet would lose the field), then the FP32 push increment
-// H = float(E c) with c = q dt / (2 m) formed once on the host, so no FP64
-// division runs per tet. The FP64 record of the plain form is not touched.
-__global__ void k_efield_mixed(const int4 *__restrict__ tet_nodes, const TetRec *__restrict__ rec64,
-                               TetRec32 *__restrict__ rec, double *__restrict__ efield,
-                               const double *__restrict__ phi, int64_t n, double c) {
-    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int4 tn = __ldg(tet_nodes + t);
-    const double f0 = phi[tn.x], f1 = phi[tn.y], f2 = phi[tn.z], f3 = phi[tn.w];
-    const double d1 = f1 - f0, d2 = f2 - f0, d3 = f3 - f0;
-    const TetRec &r = rec64[t];
-    double E[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        efield[3 * t + k] = E[k];
-        rec[t].H[k] = float(E[k] * c);
+// The field of the tets listed by the deposit (each once).
+__global__ void k_field32_list(const __grid_constant__ FieldArgs f, const int32_t *__restrict__ list,
+                               const unsigned int *__restrict__ list_n) {
+    const unsigned nl = *list_n;
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += gridDim.x * blockDim.x) {
+        const int t = list[j];
+        field_of_tet32(f, t);
+        f.stamp[t] = f.epoch;
     }
-    rec[t].ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
+}
+
+__global__ void k_field32_full(const __grid_constant__ FieldArgs f, int64_t n) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    field_of_tet32(f, t);
+    f.stamp[t] = f.epoch;
+}
+
+// The field of every tet holding an alive particle. Particles are tet-sorted
+// (up to the drift since the last re-sort), so only the first lane of each
+// run of equal tets in a warp checks the stamp.
+__global__ void k_refresh32(DevParticles32 p, int64_t n, const __grid_constant__ FieldArgs f) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int key = (i < n && !(p.idf[i] & kDead)) ? p.tet[i] : -1;
+    const int prev = __shfl_up_sync(kFull, key, 1);
+    if (key >= 0 && ((threadIdx.x & 31) == 0 || prev != key))
+        refresh_tet(f.stamp, f.epoch, key, [&f](int t) { field_of_tet32(f, t); });
 }
 
 // Global FP64 state -> local FP32 state (and back).
@@ -658,20 +677,20 @@ MixedArgs make_args(const DevParticles32 &p, int64_t n, const MeshDev32 &m) {
 }  // namespace
 
 void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c,
-                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
-                   LandRec *land) {
+                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, const FieldArgs &f,
+                   cudaStream_t s, LandRec *land) {
     if (n <= 0) return;
     const MixedArgs a = make_args(p, n, m);
     cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
     k_step32<<<grid_for(n, 256), 256, 0, s>>>(a, c, static_cast<WalkItem32 *>(wq), wq_n, ctr);
     k_walk_queue32<<<152 * 8, 128, 0, s>>>(a, c.max_cross, static_cast<WalkItem32 *>(wq), wq_n, tri_count, ctr,
-                                            land, c.step);
+                                            land, c.step, f);
 }
 
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
-                      cudaStream_t s) {
+                      const OccList &occ, cudaStream_t s) {
     if (n <= 0) return;
-    k_deposit32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), k, node_fix);
+    k_deposit32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), k, node_fix, occ);
 }
 
 void launch_record32(const DevParticles32 &p, int64_t n, const AdjHist &h, int k, cudaStream_t s) {
@@ -698,15 +717,16 @@ void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, c
     if (n > 0) k_gather_adj32<<<grid_for(n, 256), 256, 0, s>>>(p, n, ax, av, dx, dv);
 }
 
-void launch_efield_mixed(const int4 *tet_nodes, const TetRec *rec64, TetRec32 *rec, double *efield, const double *phi,
-                         int64_t n_tets, double charge, double mass, double dt, cudaStream_t s) {
-    const double c = ((charge / mass) * dt) / 2.0;
-    k_efield_mixed<<<grid_for(n_tets, 256), 256, 0, s>>>(tet_nodes, rec64, rec, efield, phi, n_tets, c);
+void launch_field32_full(const FieldArgs &f, int64_t n_tets, cudaStream_t s) {
+    if (n_tets > 0) k_field32_full<<<grid_for(n_tets, 256), 256, 0, s>>>(f, n_tets);
 }
 
-void launch_push32(TetRec32 *rec, const double *efield, int64_t n_tets, double charge, double mass, double dt,
-                   cudaStream_t s) {
-    k_push32<<<grid_for(n_tets, 256), 256, 0, s>>>(rec, efield, n_tets, charge, mass, dt);
+void launch_field32_list(const FieldArgs &f, const int32_t *list, const unsigned int *list_n, cudaStream_t s) {
+    k_field32_list<<<152 * 4, 256, 0, s>>>(f, list, list_n);
+}
+
+void launch_refresh32(const DevParticles32 &p, int64_t n, const FieldArgs &f, cudaStream_t s) {
+    if (n > 0) k_refresh32<<<grid_for(n, 256), 256, 0, s>>>(p, n, f);
 }
 
 void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,

@@ -19,6 +19,7 @@
 
 #include "philox.h"
 #include "deposit.cuh"
+#include "field.cuh"
 #include "exact_div.h"
 #include "screen.h"
 #include "spg_internal.h"
@@ -341,6 +342,28 @@ __device__ __forceinline__ void queue_walk(WalkItem *__restrict__ q, unsigned in
     w.z0 = z;
 }
 
+// E per tet: E = -sum_i phi_i grad(lambda_i) = -sum_r (phi_{r+1} - phi_0) M_r
+// (VolumetricMesh::computeElectricFields, VolumetricMesh.cpp:382-411, with the
+// sign and scale of E = -grad(phi)), plus the push increment
+// H = ((q E / m) dt) / 2, the operations of Particle::electroMagneticPush.
+__device__ __forceinline__ void field_of_tet64(const FieldArgs &f, int64_t t) {
+    const int4 tn = __ldg(f.tet_nodes + t);
+    const double f0 = f.phi[tn.x], f1 = f.phi[tn.y], f2 = f.phi[tn.z], f3 = f.phi[tn.w];
+    const double d1 = f1 - f0, d2 = f2 - f0, d3 = f3 - f0;
+    TetRec &r = f.rec[t];
+    double E[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f.efield[3 * t + k] = E[k];
+        const double a = div_by_known(f.charge * E[k], f.mass, f.inv_mass);  // (q E) / m
+        r.H[k] = (a * f.dt) / 2.0;
+    }
+    r.ezero = (((__double_as_longlong(E[0]) | __double_as_longlong(E[1]) | __double_as_longlong(E[2])) << 1) == 0)
+                  ? 1u : 0u;  // all three +-0
+}
+
 // One particle step (ParticleDynamicsProcessor.cpp:161-200 order):
 // settled? -> |v| < vmin? -> outside bbox? -> E push (Boris, B = 0) -> move ->
 // gas collision -> surface crossing along the move segment.
@@ -437,7 +460,7 @@ __global__ void __launch_bounds__(128) k_walk_queue64(DevParticles p, MeshDev m,
                                                       const WalkItem *__restrict__ wq,
                                                       const unsigned int *__restrict__ wq_n,
                                                       unsigned int *__restrict__ tri_count, DevCounters *ctr,
-                                                      LandRec *__restrict__ land, int64_t step) {
+                                                      LandRec *__restrict__ land, int64_t step, const __grid_constant__ FieldArgs f) {
     const unsigned nq = *wq_n;
     unsigned cross = 0, settled = 0, lost = 0, capped = 0;
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
@@ -468,7 +491,10 @@ __global__ void __launch_bounds__(128) k_walk_queue64(DevParticles p, MeshDev m,
             lost++;
             if (w.status == W_CAP) capped++;
         }
-        if (w.tet != t) p.tet[i] = w.tet;
+        if (w.tet != t) {
+            p.tet[i] = w.tet;
+            if (w.status == W_INSIDE) refresh_tet(f.stamp, f.epoch, w.tet, [&f](int tt) { field_of_tet64(f, tt); });
+        }
     }
     const unsigned long long a0 = __reduce_add_sync(kFull, cross), a1 = __reduce_add_sync(kFull, settled);
     const unsigned long long a2 = __reduce_add_sync(kFull, lost), a3 = __reduce_add_sync(kFull, capped);
@@ -506,7 +532,7 @@ __device__ __forceinline__ long long fix_round(double x, int k) {
 // particles; runs of equal tet are summed over the block (deposit.cuh) and
 // the last thread of each run issues the four atomics.
 __global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, MeshDev m, int k,
-                                                   unsigned long long *__restrict__ node_fix) {
+                                                   unsigned long long *__restrict__ node_fix, const OccList occ) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int key = -1;
     long long v[4] = {0, 0, 0, 0};
@@ -523,7 +549,7 @@ __global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, Me
         v[3] = fix_round(l3, k);
         v[0] = (1LL << k) - v[1] - v[2] - v[3];
     }
-    deposit_block_flush<256>(key, v, 1LL << k, m.tet_nodes, node_fix);
+    deposit_block_flush<256>(key, v, 1LL << k, m.tet_nodes, node_fix, occ);
 }
 
 __global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix, double scale,
@@ -533,41 +559,53 @@ __global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix,
     node_q[i] = double((long long)node_fix[i]) * scale;
 }
 
-// E per tet: E = -sum_i phi_i grad(lambda_i) = -sum_r (phi_{r+1} - phi_0) M_r
-// (VolumetricMesh::computeElectricFields, VolumetricMesh.cpp:382-411, with the
-// sign and scale of E = -grad(phi)), plus the push increment
-// H = ((q E / m) dt) / 2, the operations of Particle::electroMagneticPush.
-__global__ void k_efield64(MeshDev m, TetRec *__restrict__ rec, double *__restrict__ efield,
-                           const double *__restrict__ phi, double charge, double mass, double inv_mass, double dt) {
-    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= m.n_tets) return;
-    const int4 tn = __ldg(m.tet_nodes + t);
-    const double f0 = phi[tn.x], f1 = phi[tn.y], f2 = phi[tn.z], f3 = phi[tn.w];
-    const double d1 = f1 - f0, d2 = f2 - f0, d3 = f3 - f0;
-    TetRec &r = rec[t];
-    double E[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        efield[3 * t + k] = E[k];
-        const double a = div_by_known(charge * E[k], mass, inv_mass);  // (q E) / m
-        r.H[k] = (a * dt) / 2.0;
+// The field of the tets listed by the deposit (each once).
+__global__ void k_field64_list(const __grid_constant__ FieldArgs f, const int32_t *__restrict__ list,
+                               const unsigned int *__restrict__ list_n) {
+    const unsigned nl = *list_n;
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += gridDim.x * blockDim.x) {
+        const int t = list[j];
+        field_of_tet64(f, t);
+        f.stamp[t] = f.epoch;
     }
-    r.ezero = (((__double_as_longlong(E[0]) | __double_as_longlong(E[1]) | __double_as_longlong(E[2])) << 1) == 0)
-                  ? 1u : 0u;  // all three +-0
 }
 
-__global__ void k_zero_efield(TetRec *__restrict__ rec, double *__restrict__ efield, int64_t n) {
+__global__ void k_field64_full(const __grid_constant__ FieldArgs f, int64_t n) {
     const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    rec[t].H[0] = 0.0;
-    rec[t].H[1] = 0.0;
-    rec[t].H[2] = 0.0;
-    rec[t].ezero = 1u;
-    efield[3 * t] = 0.0;
-    efield[3 * t + 1] = 0.0;
-    efield[3 * t + 2] = 0.0;
+    field_of_tet64(f, t);
+    f.stamp[t] = f.epoch;
+}
+
+// The field of every tet holding an alive particle. Particles are tet-sorted
+// (up to the drift since the last re-sort), so only the first lane of each
+// run of equal tets in a warp checks the stamp.
+__global__ void k_refresh64(DevParticles p, int64_t n, const __grid_constant__ FieldArgs f) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int key = (i < n && !(p.idf[i] & kDead)) ? p.tet[i] : -1;
+    const int prev = __shfl_up_sync(kFull, key, 1);
+    if (key >= 0 && ((threadIdx.x & 31) == 0 || prev != key))
+        refresh_tet(f.stamp, f.epoch, key, [&f](int t) { field_of_tet64(f, t); });
+}
+
+// E = 0 and H = 0 everywhere (before the first solve), stamped.
+__global__ void k_zero_field(const __grid_constant__ FieldArgs f, int64_t n) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    f.rec[t].H[0] = 0.0;
+    f.rec[t].H[1] = 0.0;
+    f.rec[t].H[2] = 0.0;
+    f.rec[t].ezero = 1u;
+    if (f.rec32) {
+        f.rec32[t].H[0] = 0.0f;
+        f.rec32[t].H[1] = 0.0f;
+        f.rec32[t].H[2] = 0.0f;
+        f.rec32[t].ezero = 1u;
+    }
+    f.efield[3 * t] = 0.0;
+    f.efield[3 * t + 1] = 0.0;
+    f.efield[3 * t + 2] = 0.0;
+    f.stamp[t] = f.epoch;
 }
 
 __global__ void k_count_lost(const int32_t *__restrict__ tet, int64_t n, unsigned long long *out) {
@@ -779,17 +817,18 @@ inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1)
 }  // namespace
 
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c, unsigned int *tri_count,
-                   WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s, LandRec *land) {
+                   WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, const FieldArgs &f, cudaStream_t s,
+                   LandRec *land) {
     if (n <= 0) return;
     cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
     k_step64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, c, wq, wq_n, ctr);
-    k_walk_queue64<<<152 * 8, 128, 0, s>>>(p, m, c.max_cross, wq, wq_n, tri_count, ctr, land, c.step);
+    k_walk_queue64<<<152 * 8, 128, 0, s>>>(p, m, c.max_cross, wq, wq_n, tri_count, ctr, land, c.step, f);
 }
 
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,
-                      cudaStream_t s) {
+                      const OccList &occ, cudaStream_t s) {
     if (n <= 0) return;
-    k_deposit64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, k, node_fix);
+    k_deposit64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, k, node_fix, occ);
 }
 
 void launch_fix_to_charge(const unsigned long long *node_fix, double scale, double *node_q, int64_t n,
@@ -797,13 +836,20 @@ void launch_fix_to_charge(const unsigned long long *node_fix, double scale, doub
     k_fix_to_charge<<<grid_for(n, 256), 256, 0, s>>>(node_fix, scale, node_q, n);
 }
 
-void launch_efield64(const MeshDev &m, TetRec *rec, double *efield, const double *phi, double charge, double mass,
-                     double dt, cudaStream_t s) {
-    k_efield64<<<grid_for(m.n_tets, 256), 256, 0, s>>>(m, rec, efield, phi, charge, mass, 1.0 / mass, dt);
+void launch_field64_full(const FieldArgs &f, int64_t n_tets, cudaStream_t s) {
+    if (n_tets > 0) k_field64_full<<<grid_for(n_tets, 256), 256, 0, s>>>(f, n_tets);
 }
 
-void launch_zero_efield(TetRec *rec, double *efield, int64_t n_tets, cudaStream_t s) {
-    k_zero_efield<<<grid_for(n_tets, 256), 256, 0, s>>>(rec, efield, n_tets);
+void launch_field64_list(const FieldArgs &f, const int32_t *list, const unsigned int *list_n, cudaStream_t s) {
+    k_field64_list<<<152 * 4, 256, 0, s>>>(f, list, list_n);
+}
+
+void launch_refresh64(const DevParticles &p, int64_t n, const FieldArgs &f, cudaStream_t s) {
+    if (n > 0) k_refresh64<<<grid_for(n, 256), 256, 0, s>>>(p, n, f);
+}
+
+void launch_zero_field(const FieldArgs &f, int64_t n_tets, cudaStream_t s) {
+    if (n_tets > 0) k_zero_field<<<grid_for(n_tets, 256), 256, 0, s>>>(f, n_tets);
 }
 
 void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, cudaStream_t s) {

@@ -183,25 +183,35 @@ void launch_set_dirichlet(const uint8_t *is_dir, const double *g, double *dir_va
 void launch_gather_adj(const DevParticles &p, int64_t n, const double *ax, const double *av, double *dx, double *dv,
                        cudaStream_t s);
 
+struct FieldArgs;
+// List of the tets that hold particles at a deposit (the tets whose field the
+// next solve of a run must compute): gen_of[t] == gen marks a listed tet.
+struct OccList {
+    int32_t *list;  // nullptr: no list is kept
+    unsigned int *n;
+    uint32_t *gen_of;
+    uint32_t gen;
+};
 // Kernel launchers (kernels_particles.cu).
 // Step kernel plus the exact walk of the queued particles (wq holds up to n
-// items); land (nullable) receives the landing records.
+// items); land (nullable) receives the landing records; a walk that brings a
+// particle into a tet with an older field computes that tet's field (f).
 void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const StepConst &c,
-                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
-                   LandRec *land = nullptr);
+                   unsigned int *tri_count, WalkItem *wq, unsigned int *wq_n, DevCounters *ctr, const FieldArgs &f,
+                   cudaStream_t s, LandRec *land = nullptr);
 // Fixed-point P1 deposit: node_fix[n] += round(lambda_n * 2^k) per alive
 // particle (lambda_0 takes the remainder so each particle adds exactly 2^k).
+// occ (list nullable) collects the tets holding particles.
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,
-                      cudaStream_t s);
+                      const OccList &occ, cudaStream_t s);
 // node_q = node_fix * scale
 void launch_fix_to_charge(const unsigned long long *node_fix, double scale, double *node_q, int64_t n,
                           cudaStream_t s);
-void launch_efield64(const MeshDev &m, TetRec *rec, double *efield, const double *phi, double charge, double mass,
-                     double dt, cudaStream_t s);
 void launch_locate(const double *pos, int64_t n, const MeshDev &m, const int32_t *vox_seed,
                    const double *vox_origin_inv, const int32_t *vox_dims, int max_cross,
                    int32_t *tet_out, cudaStream_t s);
-void launch_zero_efield(TetRec *rec, double *efield, int64_t n_tets, cudaStream_t s);
+// E = 0 and H = 0 in every tet, stamped with f.epoch (both forms' records).
+void launch_zero_field(const FieldArgs &f, int64_t n_tets, cudaStream_t s);
 void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, cudaStream_t s);
 void launch_init_particles(const double *pos, const double *vel, const int32_t *tet, int64_t n,
                            DevParticles p, cudaStream_t s);
@@ -232,6 +242,31 @@ struct alignas(64) TetRec32 {
 };
 static_assert(sizeof(TetRec32) == 64, "TetRec32 must be 64 bytes");
 
+// Per-tet field (E and the push increment H with its E-null flag) of the
+// current potential. A full update computes every tet. After a solve inside
+// spg_run only the tets holding particles are computed (launch_refresh*),
+// and a walk that brings a particle into a tet whose field belongs to an
+// older potential (stamp[t] != epoch) computes that tet there: the first
+// lane to swap the stamp computes, the values are those of the full update,
+// and the next step (a later launch) reads them.
+struct FieldArgs {
+    const int4 *tet_nodes;
+    const double *phi;
+    double *efield;    // 3 per tet
+    TetRec *rec;       // FP64 map (read); H and ezero written in the FP64 form
+    TetRec32 *rec32;   // mixed form: FP32 H and ezero written; nullptr in the FP64 form
+    uint32_t *stamp;   // per tet: epoch of its field
+    uint32_t epoch;
+    double charge, mass, inv_mass, dt;
+    double c32;        // mixed form: q dt / (2 m)
+};
+void launch_field64_full(const FieldArgs &f, int64_t n_tets, cudaStream_t s);
+void launch_field32_full(const FieldArgs &f, int64_t n_tets, cudaStream_t s);
+void launch_refresh64(const DevParticles &p, int64_t n, const FieldArgs &f, cudaStream_t s);
+// The field of the tets a deposit listed (list_n entries on the device).
+void launch_field64_list(const FieldArgs &f, const int32_t *list, const unsigned int *list_n, cudaStream_t s);
+void launch_field32_list(const FieldArgs &f, const int32_t *list, const unsigned int *list_n, cudaStream_t s);
+
 // 32 B per particle: position relative to the owning tet's centroid.
 struct DevParticles32 {
     float *x, *y, *z, *vx, *vy, *vz;
@@ -249,8 +284,9 @@ struct MeshDev32 {
 
 // kernels_mixed.cu
 void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c,
-                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, cudaStream_t s,
-                   LandRec *land = nullptr);
+                   unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, const FieldArgs &f,
+                   cudaStream_t s, LandRec *land = nullptr);
+void launch_refresh32(const DevParticles32 &p, int64_t n, const FieldArgs &f, cudaStream_t s);
 // adjoint of the FP32 form (kernels_mixed.cu)
 void launch_record32(const DevParticles32 &p, int64_t n, const AdjHist &h, int k, cudaStream_t s);
 void launch_objective32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const LandRec *land,
@@ -261,11 +297,7 @@ void launch_backward32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, c
 void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, const double *av, double *dx,
                          double *dv, cudaStream_t s);
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
-                      cudaStream_t s);
-void launch_efield_mixed(const int4 *tet_nodes, const TetRec *rec64, TetRec32 *rec, double *efield, const double *phi,
-                         int64_t n_tets, double charge, double mass, double dt, cudaStream_t s);
-void launch_push32(TetRec32 *rec, const double *efield, int64_t n_tets, double charge, double mass, double dt,
-                   cudaStream_t s);
+                      const OccList &occ, cudaStream_t s);
 void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
                      DevParticles32 p, cudaStream_t s);
 void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,
