@@ -47,12 +47,19 @@ __device__ __forceinline__ void load_geo(const TetRec *__restrict__ rec, int t, 
     g.x0[0] = e.y; g.x0[1] = f.x; g.x0[2] = f.y;
 }
 
-// Barycentric coordinates; same expression order as the oracle.
-__device__ __forceinline__ void bary(const TetGeo &g, double px, double py, double pz, double l[4]) {
-    const double d0 = px - g.x0[0], d1 = py - g.x0[1], d2 = pz - g.x0[2];
-    l[1] = g.M[0] * d0 + g.M[1] * d1 + g.M[2] * d2;
-    l[2] = g.M[3] * d0 + g.M[4] * d1 + g.M[5] * d2;
-    l[3] = g.M[6] * d0 + g.M[7] * d1 + g.M[8] * d2;
+// Barycentric coordinates from the tet's record in memory (L1-resident
+// during a walk), so a walk holds no FP64 map in registers; same values as
+// the oracle's evaluation order.
+__device__ __forceinline__ void bary_rec(const TetRec *__restrict__ r, double px, double py, double pz,
+                                         double l[4]) {
+    const double2 *rp = reinterpret_cast<const double2 *>(r);
+    const double2 e = __ldg(rp + 4), f = __ldg(rp + 5);
+    const double d0 = px - e.y, d1 = py - f.x, d2 = pz - f.y;
+    const double2 a = __ldg(rp + 0), b = __ldg(rp + 1);
+    l[1] = a.x * d0 + a.y * d1 + b.x * d2;
+    const double2 c = __ldg(rp + 2), d = __ldg(rp + 3);
+    l[2] = b.y * d0 + c.x * d1 + c.y * d2;
+    l[3] = d.x * d0 + d.y * d1 + e.x * d2;
     l[0] = 1.0 - l[1] - l[2] - l[3];
 }
 
@@ -74,9 +81,10 @@ __device__ __forceinline__ bool same_value(double a, double b) {
     return x == y || ((x | y) << 1) == 0;
 }
 
-// Screened inside test: true = lambda(p) >= 0 in all four coordinates for
-// certain; false = undecided (the caller evaluates the exact FP64 walk). No
-// FP64 instruction runs: M is truncated to 20 mantissa bits and
+// Screened inside test from the tet's TetScreen record: true = lambda(p) >= 0
+// in all four coordinates for certain; false = undecided (the caller
+// evaluates the exact FP64 walk). No FP64 instruction runs: M is truncated to
+// 20 mantissa bits (hi_float, once per tet on the host) and
 // d = p - x0 is formed in FP32 from p and x0 truncated the same way (integer
 // ops). With S_i = sum_j |M_ij d_j|, the truncation of M and the FP32
 // products put lambda_i within 2.2e-6 S_i of its value for the exact d; the
@@ -87,31 +95,6 @@ __device__ __forceinline__ bool same_value(double a, double b) {
 // That adds sum_k |M_ik| delta_k (times 1.01 for the truncation of M) to the
 // margin of lambda_i; lambda_0 = 1 - sum gets the sum of the three margins
 // plus 1e-6 for its own FP32 rounding.
-__device__ __forceinline__ bool inside_sure_pos(const TetGeo &g, double px, double py, double pz) {
-    const float pf[3] = {hi_float(px), hi_float(py), hi_float(pz)};
-    float e[3], dl[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float x0 = hi_float(g.x0[k]);
-        e[k] = pf[k] - x0;
-        dl[k] = fmaf(9.6e-7f, fabsf(pf[k]) + fabsf(x0), fmaf(6e-8f, fabsf(e[k]), 1e-30f));
-    }
-    float l[3], b[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        const float m0 = hi_float(g.M[3 * r]), m1 = hi_float(g.M[3 * r + 1]), m2 = hi_float(g.M[3 * r + 2]);
-        l[r] = fmaf(m2, e[2], fmaf(m1, e[1], m0 * e[0]));
-        const float s = fmaf(fabsf(m2), fabsf(e[2]), fmaf(fabsf(m1), fabsf(e[1]), fabsf(m0) * fabsf(e[0])));
-        const float pd = fmaf(fabsf(m2), dl[2], fmaf(fabsf(m1), dl[1], fabsf(m0) * dl[0]));
-        b[r] = fmaf(4e-6f, s, fmaf(1.01f, pd, 1e-30f));
-    }
-    const float l0 = 1.0f - l[0] - l[1] - l[2];
-    const float b0 = b[0] + b[1] + b[2] + 1e-6f;
-    return l[0] > b[0] && l[1] > b[1] && l[2] > b[2] && l0 > b0;
-}
-
-// inside_sure_pos from the tet's TetScreen record (the same truncated floats,
-// so the same decision), without holding the FP64 map in registers.
 __device__ __forceinline__ bool inside_sure_scr(const TetScreen *__restrict__ scr, double px, double py, double pz) {
     const float4 *sp = reinterpret_cast<const float4 *>(scr);
     const float4 q0 = __ldg(sp), q1 = __ldg(sp + 1), q2 = __ldg(sp + 2);
@@ -154,8 +137,8 @@ struct WalkOut {
 // crossing the FP32 inside screen usually decides; lambda(p0) and the
 // divisions are formed only when two or more faces compete or s is returned
 // (the same expressions as the full evaluation, so the same values).
-__device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double p0x, double p0y, double p0z,
-                                       double p1x, double p1y, double p1z, int max_cross, bool stop_surface) {
+__device__ __noinline__ WalkOut walk64(const MeshDev m, int t, double p0x, double p0y, double p0z, double p1x,
+                                       double p1y, double p1z, int max_cross, bool stop_surface) {
     WalkOut o;
     o.crossings = 0;
     o.tri = -1;
@@ -163,13 +146,14 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
     o.s = 1.0;
     int enter = -1;
     for (;;) {
-        if (enter >= 0 && inside_sure_pos(g, p1x, p1y, p1z)) {
+        if (enter >= 0 && inside_sure_scr(m.screen + t, p1x, p1y, p1z)) {
             o.tet = t;
             o.status = W_INSIDE;
             return o;
         }
+        const TetRec *rt = m.rec + t;
         double l1[4];
-        bary(g, p1x, p1y, p1z, l1);
+        bary_rec(rt, p1x, p1y, p1z, l1);
         if (l1[0] >= 0.0 && l1[1] >= 0.0 && l1[2] >= 0.0 && l1[3] >= 0.0) {
             o.tet = t;
             o.status = W_INSIDE;
@@ -191,7 +175,7 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
         double sb = 0.0;
         bool have_s = false;
         if (ncand > 1) {
-            bary(g, p0x, p0y, p0z, l0);
+            bary_rec(rt, p0x, p0y, p0z, l0);
             best = -1;
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
@@ -208,7 +192,7 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
         const int nb = comp(__ldg(m.nbr + t), best);
         const bool surface = stop_surface && tri >= 0;
         if ((surface || nb < 0) && !have_s) {
-            bary(g, p0x, p0y, p0z, l0);
+            bary_rec(rt, p0x, p0y, p0z, l0);
             sb = l0[best] / (l0[best] - l1[best]);
         }
         if (surface) {
@@ -233,7 +217,6 @@ __device__ __noinline__ WalkOut walk64(const MeshDev m, int t, TetGeo g, double 
         o.crossings++;
         t = nb >> 2;
         enter = nb & 3;
-        load_geo(m.rec, t, g);
     }
 }
 
@@ -468,9 +451,7 @@ __global__ void __launch_bounds__(128) k_walk_queue64(DevParticles p, MeshDev m,
         const int64_t i = it.i;
         const int t = p.tet[i];
         const double nx = p.x[i], ny = p.y[i], nz = p.z[i];
-        TetGeo g;
-        load_geo(m.rec, t, g);
-        const WalkOut w = walk64(m, t, g, it.x0, it.y0, it.z0, nx, ny, nz, max_cross, true);
+        const WalkOut w = walk64(m, t, it.x0, it.y0, it.z0, nx, ny, nz, max_cross, true);
         cross += unsigned(w.crossings);
         uint32_t idf = p.idf[i];
         if (w.status == W_SURFACE) {
@@ -636,9 +617,7 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t n, MeshDev m, c
     for (int k = 0; k < 3; ++k)
         c[k] = 0.25 * (((m.node_xyz[3 * tn.x + k] + m.node_xyz[3 * tn.y + k]) + m.node_xyz[3 * tn.z + k]) +
                        m.node_xyz[3 * tn.w + k]);
-    TetGeo g;
-    load_geo(m.rec, seed, g);
-    const WalkOut w = walk64(m, seed, g, c[0], c[1], c[2], px, py, pz, max_cross, false);
+    const WalkOut w = walk64(m, seed, c[0], c[1], c[2], px, py, pz, max_cross, false);
     tet_out[i] = w.status == W_INSIDE ? w.tet : -1;
 }
 
