@@ -13,6 +13,7 @@
 //   * the deposit accumulates in 64-bit fixed point (exact).
 // Every other operation (push, move, collision, exit parameter) is FP32,
 // which on GB300 issues ~60x faster than FP64.
+#include <algorithm>
 #include <cmath>
 
 #include "philox.h"
@@ -234,74 +235,98 @@ struct WalkItem32 {
     float x0, y0, z0;
 };
 
-__global__ void __launch_bounds__(256) k_step32(MixedArgs a, StepConst c, WalkItem32 *__restrict__ wq,
+// The eight 4-byte words of one particle.
+struct Words32 {
+    uint32_t idf;
+    int t;
+    float x, y, z, vx, vy, vz;
+};
+
+__device__ __forceinline__ Words32 load_words32(const DevParticles32 &p, int64_t i) {
+    Words32 w;
+    w.idf = p.idf[i];
+    w.t = p.tet[i];
+    w.x = p.x[i];
+    w.y = p.y[i];
+    w.z = p.z[i];
+    w.vx = p.vx[i];
+    w.vy = p.vy[i];
+    w.vz = p.vz[i];
+    return w;
+}
+
+// Append of this lane's item to the walk queue where the lane decides (the
+// lanes converged there share one atomic; queue order does not matter).
+__device__ __forceinline__ void queue_walk32(WalkItem32 *__restrict__ q, unsigned int *__restrict__ qn, int64_t i,
+                                             float x, float y, float z) {
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(qn, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    WalkItem32 &w = q[base + __popc(act & ((1u << lane) - 1u))];
+    w.i = int32_t(i);
+    w.x0 = x;
+    w.y0 = y;
+    w.z0 = z;
+}
+
+// Grid-stride over the particles: the next particle's words are loaded
+// before the current one is computed, so each thread keeps a particle's
+// loads in flight while it works (the kernel is bound by memory latency).
+__global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, WalkItem32 *__restrict__ wq,
                                                 unsigned int *__restrict__ wq_n, DevCounters *ctr) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     unsigned processed = 0, coll = 0, lost = 0;
-    bool want_walk = false;
-    float x = 0.f, y = 0.f, z = 0.f;
-    if (i < a.n) {
-        // all of the particle's words in one round trip (the flags gate their use)
-        const uint32_t idf = a.p.idf[i];
-        const int t = a.p.tet[i];
-        x = a.p.x[i];
-        y = a.p.y[i];
-        z = a.p.z[i];
-        float vx = a.p.vx[i], vy = a.p.vy[i], vz = a.p.vz[i];
-        if (!(idf & kDead)) {
-            processed = 1;
-            const float vmin = c.vmin_f;
-            const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
-            const TetRec32 &R = a.rec[t];
-            const float gx = __ldg(&R.cen[0]) + x, gy = __ldg(&R.cen[1]) + y, gz = __ldg(&R.cen[2]) + z;
-            const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
-                                gz >= c.lo_f[2] && gz <= c.hi_f[2];
-            if (!slow && in_box) {
-                if (!__ldg(&R.ezero)) {
-                    const float hx = __ldg(&R.H[0]), hy = __ldg(&R.H[1]), hz = __ldg(&R.H[2]);
-                    vx = (vx + hx) + hx;
-                    vy = (vy + hy) + hy;
-                    vz = (vz + hz) + hz;
-                }
-                const float dt = c.dt_f;
-                const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
-                if (!(nx == x && ny == y && nz == z)) {
-                    if (c.model != SPG_COLL_NONE) coll = collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
-                    if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
-                        a.p.idf[i] = idf | kLost;
-                        lost = 1;
-                    } else {
-                        Geo32 g;
-                        load_geo32(a.rec, t, g);
-                        float l[4];
-                        bary32(g, nx, ny, nz, l);
-                        const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
-                        want_walk = !(mn > kNearZero);
-                        a.p.x[i] = nx;
-                        a.p.y[i] = ny;
-                        a.p.z[i] = nz;
-                    }
-                }
-                a.p.vx[i] = vx;
-                a.p.vy[i] = vy;
-                a.p.vz[i] = vz;
+    Words32 cur{};
+    if (i < a.n) cur = load_words32(a.p, i);
+    for (; i < a.n; i += stride) {
+        Words32 nxt{};
+        if (i + stride < a.n) nxt = load_words32(a.p, i + stride);
+        const uint32_t idf = cur.idf;
+        const int t = cur.t;
+        const float x = cur.x, y = cur.y, z = cur.z;
+        float vx = cur.vx, vy = cur.vy, vz = cur.vz;
+        cur = nxt;
+        if (idf & kDead) continue;
+        processed++;
+        const float vmin = c.vmin_f;
+        const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
+        const TetRec32 &R = a.rec[t];
+        const float gx = __ldg(&R.cen[0]) + x, gy = __ldg(&R.cen[1]) + y, gz = __ldg(&R.cen[2]) + z;
+        const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
+                            gz >= c.lo_f[2] && gz <= c.hi_f[2];
+        if (slow || !in_box) continue;
+        if (!__ldg(&R.ezero)) {
+            const float hx = __ldg(&R.H[0]), hy = __ldg(&R.H[1]), hz = __ldg(&R.H[2]);
+            vx = (vx + hx) + hx;
+            vy = (vy + hy) + hy;
+            vz = (vz + hz) + hz;
+        }
+        const float dt = c.dt_f;
+        const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
+        if (!(nx == x && ny == y && nz == z)) {
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
+            if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
+                a.p.idf[i] = idf | kLost;
+                lost++;
+            } else {
+                Geo32 g;
+                load_geo32(a.rec, t, g);
+                float l[4];
+                bary32(g, nx, ny, nz, l);
+                const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
+                if (!(mn > kNearZero)) queue_walk32(wq, wq_n, i, x, y, z);
+                a.p.x[i] = nx;
+                a.p.y[i] = ny;
+                a.p.z[i] = nz;
             }
         }
-    }
-    const unsigned ballot = __ballot_sync(kFull, want_walk);
-    if (ballot) {
-        const int lane = threadIdx.x & 31;
-        const int leader = __ffs(ballot) - 1;
-        unsigned base = 0;
-        if (lane == leader) base = atomicAdd(wq_n, unsigned(__popc(ballot)));
-        base = __shfl_sync(kFull, base, leader);
-        if (want_walk) {
-            WalkItem32 &w = wq[base + __popc(ballot & ((1u << lane) - 1u))];
-            w.i = int32_t(i);
-            w.x0 = x;
-            w.y0 = y;
-            w.z0 = z;
-        }
+        a.p.vx[i] = vx;
+        a.p.vy[i] = vy;
+        a.p.vz[i] = vz;
     }
     const unsigned long long s0 = __reduce_add_sync(kFull, processed), s1 = __reduce_add_sync(kFull, coll);
     const unsigned long long s2 = __reduce_add_sync(kFull, lost);
@@ -682,7 +707,16 @@ void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const
     if (n <= 0) return;
     const MixedArgs a = make_args(p, n, m);
     cudaMemsetAsync(wq_n, 0, sizeof(unsigned int), s);
-    k_step32<<<grid_for(n, 256), 256, 0, s>>>(a, c, static_cast<WalkItem32 *>(wq), wq_n, ctr);
+    static int step32_blocks = 0;  // SMs x resident blocks of k_step32 (same on every device of this build)
+    if (!step32_blocks) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step32, 256, 0);
+        step32_blocks = std::max(1, sms * std::max(1, per_sm));
+    }
+    const unsigned grid = unsigned(std::min<int64_t>(grid_for(n, 256), step32_blocks));
+    k_step32<<<grid, 256, 0, s>>>(a, c, static_cast<WalkItem32 *>(wq), wq_n, ctr);
     k_walk_queue32<<<152 * 8, 128, 0, s>>>(a, c.max_cross, static_cast<WalkItem32 *>(wq), wq_n, tri_count, ctr,
                                             land, c.step, f);
 }
