@@ -111,6 +111,16 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of the step kernel and its walk kernel per alive
+# particle, workload 1 geometry, one ncu --set full capture at 4e6 particles (FP64: 229.1 + 151.4
+# MB for k_step64, 71.27 + 1.472 MB for k_walk_queue64; mixed: 128.2 + 40.67 MB for k_step32,
+# 53.52 + 1.419 MB for k_walk_queue32)
+STEP_TRAFFIC_B = {
+    "64": (453.2e6 / 4e6, "ncu capture of k_step64 + k_walk_queue64 at 4e6 particles, scaled by particles"),
+    "32": (223.8e6 / 4e6, "ncu capture of k_step32 + k_walk_queue32 at 4e6 particles, scaled by particles"),
+}
+
+
 def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -320,9 +330,15 @@ def run_gpu(args):
     dom = max(phases, key=lambda k: phases[k][1])
     name, dms, dbytes, dl = phases[dom]
     bw = dbytes / (dms / 1e3) / 1e9 if dms > 0 else None
+    traffic, traffic_src = args.traffic, "--traffic" if args.traffic else None
+    if traffic is None and dom == "step" and args.workload == 1:
+        # DRAM bytes (read + write) of the step kernel pair per alive particle from one ncu capture
+        # of the same geometry at 4e6 particles, scaled by the particles one launch processes
+        per_particle, src = STEP_TRAFFIC_B[sfx]
+        traffic, traffic_src = per_particle * ps / max(1, args.steps), src
     roof = {"kernel": name, "phase": dom, "bound": "hbm", "achieved": bw, "peak": peak, "unit": "GB/s",
-            "frac": (bw / peak) if bw else None, "traffic": args.traffic, "peak_source": peak_src,
-            "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl)}
+            "frac": (bw / peak) if bw else None, "traffic": traffic, "traffic_source": traffic_src,
+            "peak_source": peak_src, "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl)}
     for k, (nm, ms_k, b_k, l_k) in phases.items():
         roof[f"{k}_GBps"] = b_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
     breakdown = {k: prof[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")}
