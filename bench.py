@@ -143,6 +143,8 @@ def build_workload(args):
         w = workload1(n_particles=args.particles, cells=args.cells, seed=0, steps=args.warmup + args.steps)
     w.params["precision"] = 1 if args.precision == "mixed" else 0
     w.params["preconditioner"] = {"jacobi": 0, "amg": 1, "amg32": 2}[args.precond]
+    if args.resort_every is not None:
+        w.params["resort_every"] = args.resort_every
     return w
 
 
@@ -469,6 +471,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--precond", default="amg32", choices=["jacobi", "amg", "amg32"],
                     help="Poisson PCG preconditioner (both forms)")
+    ap.add_argument("--resort-every", type=int, default=None,
+                    help="steps between tet re-sorts of the particles (default: the workload's)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="particles in the CPU sample (0: all)")
     ap.add_argument("--cpu-steps", type=int, default=0, help="timed CPU steps (0: --steps)")
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient leg")
