@@ -184,8 +184,20 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
  * p += d / max|d_k| * displacement. Particle i draws from Philox4x32-10 keyed
  * by (seed) and counted by (i, block), so a source is reproducible and does
  * not depend on the launch shape. */
-typedef enum spg_source_shape { SPG_SRC_DISK = 0, SPG_SRC_RECT = 1 } spg_source_shape;
-typedef enum spg_source_directions { SPG_DIR_CONE = 0, SPG_DIR_COSINE = 1 } spg_source_directions;
+typedef enum spg_source_shape {
+    SPG_SRC_DISK = 0,
+    SPG_SRC_RECT = 1,
+    SPG_SRC_POINT = 2, /* every particle at centre (ParticleGenerator::fromPointSource) */
+    SPG_SRC_CELLS = 3  /* surface cells: count split evenly over the cells, the remainder one each to
+                          seed-chosen cells (ParticleGenerator::fromSurfaceSource) */
+} spg_source_shape;
+typedef enum spg_source_directions {
+    SPG_DIR_CONE = 0,
+    SPG_DIR_COSINE = 1,
+    SPG_DIR_FAN = 2 /* the reference's law: polar angle theta0 + U(-1,1) expansion at the fixed azimuth
+                       phi0 of the normal, theta0 = acos(n_z), phi0 = atan2(n_y, n_x)
+                       (ParticleDynamicUtils::calculateVelocityFromEnergy_eV) */
+} spg_source_directions;
 typedef enum spg_source_energy { SPG_ENERGY_MONO = 0, SPG_ENERGY_THOMPSON = 1 } spg_source_energy;
 typedef struct spg_source {
     int32_t shape;        /* spg_source_shape */
@@ -202,6 +214,12 @@ typedef struct spg_source {
     double emax_ev;       /* Thompson truncation [eV] */
     double displacement;  /* shift along the direction [m]; 0.05 mm in the reference */
     uint64_t seed;
+    /* SPG_SRC_CELLS: n_cells cells, cells[6 k .. 6 k + 5] = centre xyz [m], normal xyz (the
+     * baseCoordinates of a surface source); host memory, read during the call */
+    int32_t n_cells;
+    int32_t reserved1;
+    const double *cells;
+    double expansion;     /* SPG_DIR_FAN: polar-angle spread [rad] (expansionAngle) */
 } spg_source;
 void spg_default_source(spg_source *src);
 
@@ -220,6 +238,12 @@ int spg_get_tracks(spg_handle *h, int32_t *counts, double *xyz, double *last_xyz
  * spg_set_particles does (location, LOST flags, reset of step, counters and
  * potential); nothing crosses the host link. */
 int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src);
+/* Continuous injection (the per-step _spawnParticles of ModelingMainDriver.cpp:37-68 with
+ * sputtering on): samples n more particles from src on the device and appends them to the
+ * current set, after the existing ones, with ids np .. np + n - 1. Step, counters, potential,
+ * field and tracks are kept; the Philox counter of a particle is its id, so each injection
+ * draws new numbers from the same seed. */
+int spg_inject_particles(spg_handle *h, int64_t n, const spg_source *src);
 
 /* (a) P1 charge deposit of all alive particles; rho_out [n_nodes] C/m^3 (nullable). */
 int spg_gather(spg_handle *h, double *rho_out);

@@ -64,11 +64,13 @@ class Source(C.Structure):
         ("xlim", C.c_double * 2), ("ylim", C.c_double * 2), ("z", C.c_double),
         ("half_angle", C.c_double), ("energy_ev", C.c_double), ("binding_ev", C.c_double),
         ("emax_ev", C.c_double), ("displacement", C.c_double), ("seed", C.c_uint64),
+        ("n_cells", C.c_int32), ("reserved1", C.c_int32), ("cells", C.POINTER(C.c_double)),
+        ("expansion", C.c_double),
     ]
 
 
-SPG_SRC_DISK, SPG_SRC_RECT = 0, 1
-SPG_DIR_CONE, SPG_DIR_COSINE = 0, 1
+SPG_SRC_DISK, SPG_SRC_RECT, SPG_SRC_POINT, SPG_SRC_CELLS = 0, 1, 2, 3
+SPG_DIR_CONE, SPG_DIR_COSINE, SPG_DIR_FAN = 0, 1, 2
 SPG_ENERGY_MONO, SPG_ENERGY_THOMPSON = 0, 1
 
 
@@ -110,6 +112,7 @@ SIGNATURES = {
     "spg_set_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32]),
     "spg_default_source": (None, [C.POINTER(Source)]),
     "spg_generate_particles": (C.c_int, [_H, C.c_int64, C.POINTER(Source)]),
+    "spg_inject_particles": (C.c_int, [_H, C.c_int64, C.POINTER(Source)]),
     "spg_track_particles": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
     "spg_get_tracks": (C.c_int, [_H, _pi32, _pd, _pd, C.POINTER(C.c_uint32)]),
     "spg_get_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32, C.POINTER(C.c_uint32)]),

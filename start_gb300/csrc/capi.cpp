@@ -6,6 +6,7 @@
 // when due, then process; plus the periodic re-sort that has no reference
 // counterpart (it only changes memory order).
 #include <algorithm>
+#include <random>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -104,6 +105,7 @@ struct spg_handle {
     int32_t track_k = 0, track_cap = 0;
     int64_t *track_ids = nullptr;
     int32_t *track_of_id = nullptr, *track_slot = nullptr, *track_count = nullptr;
+    int64_t track_table_n = 0;  // ids the id -> track table covers (particles injected later are not tracked)
     double *track_xyz = nullptr, *track_cur = nullptr;
     uint32_t *track_flags = nullptr;
     bool amg = false, amg32 = false;
@@ -464,6 +466,63 @@ int alloc_particles(spg_handle *h, int64_t n) {
     }
     CK(dalloc(&h->walkq, n));
     h->cap = n;
+    return SPG_OK;
+}
+
+// Capacity for `need` particles keeping the current ones: new buffers (both
+// of the re-sort pair), the current set copied into buffer 0.
+int grow_particles(spg_handle *h, int64_t need) {
+    if (need <= h->cap) return SPG_OK;
+    const int64_t cap = std::max<int64_t>(need, h->cap + h->cap / 2);
+    const int64_t np = h->np;
+    cudaStream_t s = h->stream;
+    if (h->mixed) {
+        DevParticles32 N[2];
+        for (auto &Q : N) {
+            CK(dalloc(&Q.x, cap));
+            CK(dalloc(&Q.y, cap));
+            CK(dalloc(&Q.z, cap));
+            CK(dalloc(&Q.vx, cap));
+            CK(dalloc(&Q.vy, cap));
+            CK(dalloc(&Q.vz, cap));
+            CK(dalloc(&Q.tet, cap));
+            CK(dalloc(&Q.idf, cap));
+        }
+        const DevParticles32 &O = h->Q[h->cur];
+        void *dst[8] = {N[0].x, N[0].y, N[0].z, N[0].vx, N[0].vy, N[0].vz, N[0].tet, N[0].idf};
+        const void *src[8] = {O.x, O.y, O.z, O.vx, O.vy, O.vz, O.tet, O.idf};
+        for (int k = 0; k < 8; ++k)
+            if (np) CK(cudaMemcpyAsync(dst[k], src[k], 4 * size_t(np), cudaMemcpyDeviceToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        free_particles(h);
+        h->Q[0] = N[0];
+        h->Q[1] = N[1];
+    } else {
+        DevParticles N[2];
+        for (auto &P : N) {
+            CK(dalloc(&P.x, cap));
+            CK(dalloc(&P.y, cap));
+            CK(dalloc(&P.z, cap));
+            CK(dalloc(&P.vx, cap));
+            CK(dalloc(&P.vy, cap));
+            CK(dalloc(&P.vz, cap));
+            CK(dalloc(&P.tet, cap));
+            CK(dalloc(&P.idf, cap));
+        }
+        const DevParticles &O = h->P[h->cur];
+        void *dst[8] = {N[0].x, N[0].y, N[0].z, N[0].vx, N[0].vy, N[0].vz, N[0].tet, N[0].idf};
+        const void *src[8] = {O.x, O.y, O.z, O.vx, O.vy, O.vz, O.tet, O.idf};
+        const size_t w[8] = {8, 8, 8, 8, 8, 8, 4, 4};
+        for (int k = 0; k < 8; ++k)
+            if (np) CK(cudaMemcpyAsync(dst[k], src[k], w[k] * size_t(np), cudaMemcpyDeviceToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        free_particles(h);
+        h->P[0] = N[0];
+        h->P[1] = N[1];
+    }
+    CK(dalloc(&h->walkq, cap));
+    h->cap = cap;
+    h->cur = 0;
     return SPG_OK;
 }
 
@@ -896,7 +955,7 @@ int do_solve(spg_handle *h) {
 // the step, as the reference records it before the move).
 int record_tracks(spg_handle *h) {
     const uint32_t *idf = h->mixed ? h->Q[h->cur].idf : h->P[h->cur].idf;
-    launch_track_find(idf, h->np, h->track_of_id, h->track_slot, h->stream);
+    launch_track_find(idf, h->np, h->track_of_id, h->track_table_n, h->track_slot, h->stream);
     if (h->mixed)
         launch_track_record32(h->Q[h->cur], h->cen, h->track_slot, h->track_k, h->track_cap, h->track_count,
                               h->track_xyz, h->stream);
@@ -1332,19 +1391,24 @@ void spg_default_source(spg_source *src) {
     src->displacement = 0.05e-3;
 }
 
-int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
-    if (!h) return SPG_E_INVALID;
-    if (!src) return fail(h, SPG_E_INVALID, "generate_particles: null source");
-    if (n < 0 || n > kMaxParticles) return fail(h, SPG_E_INVALID, "generate_particles: n out of range");
-    if (src->shape != SPG_SRC_DISK && src->shape != SPG_SRC_RECT)
-        return fail(h, SPG_E_INVALID, "generate_particles: bad shape");
-    if (src->directions != SPG_DIR_CONE && src->directions != SPG_DIR_COSINE)
-        return fail(h, SPG_E_INVALID, "generate_particles: bad directions");
+// Validates src and samples n particles with ids id_base .. id_base + n - 1
+// into the device arrays pos, vel (3 n each); tet (n) receives their tets.
+int sample_particles(spg_handle *h, int64_t n, const spg_source *src, int64_t id_base, double *dpos, double *dvel,
+                     int32_t *dtet, const char *who) {
+    const std::string w(who);
+    if (!src) return fail(h, SPG_E_INVALID, w + ": null source");
+    if (src->shape < SPG_SRC_DISK || src->shape > SPG_SRC_CELLS) return fail(h, SPG_E_INVALID, w + ": bad shape");
+    if (src->directions < SPG_DIR_CONE || src->directions > SPG_DIR_FAN)
+        return fail(h, SPG_E_INVALID, w + ": bad directions");
     if (src->energy != SPG_ENERGY_MONO && src->energy != SPG_ENERGY_THOMPSON)
-        return fail(h, SPG_E_INVALID, "generate_particles: bad energy law");
+        return fail(h, SPG_E_INVALID, w + ": bad energy law");
     const double eV = 1.60217733000001e-19;  // Constants.hpp eV_J
     if (src->energy == SPG_ENERGY_MONO ? !(src->energy_ev > 0.0) : !(src->binding_ev > 0.0 && src->emax_ev > 0.0))
-        return fail(h, SPG_E_INVALID, "generate_particles: energies must be > 0");
+        return fail(h, SPG_E_INVALID, w + ": energies must be > 0");
+    if (src->shape == SPG_SRC_CELLS && (src->n_cells <= 0 || !src->cells))
+        return fail(h, SPG_E_INVALID, w + ": a cell source needs n_cells > 0 and cells");
+    if (src->directions == SPG_DIR_FAN && !(src->expansion >= 0.0))
+        return fail(h, SPG_E_INVALID, w + ": expansion must be >= 0");
     SourceConst c{};
     c.shape = src->shape;
     c.directions = src->directions;
@@ -1353,8 +1417,11 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
     double nv[3] = {src->normal[0], src->normal[1], src->normal[2]};
     if (src->shape == SPG_SRC_RECT) nv[0] = nv[1] = 0.0, nv[2] = 1.0;
     const double nn = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-    if (!(nn > 0.0)) return fail(h, SPG_E_INVALID, "generate_particles: zero normal");
-    for (double &x : nv) x /= nn;
+    if (src->shape != SPG_SRC_CELLS && !(nn > 0.0)) return fail(h, SPG_E_INVALID, w + ": zero normal");
+    if (nn > 0.0)
+        for (double &x : nv) x /= nn;
+    else
+        nv[0] = nv[1] = 0.0, nv[2] = 1.0;
     const double t[3] = {std::fabs(nv[0]) < 0.9 ? 1.0 : 0.0, std::fabs(nv[0]) < 0.9 ? 0.0 : 1.0, 0.0};
     double e1[3] = {nv[1] * t[2] - nv[2] * t[1], nv[2] * t[0] - nv[0] * t[2], nv[0] * t[1] - nv[1] * t[0]};
     const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
@@ -1366,6 +1433,9 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
         c.e2[k] = e2[k];
         c.nrm[k] = nv[k];
     }
+    c.theta0 = std::acos(std::max(-1.0, std::min(1.0, nv[2])));
+    c.phi0 = std::atan2(nv[1], nv[0]);
+    c.expansion = src->expansion;
     c.radius = src->radius;
     c.xlim[0] = src->xlim[0];
     c.xlim[1] = src->xlim[1];
@@ -1380,9 +1450,55 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
     c.displacement = src->displacement;
     c.seed_lo = uint32_t(src->seed);
     c.seed_hi = uint32_t(src->seed >> 32);
+    c.id_base = id_base;
+    cudaStream_t s = h->stream;
+    double *dcells = nullptr;
+    int64_t *dfirst = nullptr;
+    if (src->shape == SPG_SRC_CELLS) {
+        // per cell: centre and the polar / azimuthal angle of its normal; the
+        // count splits evenly and the remainder goes one each to cells chosen
+        // by a shuffle seeded from the source seed and the first id
+        const int k = src->n_cells;
+        std::vector<double> cells(5 * size_t(k));
+        for (int q = 0; q < k; ++q) {
+            const double *cc = src->cells + 6 * size_t(q);
+            const double m = std::sqrt(cc[3] * cc[3] + cc[4] * cc[4] + cc[5] * cc[5]);
+            if (!(m > 0.0)) return fail(h, SPG_E_INVALID, w + ": zero cell normal");
+            cells[5 * q] = cc[0];
+            cells[5 * q + 1] = cc[1];
+            cells[5 * q + 2] = cc[2];
+            cells[5 * q + 3] = std::acos(std::max(-1.0, std::min(1.0, cc[5] / m)));
+            cells[5 * q + 4] = std::atan2(cc[4] / m, cc[3] / m);
+        }
+        std::vector<int64_t> count(k, n / k);
+        std::vector<int> order(k);
+        for (int q = 0; q < k; ++q) order[q] = q;
+        std::mt19937_64 gen(src->seed ^ (uint64_t(id_base) * 0x9E3779B97F4A7C15ull));
+        std::shuffle(order.begin(), order.end(), gen);
+        for (int64_t q = 0; q < n % k; ++q) count[order[q]]++;
+        std::vector<int64_t> first(k + 1, 0);
+        for (int q = 0; q < k; ++q) first[q + 1] = first[q] + count[q];
+        CK(upload(&dcells, cells, s));
+        CK(upload(&dfirst, first, s));
+        c.n_cells = k;
+        c.cells = dcells;
+        c.cell_first = dfirst;
+    }
+    launch_generate(c, n, dpos, dvel, s);
+    launch_locate(dpos, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings, dtet, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    cudaFree(dcells);
+    cudaFree(dfirst);
+    return SPG_OK;
+}
+
+int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
+    if (!h) return SPG_E_INVALID;
+    if (n < 0 || n > kMaxParticles) return fail(h, SPG_E_INVALID, "generate_particles: n out of range");
     CK(cudaSetDevice(h->device));
     h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
-    free_tracks(h);  // a new particle set ends any tracking
+    free_tracks(h);   // a new particle set ends any tracking
     cudaStream_t s = h->stream;
     {
         const int rc = alloc_particles(h, n);
@@ -1401,8 +1517,15 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
         CK(dalloc(&dvel, 3 * n));
         CK(dalloc(&dtet, n));
         CK(dalloc(&dlost, 1));
-        launch_generate(c, n, dpos, dvel, s);
-        launch_locate(dpos, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings, dtet, s);
+        const int rc = sample_particles(h, n, src, 0, dpos, dvel, dtet, "generate_particles");
+        if (rc) {
+            cudaFree(dpos);
+            cudaFree(dvel);
+            cudaFree(dtet);
+            cudaFree(dlost);
+            h->np = h->n_active = 0;
+            return rc;
+        }
         CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
         launch_count_lost(dtet, n, dlost, s);
         if (h->mixed)
@@ -1424,6 +1547,60 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
     return reset_run_state(h);
 }
 
+int spg_inject_particles(spg_handle *h, int64_t n, const spg_source *src) {
+    if (!h) return SPG_E_INVALID;
+    if (!h->have_particles) return fail(h, SPG_E_STATE, "inject_particles: no particles set");
+    if (n < 0 || h->np + n > kMaxParticles) return fail(h, SPG_E_INVALID, "inject_particles: n out of range");
+    if (n == 0) return SPG_OK;
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    double *dpos = nullptr, *dvel = nullptr;
+    int32_t *dtet = nullptr;
+    unsigned long long *dlost = nullptr;
+    CK(dalloc(&dpos, 3 * n));
+    CK(dalloc(&dvel, 3 * n));
+    CK(dalloc(&dtet, n));
+    CK(dalloc(&dlost, 1));
+    auto release = [&]() {
+        cudaFree(dpos);
+        cudaFree(dvel);
+        cudaFree(dtet);
+        cudaFree(dlost);
+    };
+    int rc = sample_particles(h, n, src, h->np, dpos, dvel, dtet, "inject_particles");
+    if (!rc) rc = grow_particles(h, h->np + n);
+    if (rc) {
+        release();
+        return rc;
+    }
+    CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
+    launch_count_lost(dtet, n, dlost, s);
+    if (h->mixed)
+        launch_to_local(dpos, dvel, dtet, h->cen, n, h->Q[h->cur], s, h->np);
+    else
+        launch_init_particles(dpos, dvel, dtet, n, h->P[h->cur], s, h->np);
+    CK(cudaGetLastError());
+    unsigned long long lost = 0;
+    CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    release();
+    h->grad_ready = false;  // the recorded gradient forward no longer matches the particle set
+    // the new particles come after the active range; every slot up to np is processed
+    h->np += n;
+    h->n_active = h->np;
+    h->init_lost += int64_t(lost);
+    h->fix_bits = fix_bits_for(h->np);
+    // their tets get the current field (the lazy field computes occupied tets only)
+    const FieldArgs f = field_args(h);
+    if (h->mixed)
+        launch_refresh32(h->Q[h->cur], h->np, f, s);
+    else
+        launch_refresh64(h->P[h->cur], h->np, f, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return SPG_OK;
+}
+
 int spg_track_particles(spg_handle *h, int32_t k, const int64_t *ids, int32_t capacity) {
     if (!h) return SPG_E_INVALID;
     if (!h->have_particles) return fail(h, SPG_E_STATE, "track_particles: no particles set");
@@ -1436,6 +1613,7 @@ int spg_track_particles(spg_handle *h, int32_t k, const int64_t *ids, int32_t ca
     cudaStream_t s = h->stream;
     CK(dalloc(&h->track_ids, k));
     CK(dalloc(&h->track_of_id, std::max<int64_t>(h->np, 1)));
+    h->track_table_n = std::max<int64_t>(h->np, 1);
     CK(dalloc(&h->track_slot, k));
     CK(dalloc(&h->track_count, k));
     CK(dalloc(&h->track_xyz, 3 * int64_t(k) * capacity));
@@ -1460,7 +1638,7 @@ int spg_get_tracks(spg_handle *h, int32_t *counts, double *xyz, double *last_xyz
     cudaStream_t s = h->stream;
     const int k = h->track_k;
     const uint32_t *idf = h->mixed ? h->Q[h->cur].idf : h->P[h->cur].idf;
-    launch_track_find(idf, h->np, h->track_of_id, h->track_slot, s);
+    launch_track_find(idf, h->np, h->track_of_id, h->track_table_n, h->track_slot, s);
     if (h->mixed)
         launch_track_current32(h->Q[h->cur], h->cen, h->track_slot, k, h->track_cur, h->track_flags, s);
     else

@@ -474,19 +474,20 @@ __global__ void k_refresh32(DevParticles32 p, int64_t n, const __grid_constant__
 // Global FP64 state -> local FP32 state (and back).
 __global__ void k_to_local(const double *__restrict__ pos, const double *__restrict__ vel,
                            const int32_t *__restrict__ tet, const double *__restrict__ cen, int64_t n,
-                           DevParticles32 p) {
+                           DevParticles32 p, int64_t id_base) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const int64_t j = id_base + i;
     const int32_t t = tet[i];
     const int64_t tc = t < 0 ? 0 : t;
-    p.x[i] = float(pos[3 * i] - (t < 0 ? 0.0 : cen[3 * tc]));
-    p.y[i] = float(pos[3 * i + 1] - (t < 0 ? 0.0 : cen[3 * tc + 1]));
-    p.z[i] = float(pos[3 * i + 2] - (t < 0 ? 0.0 : cen[3 * tc + 2]));
-    p.vx[i] = float(vel[3 * i]);
-    p.vy[i] = float(vel[3 * i + 1]);
-    p.vz[i] = float(vel[3 * i + 2]);
-    p.tet[i] = t;
-    p.idf[i] = uint32_t(i) | (t < 0 ? kLost : 0u);
+    p.x[j] = float(pos[3 * i] - (t < 0 ? 0.0 : cen[3 * tc]));
+    p.y[j] = float(pos[3 * i + 1] - (t < 0 ? 0.0 : cen[3 * tc + 1]));
+    p.z[j] = float(pos[3 * i + 2] - (t < 0 ? 0.0 : cen[3 * tc + 2]));
+    p.vx[j] = float(vel[3 * i]);
+    p.vy[j] = float(vel[3 * i + 1]);
+    p.vz[j] = float(vel[3 * i + 2]);
+    p.tet[j] = t;
+    p.idf[j] = uint32_t(j) | (t < 0 ? kLost : 0u);
 }
 
 __global__ void k_gather32(DevParticles32 p, int64_t n, const double *__restrict__ cen, double *pos, double *vel,
@@ -764,9 +765,9 @@ void launch_refresh32(const DevParticles32 &p, int64_t n, const FieldArgs &f, cu
 }
 
 void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
-                     DevParticles32 p, cudaStream_t s) {
+                     DevParticles32 p, cudaStream_t s, int64_t id_base) {
     if (n <= 0) return;
-    k_to_local<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, cen, n, p);
+    k_to_local<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, cen, n, p, id_base);
 }
 
 void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,

@@ -622,18 +622,19 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t n, MeshDev m, c
 }
 
 __global__ void k_init_particles(const double *__restrict__ pos, const double *__restrict__ vel,
-                                 const int32_t *__restrict__ tet, int64_t n, DevParticles p) {
+                                 const int32_t *__restrict__ tet, int64_t n, DevParticles p, int64_t id_base) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    p.x[i] = pos[3 * i];
-    p.y[i] = pos[3 * i + 1];
-    p.z[i] = pos[3 * i + 2];
-    p.vx[i] = vel[3 * i];
-    p.vy[i] = vel[3 * i + 1];
-    p.vz[i] = vel[3 * i + 2];
+    const int64_t j = id_base + i;
+    p.x[j] = pos[3 * i];
+    p.y[j] = pos[3 * i + 1];
+    p.z[j] = pos[3 * i + 2];
+    p.vx[j] = vel[3 * i];
+    p.vy[j] = vel[3 * i + 1];
+    p.vz[j] = vel[3 * i + 2];
     const int32_t t = tet[i];
-    p.tet[i] = t;
-    p.idf[i] = uint32_t(i) | (t < 0 ? kLost : 0u);
+    p.tet[j] = t;
+    p.idf[j] = uint32_t(j) | (t < 0 ? kLost : 0u);
 }
 
 __global__ void k_gather_by_id(DevParticles p, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags) {
@@ -844,9 +845,9 @@ void launch_locate(const double *pos, int64_t n, const MeshDev &m, const int32_t
 }
 
 void launch_init_particles(const double *pos, const double *vel, const int32_t *tet, int64_t n, DevParticles p,
-                           cudaStream_t s) {
+                           cudaStream_t s, int64_t id_base) {
     if (n <= 0) return;
-    k_init_particles<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, n, p);
+    k_init_particles<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, n, p, id_base);
 }
 
 void launch_gather_by_id(const DevParticles &p, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags,

@@ -17,10 +17,12 @@ __global__ void k_track_map(const int64_t *__restrict__ ids, int k, int32_t *__r
 }
 
 __global__ void k_track_find(const uint32_t *__restrict__ idf, int64_t n, const int32_t *__restrict__ track_of_id,
-                             int32_t *__restrict__ slot) {
+                             int64_t table_n, int32_t *__restrict__ slot) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int32_t t = track_of_id[idf[i] & kIdMask];
+    const uint32_t id = idf[i] & kIdMask;
+    if (int64_t(id) >= table_n) return;  // injected after the tracking began
+    const int32_t t = track_of_id[id];
     if (t >= 0) slot[t] = int32_t(i);
 }
 
@@ -98,8 +100,9 @@ void launch_track_map(const int64_t *ids, int k, int32_t *track_of_id, cudaStrea
     if (k > 0) k_track_map<<<(k + 127) / 128, 128, 0, s>>>(ids, k, track_of_id);
 }
 
-void launch_track_find(const uint32_t *idf, int64_t n, const int32_t *track_of_id, int32_t *slot, cudaStream_t s) {
-    if (n > 0) k_track_find<<<unsigned((n + 255) / 256), 256, 0, s>>>(idf, n, track_of_id, slot);
+void launch_track_find(const uint32_t *idf, int64_t n, const int32_t *track_of_id, int64_t table_n, int32_t *slot,
+                       cudaStream_t s) {
+    if (n > 0) k_track_find<<<unsigned((n + 255) / 256), 256, 0, s>>>(idf, n, track_of_id, table_n, slot);
 }
 
 void launch_track_record64(const DevParticles &p, const int32_t *slot, int k, int cap, int32_t *count, double *xyz,

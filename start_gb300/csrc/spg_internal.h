@@ -213,8 +213,9 @@ void launch_locate(const double *pos, int64_t n, const MeshDev &m, const int32_t
 // E = 0 and H = 0 in every tet, stamped with f.epoch (both forms' records).
 void launch_zero_field(const FieldArgs &f, int64_t n_tets, cudaStream_t s);
 void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, cudaStream_t s);
+// Installs n particles at slots [id_base, id_base + n) with ids id_base + i.
 void launch_init_particles(const double *pos, const double *vel, const int32_t *tet, int64_t n,
-                           DevParticles p, cudaStream_t s);
+                           DevParticles p, cudaStream_t s, int64_t id_base = 0);
 void launch_gather_by_id(const DevParticles &p, int64_t n, double *pos, double *vel, int32_t *tet,
                          uint32_t *flags, cudaStream_t s);
 // Re-sort: histogram, exclusive scan, scatter. Writes the number of alive
@@ -299,7 +300,7 @@ void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, c
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
                       const OccList &occ, cudaStream_t s);
 void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
-                     DevParticles32 p, cudaStream_t s);
+                     DevParticles32 p, cudaStream_t s, int64_t id_base = 0);
 void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,
                      uint32_t *flags, cudaStream_t s);
 void launch_resort32(const DevParticles32 &src, DevParticles32 dst, int64_t n, int64_t n_tets, int32_t *scratch,
@@ -372,13 +373,23 @@ struct SourceConst {
     double binding_j, s_max, mass;  // Thompson: U [J], Emax/(Emax+U); particle mass
     double displacement;
     uint32_t seed_lo, seed_hi;
+    int64_t id_base;       // Philox counter of particle i is id_base + i (its particle id)
+    double theta0, phi0;   // SPG_DIR_FAN: polar and azimuthal angle of the normal
+    double expansion;      // SPG_DIR_FAN: polar spread
+    // SPG_SRC_CELLS: per cell centre xyz, theta0, phi0 (5 doubles), and the
+    // first particle index of each cell (n_cells + 1 prefix offsets)
+    int32_t n_cells;
+    const double *cells;
+    const int64_t *cell_first;
 };
 void launch_generate(const SourceConst &c, int64_t n, double *pos, double *vel, cudaStream_t s);
 
 // ---------------------------------------------------------------- tracks
 // Trajectory sampling of a fixed set of particle ids (kernels_track.cu).
 void launch_track_map(const int64_t *ids, int k, int32_t *track_of_id, cudaStream_t s);
-void launch_track_find(const uint32_t *idf, int64_t n, const int32_t *track_of_id, int32_t *slot, cudaStream_t s);
+// track_of_id holds table_n ids; particles with larger ids (injected later) are not tracked.
+void launch_track_find(const uint32_t *idf, int64_t n, const int32_t *track_of_id, int64_t table_n, int32_t *slot,
+                       cudaStream_t s);
 void launch_track_record64(const DevParticles &p, const int32_t *slot, int k, int cap, int32_t *count, double *xyz,
                            cudaStream_t s);
 void launch_track_record32(const DevParticles32 &p, const double *cen, const int32_t *slot, int k, int cap,

@@ -136,17 +136,15 @@ class StartPIC:
                                                N.as_ptr(vel, C.c_double), tp))
         self.n_particles = len(pos)
 
-    def generate_particles(self, n, *, shape="disk", directions="cone", energy="mono", centre=(0.0, 0.0, 0.0),
-                           normal=(0.0, 0.0, 1.0), radius=0.02, xlim=(0.0, 0.0), ylim=(0.0, 0.0), z=0.0,
-                           half_angle=None, energy_ev=1.0, binding_ev=4.9, emax_ev=50.0, displacement=0.05e-3,
-                           seed=0):
-        """Samples n particles on the device (spg_generate_particles): disk or
-        rectangle points, cone or cosine directions, monoenergetic or
-        Thompson energies, and the reference's 0.05 mm displacement."""
+    def _source(self, shape="disk", directions="cone", energy="mono", centre=(0.0, 0.0, 0.0),
+                normal=(0.0, 0.0, 1.0), radius=0.02, xlim=(0.0, 0.0), ylim=(0.0, 0.0), z=0.0, half_angle=None,
+                energy_ev=1.0, binding_ev=4.9, emax_ev=50.0, displacement=0.05e-3, seed=0, cells=None,
+                expansion=0.0):
         src = N.Source()
         self.lib.spg_default_source(C.byref(src))
-        src.shape = {"disk": N.SPG_SRC_DISK, "rect": N.SPG_SRC_RECT, "plate": N.SPG_SRC_RECT}[shape]
-        src.directions = {"cone": N.SPG_DIR_CONE, "cosine": N.SPG_DIR_COSINE}[directions]
+        src.shape = {"disk": N.SPG_SRC_DISK, "rect": N.SPG_SRC_RECT, "plate": N.SPG_SRC_RECT,
+                     "point": N.SPG_SRC_POINT, "cells": N.SPG_SRC_CELLS, "surface": N.SPG_SRC_CELLS}[shape]
+        src.directions = {"cone": N.SPG_DIR_CONE, "cosine": N.SPG_DIR_COSINE, "fan": N.SPG_DIR_FAN}[directions]
         src.energy = {"mono": N.SPG_ENERGY_MONO, "thompson": N.SPG_ENERGY_THOMPSON}[energy]
         src.centre[:] = [float(v) for v in centre]
         src.normal[:] = [float(v) for v in normal]
@@ -159,8 +157,32 @@ class StartPIC:
         src.energy_ev, src.binding_ev, src.emax_ev = energy_ev, binding_ev, emax_ev
         src.displacement = displacement
         src.seed = int(seed)
+        src.expansion = float(expansion)
+        keep = None
+        if cells is not None:
+            keep = np.ascontiguousarray(cells, np.float64).reshape(-1, 6)
+            src.n_cells = len(keep)
+            src.cells = N.as_ptr(keep, C.c_double)
+        return src, keep
+
+    def generate_particles(self, n, **kw):
+        """Samples n particles on the device (spg_generate_particles): disk,
+        rectangle, point or surface-cell sources (cells: rows of centre xyz and
+        normal xyz), cone, cosine or the reference's fan directions
+        (expansion), monoenergetic or Thompson energies, and the reference's
+        0.05 mm displacement."""
+        src, keep = self._source(**kw)
         self._check(self.lib.spg_generate_particles(self.h, int(n), C.byref(src)))
+        del keep
         self.n_particles = int(n)
+
+    def inject_particles(self, n, **kw):
+        """Appends n device-sampled particles (the same source options) to the
+        current set mid-run, with the next ids (spg_inject_particles)."""
+        src, keep = self._source(**kw)
+        self._check(self.lib.spg_inject_particles(self.h, int(n), C.byref(src)))
+        del keep
+        self.n_particles += int(n)
 
     def track(self, ids, capacity=10000):
         """Samples the positions of particles `ids` before every step they are
