@@ -113,6 +113,7 @@ SIGNATURES = {
     "spg_default_source": (None, [C.POINTER(Source)]),
     "spg_generate_particles": (C.c_int, [_H, C.c_int64, C.POINTER(Source)]),
     "spg_inject_particles": (C.c_int, [_H, C.c_int64, C.POINTER(Source)]),
+    "spg_get_matrix": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "spg_track_particles": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
     "spg_get_tracks": (C.c_int, [_H, _pi32, _pd, _pd, C.POINTER(C.c_uint32)]),
     "spg_get_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32, C.POINTER(C.c_uint32)]),

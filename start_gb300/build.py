@@ -47,6 +47,7 @@ def _sources():
         ("kernels_amg.cu", common_nv),
         ("kernels_sources.cu", common_nv),
         ("kernels_track.cu", common_nv),
+        ("kernels_fem.cu", common_nv + ["--fmad=false"]),
         ("mesh_prep.cpp", common_cc + ["-fopenmp"]),
         ("amg_setup.cpp", common_cc + ["-O3", "-fopenmp"]),
         ("capi.cpp", common_cc),

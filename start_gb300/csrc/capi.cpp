@@ -1121,6 +1121,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         os << "spg_create: built for sm_103a (GB300); device is sm_" << prop.major << prop.minor;
         return fail(h, SPG_E_NO_DEVICE, os.str());
     }
+    if (cudaSetDevice(params->device) != cudaSuccess) return fail(h, SPG_E_NO_DEVICE, "spg_create: cudaSetDevice");
     HostMesh hm;
     std::string err;
     int rc = prepare_mesh(*mesh, params->bbox_expansion, hm, err);
@@ -1840,6 +1841,23 @@ int spg_get_efield(spg_handle *h, double *E) {
     }
     CK(cudaMemcpyAsync(E, h->efield, sizeof(double) * 3 * h->n_tets, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
+}
+
+int spg_get_matrix(spg_handle *h, int32_t *row_ptr, int32_t *col, double *val, double *lift, double *dual_vol) {
+    if (!h) return SPG_E_INVALID;
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const int64_t n = h->n_nodes;
+    int32_t nnz = 0;
+    CK(cudaMemcpyAsync(&nnz, h->row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (row_ptr) CK(cudaMemcpyAsync(row_ptr, h->row_ptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+    if (col) CK(cudaMemcpyAsync(col, h->col, sizeof(int32_t) * size_t(nnz), cudaMemcpyDeviceToHost, s));
+    if (val) CK(cudaMemcpyAsync(val, h->val, sizeof(double) * size_t(nnz), cudaMemcpyDeviceToHost, s));
+    if (lift) CK(cudaMemcpyAsync(lift, h->lift, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (dual_vol) CK(cudaMemcpyAsync(dual_vol, h->dual_vol, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     return SPG_OK;
 }
 

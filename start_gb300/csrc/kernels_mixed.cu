@@ -347,8 +347,11 @@ __device__ __forceinline__ void field_of_tet32(const FieldArgs &f, int64_t t) {
     const double d1 = f1 - f0, d2 = f2 - f0, d3 = f3 - f0;
     const TetRec &r = f.rec[t];
     double E[3];
+    // Explicitly rounded products and sums: this file is built with FMA
+    // contraction on, and E is the FP64 field the oracle computes unfused.
 #pragma unroll
-    for (int k = 0; k < 3; ++k) E[k] = -((d1 * r.M[k] + d2 * r.M[3 + k]) + d3 * r.M[6 + k]);
+    for (int k = 0; k < 3; ++k)
+        E[k] = -__dadd_rn(__dadd_rn(__dmul_rn(d1, r.M[k]), __dmul_rn(d2, r.M[3 + k])), __dmul_rn(d3, r.M[6 + k]));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         f.efield[3 * t + k] = E[k];

@@ -13,9 +13,12 @@
 // barycentric gradients, which is what one-point cubature of constant
 // gradients integrates exactly. Dirichlet rows become identity rows and the
 // Dirichlet columns move to the right-hand side, which keeps K symmetric
-// positive definite for CG (the reference only replaces rows).
+// positive definite for CG (the reference only replaces rows). The element
+// maps and volumes, the node -> tet incidence and the stiffness assembly run
+// on the GPU (kernels_fem.cu); the face matching, the surface triangles, the
+// bounding box and the point-location grid stay here.
 //
-// Compiled with -ffp-contract=off: the barycentric map computed here feeds the
+// Compiled with -ffp-contract=off, like the oracle: the geometry feeds the
 // FP64 walk, which must agree bit for bit with the CPU oracle.
 #include <algorithm>
 #include <array>
@@ -50,28 +53,6 @@ inline void sort3(int32_t v[3]) {
 
 }  // namespace
 
-// Barycentric map of one tet: rows of J^{-1} where J = [x1-x0, x2-x0, x3-x0].
-// Row 0 = (b x c)/det, row 1 = (c x a)/det, row 2 = (a x b)/det.
-// The CPU oracle evaluates the same expressions in the same order.
-static double tet_map(const double *x0, const double *x1, const double *x2, const double *x3, double M[9]) {
-    const double a0 = x1[0] - x0[0], a1 = x1[1] - x0[1], a2 = x1[2] - x0[2];
-    const double b0 = x2[0] - x0[0], b1 = x2[1] - x0[1], b2 = x2[2] - x0[2];
-    const double c0 = x3[0] - x0[0], c1 = x3[1] - x0[1], c2 = x3[2] - x0[2];
-    const double bc0 = b1 * c2 - b2 * c1, bc1 = b2 * c0 - b0 * c2, bc2 = b0 * c1 - b1 * c0;
-    const double det = a0 * bc0 + a1 * bc1 + a2 * bc2;
-    if (det == 0.0) return 0.0;
-    M[0] = bc0 / det;
-    M[1] = bc1 / det;
-    M[2] = bc2 / det;
-    M[3] = (c1 * a2 - c2 * a1) / det;
-    M[4] = (c2 * a0 - c0 * a2) / det;
-    M[5] = (c0 * a1 - c1 * a0) / det;
-    M[6] = (a1 * b2 - a2 * b1) / det;
-    M[7] = (a2 * b0 - a0 * b2) / det;
-    M[8] = (a0 * b1 - a1 * b0) / det;
-    return det;
-}
-
 int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std::string &err) {
     std::ostringstream es;
     if (d.n_nodes <= 0 || d.n_tets <= 0 || !d.node_xyz || !d.tet_nodes) {
@@ -96,37 +77,22 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
     m.rec.assign(Nt, TetRec{});
     m.vol.assign(Nt, 0.0);
 
-    // 1. Orientation, barycentric maps, volumes.
-    int bad = -1;
-    for (int64_t t = 0; t < Nt; ++t) {
-        int32_t *tn = &m.tet_nodes[4 * t];
-        for (int k = 0; k < 4; ++k)
-            if (tn[k] < 0 || tn[k] >= Nn) bad = int(t);
-        if (bad >= 0) break;
-        const double *p[4];
-        for (int k = 0; k < 4; ++k) p[k] = &m.node_xyz[3 * int64_t(tn[k])];
-        double M[9];
-        double det = tet_map(p[0], p[1], p[2], p[3], M);
-        if (det < 0.0) {
-            std::swap(tn[2], tn[3]);
-            std::swap(p[2], p[3]);
-            det = tet_map(p[0], p[1], p[2], p[3], M);
+    // 1. Orientation, barycentric maps, volumes (on the GPU, kernels_fem.cu).
+    for (int64_t k = 0; k < 4 * Nt; ++k)
+        if (m.tet_nodes[k] < 0 || m.tet_nodes[k] >= Nn) {
+            es << "mesh: tet " << k / 4 << " has a bad node index or zero volume";
+            err = es.str();
+            return SPG_E_BAD_MESH;
         }
-        if (!(det > 0.0)) {
-            bad = int(t);
-            break;
+    {
+        int64_t bad = -1;
+        const int rc = fem_elements_gpu(m, err, bad);
+        if (rc) return rc;
+        if (bad >= 0) {
+            es << "mesh: tet " << bad << " has a bad node index or zero volume";
+            err = es.str();
+            return SPG_E_BAD_MESH;
         }
-        TetRec &r = m.rec[t];
-        std::memcpy(r.M, M, sizeof(M));
-        r.x0[0] = p[0][0];
-        r.x0[1] = p[0][1];
-        r.x0[2] = p[0][2];
-        m.vol[t] = det / 6.0;
-    }
-    if (bad >= 0) {
-        es << "mesh: tet " << bad << " has a bad node index or zero volume";
-        err = es.str();
-        return SPG_E_BAD_MESH;
     }
 
     // 2. Face matching: bucket faces by their smallest node id.
@@ -206,22 +172,6 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
     faces.clear();
     faces.shrink_to_fit();
 
-    // 4. Node -> tet incidence, dual volumes.
-    std::vector<int64_t> nstart(Nn + 1, 0);
-    for (int64_t i = 0; i < 4 * Nt; ++i) nstart[m.tet_nodes[i] + 1]++;
-    for (int64_t i = 0; i < Nn; ++i) nstart[i + 1] += nstart[i];
-    std::vector<int32_t> ntet(4 * Nt);  // tet*4 + local vertex
-    {
-        std::vector<int64_t> cur(nstart.begin(), nstart.end() - 1);
-        for (int64_t i = 0; i < 4 * Nt; ++i) ntet[cur[m.tet_nodes[i]]++] = int32_t(i);
-    }
-    m.dual_vol.assign(Nn, 0.0);
-    for (int64_t n = 0; n < Nn; ++n) {
-        double s = 0.0;
-        for (int64_t k = nstart[n]; k < nstart[n + 1]; ++k) s += m.vol[ntet[k] >> 2];
-        m.dual_vol[n] = 0.25 * s;
-    }
-
     // 5. Dirichlet nodes.
     m.is_dir.assign(Nn, 0);
     m.dir_value.assign(Nn, 0.0);
@@ -238,108 +188,12 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
         m.dir_value[n] = d.dirichlet_values[k];
     }
 
-    // 6. CSR stiffness. Row i holds the nodes of its incident tets, sorted.
-    m.row_ptr.assign(Nn + 1, 0);
-    std::vector<int32_t> rowlen(Nn, 0);
-#pragma omp parallel for schedule(dynamic, 1024)
-    for (int64_t i = 0; i < Nn; ++i) {
-        if (m.is_dir[i]) {
-            rowlen[i] = 1;
-            continue;
-        }
-        std::vector<int32_t> cols;
-        cols.reserve(32);
-        for (int64_t k = nstart[i]; k < nstart[i + 1]; ++k) {
-            const int32_t *tn = &m.tet_nodes[4 * int64_t(ntet[k] >> 2)];
-            for (int v = 0; v < 4; ++v)
-                if (!m.is_dir[tn[v]]) cols.push_back(tn[v]);
-        }
-        std::sort(cols.begin(), cols.end());
-        rowlen[i] = int32_t(std::unique(cols.begin(), cols.end()) - cols.begin());
-    }
-    for (int64_t i = 0; i < Nn; ++i) m.row_ptr[i + 1] = m.row_ptr[i] + rowlen[i];
-    const int64_t nnz = m.row_ptr[Nn];
-    if (nnz >= (int64_t(1) << 31)) {
-        err = "mesh: stiffness has more than 2^31 non-zeros";
-        return SPG_E_INVALID;
-    }
-    m.col.assign(nnz, 0);
-    m.val.assign(nnz, 0.0);
-    m.diag.assign(Nn, 1.0);
-    m.lift.assign(Nn, 0.0);
-    std::vector<std::vector<std::pair<int32_t, double>>> elim(Nn);  // free row -> (Dirichlet col, K)
-#pragma omp parallel for schedule(dynamic, 1024)
-    for (int64_t i = 0; i < Nn; ++i) {
-        int32_t *c0 = &m.col[m.row_ptr[i]];
-        double *v0 = &m.val[m.row_ptr[i]];
-        const int32_t len = rowlen[i];
-        if (m.is_dir[i]) {
-            c0[0] = int32_t(i);
-            v0[0] = 1.0;
-            m.diag[i] = 1.0;
-            continue;
-        }
-        {
-            std::vector<int32_t> cols;
-            cols.reserve(32);
-            for (int64_t k = nstart[i]; k < nstart[i + 1]; ++k) {
-                const int32_t *tn = &m.tet_nodes[4 * int64_t(ntet[k] >> 2)];
-                for (int v = 0; v < 4; ++v)
-                    if (!m.is_dir[tn[v]]) cols.push_back(tn[v]);
-            }
-            std::sort(cols.begin(), cols.end());
-            cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-            std::copy(cols.begin(), cols.end(), c0);
-        }
-        double lift = 0.0;
-        for (int64_t k = nstart[i]; k < nstart[i + 1]; ++k) {
-            const int64_t t = ntet[k] >> 2;
-            const int a = ntet[k] & 3;
-            const TetRec &r = m.rec[t];
-            double G[4][3];
-            for (int c = 0; c < 3; ++c) {
-                G[1][c] = r.M[c];
-                G[2][c] = r.M[3 + c];
-                G[3][c] = r.M[6 + c];
-                G[0][c] = -(G[1][c] + G[2][c] + G[3][c]);
-            }
-            const int32_t *tn = &m.tet_nodes[4 * t];
-            for (int b = 0; b < 4; ++b) {
-                const double kab = m.vol[t] * (G[a][0] * G[b][0] + G[a][1] * G[b][1] + G[a][2] * G[b][2]);
-                const int32_t j = tn[b];
-                if (m.is_dir[j]) {
-                    lift += kab * m.dir_value[j];
-                    auto &e = elim[i];
-                    auto it = std::find_if(e.begin(), e.end(), [j](const std::pair<int32_t, double> &x) {
-                        return x.first == j;
-                    });
-                    if (it == e.end())
-                        e.emplace_back(j, kab);
-                    else
-                        it->second += kab;
-                } else {
-                    const int32_t *pos = std::lower_bound(c0, c0 + len, j);
-                    v0[pos - c0] += kab;
-                }
-            }
-        }
-        m.lift[i] = lift;
-        for (int32_t k = 0; k < len; ++k)
-            if (c0[k] == i) m.diag[i] = v0[k];
-    }
-
-    // Eliminated couplings K_fd (free row f, Dirichlet column d): the lifting
-    // vector for new Dirichlet values and the adjoint of the lifting.
-    m.elim_row.clear();
-    m.elim_col.clear();
-    m.elim_val.clear();
-    for (int64_t i = 0; i < Nn; ++i) {
-        std::sort(elim[i].begin(), elim[i].end());
-        for (const auto &e : elim[i]) {
-            m.elim_row.push_back(int32_t(i));
-            m.elim_col.push_back(e.first);
-            m.elim_val.push_back(e.second);
-        }
+    // 4. Node -> tet incidence and dual volumes; CSR stiffness with the
+    //    Dirichlet rows as identity rows, the lifting and the eliminated
+    //    couplings (on the GPU, kernels_fem.cu).
+    {
+        const int rc = fem_stiffness_gpu(m, err);
+        if (rc) return rc;
     }
 
     // 7. Expanded global bounding box of the surface triangles

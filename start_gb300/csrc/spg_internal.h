@@ -82,6 +82,11 @@ void set_thread_error(const std::string &msg);
 
 // Returns SPG_OK or SPG_E_BAD_MESH / SPG_E_INVALID with a message in err.
 int prepare_mesh(const spg_mesh_desc &desc, double bbox_expansion, HostMesh &out, std::string &err);
+// FEM set-up on the current device (kernels_fem.cu): element maps, volumes
+// and orientation (bad_tet: lowest bad tet or -1); incidence, dual volumes
+// and the CSR stiffness with its Dirichlet elimination.
+int fem_elements_gpu(HostMesh &m, std::string &err, int64_t &bad_tet);
+int fem_stiffness_gpu(HostMesh &m, std::string &err);
 
 // ---------------------------------------------------------------- device side
 

@@ -281,6 +281,19 @@ class StartPIC:
         phi = np.ascontiguousarray(phi, np.float64)
         self._check(self.lib.spg_set_potential(self.h, N.as_ptr(phi, C.c_double)))
 
+    def matrix(self):
+        """The assembled FEM system: CSR (row_ptr, col, val), the lifting and
+        the dual volumes (spg_get_matrix)."""
+        rp = np.empty(self.n_nodes + 1, np.int32)
+        self._check(self.lib.spg_get_matrix(self.h, rp.ctypes.data, None, None, None, None))
+        col = np.empty(int(rp[-1]), np.int32)
+        val = np.empty(int(rp[-1]))
+        lift = np.empty(self.n_nodes)
+        dual = np.empty(self.n_nodes)
+        self._check(self.lib.spg_get_matrix(self.h, rp.ctypes.data, col.ctypes.data, val.ctypes.data,
+                                            lift.ctypes.data, dual.ctypes.data))
+        return rp, col, val, lift, dual
+
     def efield(self):
         E = np.empty((self.n_tets, 3))
         self._check(self.lib.spg_get_efield(self.h, N.as_ptr(E, C.c_double)))
