@@ -268,7 +268,7 @@ int spg_set_potential(spg_handle *h, const double *phi);
 int spg_get_efield(spg_handle *h, double *E /* [3*n_tets] */);
 /* The assembled FEM system (the counterpart of GSMAssembler's global matrix after
  * MatrixBoundaryConditionsManager): CSR stiffness with Dirichlet rows as identity rows,
- * row_ptr [n_nodes + 1], col and val [nnz] (spg_mesh_info), the lifting of the current
+ * row_ptr [n_nodes + 1], col and val [nnz] (info[4] of spg_mesh_info), the lifting of the current
  * Dirichlet values [n_nodes] and the dual volumes [n_nodes]. Any output may be NULL. */
 int spg_get_matrix(spg_handle *h, int32_t *row_ptr, int32_t *col, double *val, double *lift, double *dual_vol);
 /* Point location through the same walk as spg_set_particles. */
