@@ -138,6 +138,11 @@ struct spg_handle {
     unsigned int *walkq_n = nullptr;
     int64_t *n_alive_dev = nullptr;
     int32_t *sort_scratch = nullptr;
+    // Staging for particles that cross the host boundary or come from a
+    // source (set/get/generate/inject): 56 B per particle + 16, kept between
+    // calls so that a copy or an injection allocates nothing once grown.
+    unsigned char *io = nullptr;
+    size_t io_bytes = 0;
     int64_t occupied = 0;
     bool have_particles = false;
     bool charge_valid = false;
@@ -211,6 +216,32 @@ cudaError_t upload(T **ptr, const std::vector<T> &v, cudaStream_t s) {
     e = cudaMemcpyAsync(*ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(s);
+}
+
+// Staging of n particles: pos [3n], vel [3n] doubles, tet [n], flags [n]
+// 32-bit words and one 64-bit counter.
+struct IoStage {
+    double *pos, *vel;
+    int32_t *tet;
+    uint32_t *flags;
+    unsigned long long *counter;
+};
+
+int io_stage(spg_handle *h, int64_t n, IoStage &st) {
+    const size_t need = 56 * size_t(n) + 16;
+    if (need > h->io_bytes) {
+        cudaFree(h->io);
+        h->io = nullptr;
+        h->io_bytes = 0;
+        CK(cudaMalloc(reinterpret_cast<void **>(&h->io), need));
+        h->io_bytes = need;
+    }
+    st.counter = reinterpret_cast<unsigned long long *>(h->io);
+    st.pos = reinterpret_cast<double *>(h->io + 16);
+    st.vel = st.pos + 3 * n;
+    st.tet = reinterpret_cast<int32_t *>(st.vel + 3 * n);
+    st.flags = reinterpret_cast<uint32_t *>(st.tet + n);
+    return SPG_OK;
 }
 
 void free_particles(spg_handle *h) {
@@ -1289,7 +1320,8 @@ int spg_destroy(spg_handle *h) {
                     h->elim_rp,  h->elim_row, h->elim_col, h->elim_val, h->land, h->gr, h->adj_x, h->adj_v,
                     h->gE,       h->lam,      h->mu,       h->dJdg,    h->sums, h->hist.tet, h->hist.vx,
                     h->hist.vy,  h->hist.vz,  h->tri_scratch, h->ctr_scratch,
-                    h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch, h->walkq_n};
+                    h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch, h->walkq_n,
+                    h->io};
     for (void *ptr : ptrs) cudaFree(ptr);
     for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
     for (void *ptr : h->amg_alloc) cudaFree(ptr);
@@ -1338,13 +1370,14 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
     h->init_lost = 0;
     h->occupied = 0;
     if (n > 0) {
-        double *dpos = nullptr, *dvel = nullptr;
-        int32_t *dtet = nullptr;
-        unsigned long long *dlost = nullptr;
-        CK(dalloc(&dpos, 3 * n));
-        CK(dalloc(&dvel, 3 * n));
-        CK(dalloc(&dtet, n));
-        CK(dalloc(&dlost, 1));
+        IoStage st;
+        {
+            const int rc = io_stage(h, n, st);
+            if (rc) return rc;
+        }
+        double *dpos = st.pos, *dvel = st.vel;
+        int32_t *dtet = st.tet;
+        unsigned long long *dlost = st.counter;
         CK(cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(dvel, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
         if (tet_or_null) {
@@ -1367,10 +1400,6 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
         CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         h->init_lost = int64_t(lost);
-        cudaFree(dpos);
-        cudaFree(dvel);
-        cudaFree(dtet);
-        cudaFree(dlost);
     }
     h->have_particles = true;
     h->fix_bits = fix_bits_for(n);
@@ -1511,22 +1540,16 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
     h->init_lost = 0;
     h->occupied = 0;
     if (n > 0) {
-        double *dpos = nullptr, *dvel = nullptr;
-        int32_t *dtet = nullptr;
-        unsigned long long *dlost = nullptr;
-        CK(dalloc(&dpos, 3 * n));
-        CK(dalloc(&dvel, 3 * n));
-        CK(dalloc(&dtet, n));
-        CK(dalloc(&dlost, 1));
-        const int rc = sample_particles(h, n, src, 0, dpos, dvel, dtet, "generate_particles");
+        IoStage st;
+        int rc = io_stage(h, n, st);
+        if (!rc) rc = sample_particles(h, n, src, 0, st.pos, st.vel, st.tet, "generate_particles");
         if (rc) {
-            cudaFree(dpos);
-            cudaFree(dvel);
-            cudaFree(dtet);
-            cudaFree(dlost);
             h->np = h->n_active = 0;
             return rc;
         }
+        double *dpos = st.pos, *dvel = st.vel;
+        int32_t *dtet = st.tet;
+        unsigned long long *dlost = st.counter;
         CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
         launch_count_lost(dtet, n, dlost, s);
         if (h->mixed)
@@ -1538,10 +1561,6 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src) {
         CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         h->init_lost = int64_t(lost);
-        cudaFree(dpos);
-        cudaFree(dvel);
-        cudaFree(dtet);
-        cudaFree(dlost);
     }
     h->have_particles = true;
     h->fix_bits = fix_bits_for(n);
@@ -1555,25 +1574,14 @@ int spg_inject_particles(spg_handle *h, int64_t n, const spg_source *src) {
     if (n == 0) return SPG_OK;
     CK(cudaSetDevice(h->device));
     cudaStream_t s = h->stream;
-    double *dpos = nullptr, *dvel = nullptr;
-    int32_t *dtet = nullptr;
-    unsigned long long *dlost = nullptr;
-    CK(dalloc(&dpos, 3 * n));
-    CK(dalloc(&dvel, 3 * n));
-    CK(dalloc(&dtet, n));
-    CK(dalloc(&dlost, 1));
-    auto release = [&]() {
-        cudaFree(dpos);
-        cudaFree(dvel);
-        cudaFree(dtet);
-        cudaFree(dlost);
-    };
-    int rc = sample_particles(h, n, src, h->np, dpos, dvel, dtet, "inject_particles");
+    IoStage st;
+    int rc = io_stage(h, n, st);
+    if (!rc) rc = sample_particles(h, n, src, h->np, st.pos, st.vel, st.tet, "inject_particles");
     if (!rc) rc = grow_particles(h, h->np + n);
-    if (rc) {
-        release();
-        return rc;
-    }
+    if (rc) return rc;
+    double *dpos = st.pos, *dvel = st.vel;
+    int32_t *dtet = st.tet;
+    unsigned long long *dlost = st.counter;
     CK(cudaMemsetAsync(dlost, 0, sizeof(unsigned long long), s));
     launch_count_lost(dtet, n, dlost, s);
     if (h->mixed)
@@ -1584,7 +1592,6 @@ int spg_inject_particles(spg_handle *h, int64_t n, const spg_source *src) {
     unsigned long long lost = 0;
     CK(cudaMemcpyAsync(&lost, dlost, sizeof(lost), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    release();
     h->grad_ready = false;  // the recorded gradient forward no longer matches the particle set
     // the new particles come after the active range; every slot up to np is processed
     h->np += n;
@@ -1662,13 +1669,14 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
     if (n == 0) return SPG_OK;
     CK(cudaSetDevice(h->device));
     cudaStream_t s = h->stream;
-    double *dpos = nullptr, *dvel = nullptr;
-    int32_t *dtet = nullptr;
-    uint32_t *dfl = nullptr;
-    if (pos) CK(dalloc(&dpos, 3 * n));
-    if (vel) CK(dalloc(&dvel, 3 * n));
-    if (tet) CK(dalloc(&dtet, n));
-    if (flags) CK(dalloc(&dfl, n));
+    IoStage st;
+    {
+        const int rc = io_stage(h, n, st);
+        if (rc) return rc;
+    }
+    double *dpos = pos ? st.pos : nullptr, *dvel = vel ? st.vel : nullptr;
+    int32_t *dtet = tet ? st.tet : nullptr;
+    uint32_t *dfl = flags ? st.flags : nullptr;
     if (h->mixed)
         launch_gather32(h->Q[h->cur], n, h->cen, dpos, dvel, dtet, dfl, s);
     else
@@ -1679,10 +1687,6 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
     if (tet) CK(cudaMemcpyAsync(tet, dtet, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
     if (flags) CK(cudaMemcpyAsync(flags, dfl, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    cudaFree(dpos);
-    cudaFree(dvel);
-    cudaFree(dtet);
-    cudaFree(dfl);
     return SPG_OK;
 }
 
@@ -1865,17 +1869,18 @@ int spg_locate(spg_handle *h, int64_t n, const double *pos, int32_t *tet_out) {
     if (!h || n < 0 || (n > 0 && (!pos || !tet_out))) return SPG_E_INVALID;
     if (n == 0) return SPG_OK;
     CK(cudaSetDevice(h->device));
-    double *dpos = nullptr;
-    int32_t *dtet = nullptr;
-    CK(dalloc(&dpos, 3 * n));
-    CK(dalloc(&dtet, n));
+    IoStage st;
+    {
+        const int rc = io_stage(h, n, st);
+        if (rc) return rc;
+    }
+    double *dpos = st.pos;
+    int32_t *dtet = st.tet;
     CK(cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
     launch_locate(dpos, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings, dtet, h->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(tet_out, dtet, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    cudaFree(dpos);
-    cudaFree(dtet);
     return SPG_OK;
 }
 

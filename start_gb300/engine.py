@@ -209,12 +209,27 @@ class StartPIC:
             out[int(pid)] = path
         return out
 
-    def particles(self):
+    def particles(self, out=None):
+        """Positions, velocities, tets and flags by particle id. `out` may hold
+        any of the four arrays (e.g. pinned host memory, so that the copy
+        needs no staging); they must be C-contiguous with the dtypes and shapes
+        returned here."""
         n = self.n_particles
-        pos = np.empty((n, 3))
-        vel = np.empty((n, 3))
-        tet = np.empty(n, np.int32)
-        flags = np.empty(n, np.uint32)
+        out = out or {}
+
+        def take(key, shape, dtype):
+            a = out.get(key)
+            if a is None:
+                return np.empty(shape, dtype)
+            if a.dtype != dtype or a.shape != shape or not a.flags.c_contiguous:
+                raise ValueError(f"particles: out[{key!r}] must be a C-contiguous {np.dtype(dtype)} array of "
+                                 f"shape {shape}")
+            return a
+
+        pos = take("pos", (n, 3), np.float64)
+        vel = take("vel", (n, 3), np.float64)
+        tet = take("tet", (n,), np.int32)
+        flags = take("flags", (n,), np.uint32)
         self._check(self.lib.spg_get_particles(self.h, n, N.as_ptr(pos, C.c_double), N.as_ptr(vel, C.c_double),
                                                N.as_ptr(tet, C.c_int32), N.as_ptr(flags, C.c_uint32)))
         return dict(pos=pos, vel=vel, tet=tet, flags=flags)

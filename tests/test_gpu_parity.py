@@ -258,3 +258,31 @@ def test_walk_cap_flags_lost(libs):
     g.set_particles(pos, vel)
     g.process(1)
     assert g.particles()["flags"][0] == 2
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_particles_into_caller_arrays(libs, precision):
+    """The staged host copies (set / get / locate reuse one device buffer):
+    a read into caller arrays equals a plain read, a smaller second particle
+    set reads back exactly, and a wrongly typed output is refused."""
+    from start_gb300 import StartPIC
+
+    w = _w0(n=3000, precision=precision)
+    g = StartPIC(w.mesh, w.params)
+    g.set_particles(w.pos, w.vel)
+    g.run(5)
+    a = g.particles()
+    out = {"pos": np.empty((3000, 3)), "vel": np.empty((3000, 3)), "tet": np.empty(3000, np.int32),
+           "flags": np.empty(3000, np.uint32)}
+    b = g.particles(out=out)
+    for k in a:
+        assert b[k] is out[k]
+        assert np.array_equal(a[k], b[k])
+    assert np.array_equal(g.locate(w.pos[:700]), g.locate(w.pos)[:700])
+    g.set_particles(w.pos[:1000], w.vel[:1000])
+    c = g.particles()
+    assert np.allclose(c["pos"], w.pos[:1000], rtol=0, atol=0.0 if precision == 0 else 2e-9)  # FP32 local offsets
+    assert np.array_equal(c["tet"], g.locate(w.pos[:1000]))
+    with pytest.raises(ValueError):
+        g.particles(out={"pos": np.empty((1000, 3), np.float32)})
+    g.close()
