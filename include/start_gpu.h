@@ -163,6 +163,12 @@ const char *spg_last_error(const spg_handle *h);
 int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle **out);
 int spg_destroy(spg_handle *h);
 
+/* Wall times of spg_create in ms: [whole call, GPU element maps and orientation,
+ * GPU node incidence + stiffness + Dirichlet elimination, host face matching +
+ * surface triangles + location grid, AMG hierarchy (0 without AMG), uploads
+ * and the rest]. (The reference's FEMInitializer + GSMAssembler set-up.) */
+int spg_setup_times(const spg_handle *h, double ms[6]);
+
 /* Mesh counters: [n_nodes, n_tets, n_triangles, n_boundary_faces, nnz, n_dirichlet]. */
 int spg_mesh_info(const spg_handle *h, int64_t info[6]);
 

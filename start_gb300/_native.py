@@ -109,6 +109,7 @@ SIGNATURES = {
     "spg_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(Params), C.POINTER(_H)]),
     "spg_destroy": (C.c_int, [_H]),
     "spg_mesh_info": (C.c_int, [_H, C.POINTER(C.c_int64)]),
+    "spg_setup_times": (C.c_int, [_H, C.POINTER(C.c_double)]),
     "spg_set_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32]),
     "spg_default_source": (None, [C.POINTER(Source)]),
     "spg_generate_particles": (C.c_int, [_H, C.c_int64, C.POINTER(Source)]),

@@ -6,6 +6,7 @@
 // when due, then process; plus the periodic re-sort that has no reference
 // counterpart (it only changes memory order).
 #include <algorithm>
+#include <chrono>
 #include <random>
 #include <cmath>
 #include <cstring>
@@ -143,6 +144,7 @@ struct spg_handle {
     // calls so that a copy or an injection allocates nothing once grown.
     unsigned char *io = nullptr;
     size_t io_bytes = 0;
+    double setup_ms[6] = {0, 0, 0, 0, 0, 0};  // spg_setup_times
     int64_t occupied = 0;
     bool have_particles = false;
     bool charge_valid = false;
@@ -1153,6 +1155,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         return fail(h, SPG_E_NO_DEVICE, os.str());
     }
     if (cudaSetDevice(params->device) != cudaSuccess) return fail(h, SPG_E_NO_DEVICE, "spg_create: cudaSetDevice");
+    const auto t_create = std::chrono::steady_clock::now();
     HostMesh hm;
     std::string err;
     int rc = prepare_mesh(*mesh, params->bbox_expansion, hm, err);
@@ -1215,8 +1218,10 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         }
     }
     if (h->prm.preconditioner == SPG_PRECOND_AMG || h->prm.preconditioner == SPG_PRECOND_AMG_F32) {
+        const auto t0 = std::chrono::steady_clock::now();
         int rc = setup_amg(h, hm);
         if (rc) return rc;
+        h->setup_ms[4] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     {
         std::vector<int64_t> erp(hm.n_nodes + 1, 0);
@@ -1302,7 +1307,22 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     CK(dalloc(&h->sort_scratch, size_t(sort_scratch_words(h->n_tets))));
     rc = reset_run_state(h);
     if (rc) return rc;
+    CK(cudaStreamSynchronize(s));
+    {
+        double *t = h->setup_ms;
+        t[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_create).count();
+        t[1] = hm.prep_ms[0];
+        t[2] = hm.prep_ms[1];
+        t[3] = hm.prep_ms[2] - hm.prep_ms[0] - hm.prep_ms[1];
+        t[5] = t[0] - hm.prep_ms[2] - t[4];
+    }
     *out = H.release();
+    return SPG_OK;
+}
+
+int spg_setup_times(const spg_handle *h, double ms[6]) {
+    if (!h || !ms) return SPG_E_INVALID;
+    for (int k = 0; k < 6; ++k) ms[k] = h->setup_ms[k];
     return SPG_OK;
 }
 

@@ -129,17 +129,23 @@ __global__ void k_row_cols(const int64_t *__restrict__ nstart, const int32_t *__
         rowlen[i] = 1;
         return;
     }
+    // Each candidate goes into the sorted unique list c[0, u) unless present:
+    // the writes are the list's own shifts, not a sort of every candidate.
     int32_t *c = cand + 4 * nstart[i];
-    int64_t m = 0;
+    int64_t u = 0;
     for (int64_t k = nstart[i]; k < nstart[i + 1]; ++k) {
         const int32_t *v = tn + 4 * int64_t(ntet[k] >> 2);
-        for (int q = 0; q < 4; ++q)
-            if (!is_dir[v[q]]) c[m++] = v[q];
+        for (int q = 0; q < 4; ++q) {
+            const int32_t x = v[q];
+            if (is_dir[x]) continue;
+            int64_t j = u;
+            while (j > 0 && c[j - 1] > x) --j;
+            if (j > 0 && c[j - 1] == x) continue;
+            for (int64_t r = u; r > j; --r) c[r] = c[r - 1];
+            c[j] = x;
+            ++u;
+        }
     }
-    insertion_sort(c, m);
-    int64_t u = 0;
-    for (int64_t k = 0; k < m; ++k)
-        if (u == 0 || c[k] != c[u - 1]) c[u++] = c[k];
     rowlen[i] = int32_t(u);
 }
 

@@ -19,6 +19,7 @@
 #include "philox.h"
 #include "deposit.cuh"
 #include "field.cuh"
+#include "sort_block.cuh"
 #include "spg_internal.h"
 
 namespace spg {
@@ -516,26 +517,10 @@ __global__ void k_gather32(DevParticles32 p, int64_t n, const double *__restrict
     if (flags) flags[id] = ((idf & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((idf & kLost) ? SPG_FLAG_LOST : 0u);
 }
 
-__global__ void k_sort_scatter32(DevParticles32 src, DevParticles32 dst, int64_t n, int n_tets,
-                                 int32_t *__restrict__ offs) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int key = i < n ? ((src.idf[i] & kDead) ? n_tets : src.tet[i]) : -1;
-    const unsigned peers = __match_any_sync(kFull, key);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    int32_t base = 0;
-    if (key >= 0 && lane == leader) base = atomicAdd(offs + key, __popc(peers));
-    base = __shfl_sync(kFull, base, leader);
-    if (key < 0) return;
-    const int64_t j = base + __popc(peers & ((1u << lane) - 1u));
-    dst.x[j] = src.x[i];
-    dst.y[j] = src.y[i];
-    dst.z[j] = src.z[i];
-    dst.vx[j] = src.vx[i];
-    dst.vy[j] = src.vy[i];
-    dst.vz[j] = src.vz[i];
-    dst.tet[j] = src.tet[i];
-    dst.idf[j] = src.idf[i];
+__global__ void __launch_bounds__(kSortBlock) k_sort_scatter32(DevParticles32 src, DevParticles32 dst, int64_t n,
+                                                               int n_tets, int32_t *__restrict__ offs) {
+    __shared__ SortTable t;
+    sort_scatter_block(t, src, dst, n, n_tets, kDead, offs);
 }
 
 inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1) / block); }
@@ -782,7 +767,9 @@ void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, doub
 void launch_resort32(const DevParticles32 &src, DevParticles32 dst, int64_t n, int64_t n_tets, int32_t *scratch,
                      int64_t *n_alive_dev, cudaStream_t s) {
     launch_sort_prepare(src.tet, src.idf, n, n_tets, scratch, n_alive_dev, s);
-    if (n > 0) k_sort_scatter32<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, int(n_tets), sort_offsets(scratch));
+    if (n > 0)
+        k_sort_scatter32<<<grid_for(n, kSortBlock), kSortBlock, 0, s>>>(src, dst, n, int(n_tets),
+                                                                        sort_offsets(scratch));
 }
 
 size_t walk_item32_bytes() { return sizeof(WalkItem32); }

@@ -22,6 +22,7 @@
 #include "field.cuh"
 #include "exact_div.h"
 #include "screen.h"
+#include "sort_block.cuh"
 #include "spg_internal.h"
 
 namespace spg {
@@ -663,17 +664,13 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-__device__ __forceinline__ int sort_key(const DevParticles &p, int64_t i, int n_tets) {
-    return (p.idf[i] & kDead) ? n_tets : p.tet[i];
-}
-
-__global__ void k_sort_hist(const int32_t *__restrict__ tet, const uint32_t *__restrict__ idf, int64_t n, int n_tets,
-                            int32_t *__restrict__ cnt) {
+__global__ void __launch_bounds__(kSortBlock) k_sort_hist(const int32_t *__restrict__ tet,
+                                                          const uint32_t *__restrict__ idf, int64_t n, int n_tets,
+                                                          int32_t *__restrict__ cnt) {
+    __shared__ SortTable t;
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int key = i < n ? ((idf[i] & kDead) ? n_tets : tet[i]) : -1;
-    const unsigned peers = __match_any_sync(kFull, key);
-    const int lane = threadIdx.x & 31;
-    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(cnt + key, __popc(peers));
+    sort_hist_block(t, key, cnt);
 }
 
 // Block-local exclusive scan of one tile; tile total to sums[blockIdx.x].
@@ -771,25 +768,10 @@ __global__ void k_scan_add(int32_t *__restrict__ a, int64_t len, const int32_t *
     if (j == n_tets) *n_alive = v;
 }
 
-__global__ void k_sort_scatter(DevParticles src, DevParticles dst, int64_t n, int n_tets, int32_t *__restrict__ offs) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int key = i < n ? sort_key(src, i, n_tets) : -1;
-    const unsigned peers = __match_any_sync(kFull, key);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    int32_t base = 0;
-    if (key >= 0 && lane == leader) base = atomicAdd(offs + key, __popc(peers));
-    base = __shfl_sync(kFull, base, leader);
-    if (key < 0) return;
-    const int64_t j = base + __popc(peers & ((1u << lane) - 1u));
-    dst.x[j] = src.x[i];
-    dst.y[j] = src.y[i];
-    dst.z[j] = src.z[i];
-    dst.vx[j] = src.vx[i];
-    dst.vy[j] = src.vy[i];
-    dst.vz[j] = src.vz[i];
-    dst.tet[j] = src.tet[i];
-    dst.idf[j] = src.idf[i];
+__global__ void __launch_bounds__(kSortBlock) k_sort_scatter(DevParticles src, DevParticles dst, int64_t n, int n_tets,
+                                                             int32_t *__restrict__ offs) {
+    __shared__ SortTable t;
+    sort_scatter_block(t, src, dst, n, n_tets, kDead, offs);
 }
 
 inline unsigned grid_for(int64_t n, int block) { return unsigned((n + block - 1) / block); }
@@ -878,7 +860,7 @@ void launch_sort_prepare(const int32_t *tet, const uint32_t *idf, int64_t n, int
     int32_t *sums = cnt + len;
     cudaMemsetAsync(cnt, 0, sizeof(int32_t) * len, s);
     cudaMemsetAsync(occupied, 0, sizeof(unsigned long long), s);
-    if (n > 0) k_sort_hist<<<grid_for(n, 256), 256, 0, s>>>(tet, idf, n, int(n_tets), cnt);
+    if (n > 0) k_sort_hist<<<grid_for(n, kSortBlock), kSortBlock, 0, s>>>(tet, idf, n, int(n_tets), cnt);
     k_scan_tile<<<unsigned(nb), kScanThreads, 0, s>>>(cnt, len, int(n_tets), sums, occupied);
     k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
     k_scan_add<<<grid_for(len, 256), 256, 0, s>>>(cnt, len, sums, int(n_tets), n_alive_dev);
@@ -887,7 +869,8 @@ void launch_sort_prepare(const int32_t *tet, const uint32_t *idf, int64_t n, int
 void launch_resort(const DevParticles &src, DevParticles dst, int64_t n, int64_t n_tets, int32_t *scratch,
                    int64_t *n_alive_dev, cudaStream_t s) {
     launch_sort_prepare(src.tet, src.idf, n, n_tets, scratch, n_alive_dev, s);
-    if (n > 0) k_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, int(n_tets), sort_offsets(scratch));
+    if (n > 0)
+        k_sort_scatter<<<grid_for(n, kSortBlock), kSortBlock, 0, s>>>(src, dst, n, int(n_tets), sort_offsets(scratch));
 }
 
 }  // namespace spg

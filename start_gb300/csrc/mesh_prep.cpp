@@ -22,6 +22,7 @@
 // FP64 walk, which must agree bit for bit with the CPU oracle.
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -53,7 +54,14 @@ inline void sort3(int32_t v[3]) {
 
 }  // namespace
 
+namespace {
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+}  // namespace
+
 int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std::string &err) {
+    const auto t_start = std::chrono::steady_clock::now();
     std::ostringstream es;
     if (d.n_nodes <= 0 || d.n_tets <= 0 || !d.node_xyz || !d.tet_nodes) {
         err = "mesh: n_nodes, n_tets, node_xyz and tet_nodes are required";
@@ -86,7 +94,9 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
         }
     {
         int64_t bad = -1;
+        const auto t0 = std::chrono::steady_clock::now();
         const int rc = fem_elements_gpu(m, err, bad);
+        m.prep_ms[0] = ms_since(t0);
         if (rc) return rc;
         if (bad >= 0) {
             es << "mesh: tet " << bad << " has a bad node index or zero volume";
@@ -192,7 +202,9 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
     //    Dirichlet rows as identity rows, the lifting and the eliminated
     //    couplings (on the GPU, kernels_fem.cu).
     {
+        const auto t0 = std::chrono::steady_clock::now();
         const int rc = fem_stiffness_gpu(m, err);
+        m.prep_ms[1] = ms_since(t0);
         if (rc) return rc;
     }
 
@@ -273,6 +285,7 @@ int prepare_mesh(const spg_mesh_desc &d, double bbox_expansion, HostMesh &m, std
                 }
         m.vox_seed.swap(next);
     }
+    m.prep_ms[2] = ms_since(t_start);
     return SPG_OK;
 }
 

@@ -65,6 +65,9 @@ struct HostMesh {
     double vox_origin[3] = {0, 0, 0}, vox_inv[3] = {1, 1, 1};
     int32_t vox_dims[3] = {1, 1, 1};
     std::vector<int32_t> vox_seed;
+    // Set-up wall times (ms): GPU element maps, GPU incidence + stiffness,
+    // the whole preparation.
+    double prep_ms[3] = {0, 0, 0};
 };
 
 // Order-preserving map of a double to int64: a < b <=> key(a) < key(b) for

@@ -296,6 +296,13 @@ class StartPIC:
         phi = np.ascontiguousarray(phi, np.float64)
         self._check(self.lib.spg_set_potential(self.h, N.as_ptr(phi, C.c_double)))
 
+    def setup_times(self):
+        """Wall times of the set-up in ms (spg_setup_times)."""
+        t = (C.c_double * 6)()
+        self._check(self.lib.spg_setup_times(self.h, t))
+        keys = ("create", "fem_elements_gpu", "fem_stiffness_gpu", "mesh_host", "amg", "upload_other")
+        return dict(zip(keys, list(t)))
+
     def matrix(self):
         """The assembled FEM system: CSR (row_ptr, col, val), the lifting and
         the dual volumes (spg_get_matrix)."""

@@ -27,6 +27,9 @@ def _compare(w):
     g.set_potential(phi)
     o.set_potential(phi)
     assert np.array_equal(g.efield(), o.efield())  # the element maps, through E
+    t = g.setup_times()
+    assert min(t.values()) >= 0.0
+    assert t["create"] >= t["fem_elements_gpu"] + t["fem_stiffness_gpu"] + t["mesh_host"]
     g.close()
     o.close()
 

@@ -194,6 +194,29 @@ def test_resort_does_not_change_results(libs):
     assert np.array_equal(a.triangle_counts(), b.triangle_counts())
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_resort_is_a_permutation_of_crowded_tets(libs, precision):
+    """The re-sort merges equal tets per block before its atomics: with
+    hundreds of particles per tet (a 4-cell cube) and settled particles among
+    them, every particle keeps its state through repeated re-sorts."""
+    from start_gb300 import StartPIC
+
+    w = _w0(n=60000, cells=4, collisions=True, precision=precision)
+    vel = w.vel.copy()
+    vel[::3, 2] = -np.abs(vel[::3, 2])  # a third head into the source plane and settle there
+    g = StartPIC(w.mesh, w.params)
+    g.set_particles(w.pos, vel)
+    g.run(12)
+    a = g.particles()
+    assert (a["flags"] != 0).any()
+    for _ in range(3):
+        g.resort()
+    b = g.particles()
+    for k in a:
+        assert np.array_equal(a[k], b[k])
+    g.close()
+
+
 @pytest.mark.parametrize("precond", [0, 2])
 def test_checkpoint_restore_is_exact(libs, precond):
     """With AMG the run solves start from an extrapolation of the previous
