@@ -119,6 +119,17 @@ STEP_TRAFFIC_B = {
     "64": (453.2e6 / 4e6, "ncu capture of k_step64 + k_walk_queue64 at 4e6 particles, scaled by particles"),
     "32": (223.8e6 / 4e6, "ncu capture of k_step32 + k_walk_queue32 at 4e6 particles, scaled by particles"),
 }
+# The resource that binds the step kernels is not HBM: the FP64 form's step is
+# FP64-issue-bound (GB300 issues about 2 FP64 thread-ops per clock per SM),
+# the FP32 form's is memory-latency-bound. Pipe utilisation from the same
+# captures (sm__pipe_fp64_cycles_active, % of peak sustained active).
+STEP_BINDING = {
+    "64": {"resource": "fp64 pipe", "k_step64": 0.783, "k_walk_queue64": 0.589,
+           "source": "ncu --set full, k_step64 + k_walk_queue64 at 4e6 particles"},
+    "32": {"resource": "memory latency (long-scoreboard stalls; fp64 pipe 0 in k_step32)",
+           "k_step32_issue_active": 0.434, "k_step32_warps_active": 0.482,
+           "source": "ncu --set full, k_step32 + k_walk_queue32 at 4e6 particles"},
+}
 
 
 def measured_peak():
@@ -334,14 +345,18 @@ def run_gpu(args):
     name, dms, dbytes, dl = phases[dom]
     bw = dbytes / (dms / 1e3) / 1e9 if dms > 0 else None
     traffic, traffic_src = args.traffic, "--traffic" if args.traffic else None
+    binding = None
     if traffic is None and dom == "step" and args.workload == 1:
         # DRAM bytes (read + write) of the step kernel pair per alive particle from one ncu capture
         # of the same geometry at 4e6 particles, scaled by the particles one launch processes
         per_particle, src = STEP_TRAFFIC_B[sfx]
         traffic, traffic_src = per_particle * ps / max(1, args.steps), src
+        binding = STEP_BINDING[sfx]
     roof = {"kernel": name, "phase": dom, "bound": "hbm", "achieved": bw, "peak": peak, "unit": "GB/s",
             "frac": (bw / peak) if bw else None, "traffic": traffic, "traffic_source": traffic_src,
             "peak_source": peak_src, "bytes_per_launch": dbytes / max(1, dl), "ms_per_launch": dms / max(1, dl)}
+    if binding:
+        roof["binding"] = binding
     for k, (nm, ms_k, b_k, l_k) in phases.items():
         roof[f"{k}_GBps"] = b_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
     breakdown = {k: prof[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")}
