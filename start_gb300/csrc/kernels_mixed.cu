@@ -293,15 +293,17 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
         cur = nxt;
         if (idf & kDead) continue;
         processed++;
+        // The whole 64-byte record in one round trip: M[0..7], {M[8], H}, {cen, ezero}.
+        const float4 *rp = reinterpret_cast<const float4 *>(a.rec + t);
+        const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
         const float vmin = c.vmin_f;
         const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
-        const TetRec32 &R = a.rec[t];
-        const float gx = __ldg(&R.cen[0]) + x, gy = __ldg(&R.cen[1]) + y, gz = __ldg(&R.cen[2]) + z;
+        const float gx = r3.x + x, gy = r3.y + y, gz = r3.z + z;
         const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
                             gz >= c.lo_f[2] && gz <= c.hi_f[2];
         if (slow || !in_box) continue;
-        if (!__ldg(&R.ezero)) {
-            const float hx = __ldg(&R.H[0]), hy = __ldg(&R.H[1]), hz = __ldg(&R.H[2]);
+        if (!__float_as_uint(r3.w)) {
+            const float hx = r2.y, hy = r2.z, hz = r2.w;
             vx = (vx + hx) + hx;
             vy = (vy + hy) + hy;
             vz = (vz + hz) + hz;
@@ -309,13 +311,14 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
         const float dt = c.dt_f;
         const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
         if (!(nx == x && ny == y && nz == z)) {
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
+            // The walk decision needs only the positions, so it comes before the
+            // collision (which changes the velocity alone) and the map's registers
+            // are free again when the collision runs.
             if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
                 a.p.idf[i] = idf | kLost;
                 lost++;
             } else {
-                Geo32 g;
-                load_geo32(a.rec, t, g);
+                const Geo32 g{{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x}};
                 float l[4];
                 bary32(g, nx, ny, nz, l);
                 const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
@@ -324,6 +327,7 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
                 a.p.y[i] = ny;
                 a.p.z[i] = nz;
             }
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
         }
         a.p.vx[i] = vx;
         a.p.vy[i] = vy;
