@@ -1,6 +1,6 @@
 """Benchmark of the PIC/DSMC time step: particle-steps/s on one GB300.
 
-Workload (BASELINE configuration 1, plain FP64): 200 mm cube at h = 2 mm
+Workload (the FP64 form): 200 mm cube at h = 2 mm
 (6.0e6 tets, 1.03e6 nodes), 1e7 Ti+ from a 20 mm disk (Thompson energies,
 cosine-law directions), Ar 0.5 Pa VHS, dt = 5e-9 s, Poisson every 10 steps,
 re-sort every 20. Synthetic, seeded inputs (no dataset is involved).
@@ -405,9 +405,9 @@ def run_gpu(args):
 
     mixed = None
     if not args.no_mixed:
-        # The mixed-precision form on the same inputs and steps (BASELINE
-        # configuration 2): throughput and the L1 error of its surface
-        # histogram against the FP64 form after the same W + K steps.
+        # The mixed-precision form on the same inputs and steps: throughput
+        # and the L1 error of its surface histogram against the FP64 form
+        # after the same W + K steps.
         wm = build_workload(args)
         wm.params["device"] = local
         wm.params["precision"] = 1
