@@ -140,7 +140,7 @@ struct spg_handle {
     int64_t *n_alive_dev = nullptr;
     int32_t *sort_scratch = nullptr;
     // Staging for particles that cross the host boundary or come from a
-    // source (set/get/generate/inject): 56 B per particle + 16, kept between
+    // source (set/get/generate/inject): 60 B per particle + 16, kept between
     // calls so that a copy or an injection allocates nothing once grown.
     unsigned char *io = nullptr;
     size_t io_bytes = 0;
@@ -220,17 +220,18 @@ cudaError_t upload(T **ptr, const std::vector<T> &v, cudaStream_t s) {
     return cudaStreamSynchronize(s);
 }
 
-// Staging of n particles: pos [3n], vel [3n] doubles, tet [n], flags [n]
+// Staging of n particles: pos [3n], vel [3n] doubles, tet [n], flags [n], slot [n]
 // 32-bit words and one 64-bit counter.
 struct IoStage {
     double *pos, *vel;
     int32_t *tet;
     uint32_t *flags;
+    int32_t *slot;  // slot of each id (spg_get_particles)
     unsigned long long *counter;
 };
 
 int io_stage(spg_handle *h, int64_t n, IoStage &st) {
-    const size_t need = 56 * size_t(n) + 16;
+    const size_t need = 60 * size_t(n) + 16;
     if (need > h->io_bytes) {
         cudaFree(h->io);
         h->io = nullptr;
@@ -243,6 +244,7 @@ int io_stage(spg_handle *h, int64_t n, IoStage &st) {
     st.vel = st.pos + 3 * n;
     st.tet = reinterpret_cast<int32_t *>(st.vel + 3 * n);
     st.flags = reinterpret_cast<uint32_t *>(st.tet + n);
+    st.slot = reinterpret_cast<int32_t *>(st.flags + n);
     return SPG_OK;
 }
 
@@ -1698,9 +1700,9 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
     int32_t *dtet = tet ? st.tet : nullptr;
     uint32_t *dfl = flags ? st.flags : nullptr;
     if (h->mixed)
-        launch_gather32(h->Q[h->cur], n, h->cen, dpos, dvel, dtet, dfl, s);
+        launch_gather32(h->Q[h->cur], n, st.slot, h->cen, dpos, dvel, dtet, dfl, s);
     else
-        launch_gather_by_id(h->P[h->cur], n, dpos, dvel, dtet, dfl, s);
+        launch_gather_by_id(h->P[h->cur], n, st.slot, dpos, dvel, dtet, dfl, s);
     CK(cudaGetLastError());
     if (pos) CK(cudaMemcpyAsync(pos, dpos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
     if (vel) CK(cudaMemcpyAsync(vel, dvel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));

@@ -498,12 +498,13 @@ __global__ void k_to_local(const double *__restrict__ pos, const double *__restr
     p.idf[j] = uint32_t(j) | (t < 0 ? kLost : 0u);
 }
 
-__global__ void k_gather32(DevParticles32 p, int64_t n, const double *__restrict__ cen, double *pos, double *vel,
-                           int32_t *tet, uint32_t *flags) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// One thread per id (slot from launch_slot_of_id): coalesced writes in id order.
+__global__ void k_gather32(DevParticles32 p, int64_t n, const int32_t *__restrict__ slot,
+                           const double *__restrict__ cen, double *pos, double *vel, int32_t *tet, uint32_t *flags) {
+    const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int64_t i = slot[id];
     const uint32_t idf = p.idf[i];
-    const int64_t id = idf & kIdMask;
     const int32_t t = p.tet[i];
     const int64_t tc = t < 0 ? 0 : t;
     const double ox = t < 0 ? 0.0 : cen[3 * tc], oy = t < 0 ? 0.0 : cen[3 * tc + 1], oz = t < 0 ? 0.0 : cen[3 * tc + 2];
@@ -762,10 +763,11 @@ void launch_to_local(const double *pos, const double *vel, const int32_t *tet, c
     k_to_local<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, cen, n, p, id_base);
 }
 
-void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,
-                     uint32_t *flags, cudaStream_t s) {
+void launch_gather32(const DevParticles32 &p, int64_t n, int32_t *slot, const double *cen, double *pos, double *vel,
+                     int32_t *tet, uint32_t *flags, cudaStream_t s) {
     if (n <= 0) return;
-    k_gather32<<<grid_for(n, 256), 256, 0, s>>>(p, n, cen, pos, vel, tet, flags);
+    launch_slot_of_id(p.idf, n, slot, s);
+    k_gather32<<<grid_for(n, 256), 256, 0, s>>>(p, n, slot, cen, pos, vel, tet, flags);
 }
 
 void launch_resort32(const DevParticles32 &src, DevParticles32 dst, int64_t n, int64_t n_tets, int32_t *scratch,

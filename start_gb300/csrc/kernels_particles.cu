@@ -638,11 +638,20 @@ __global__ void k_init_particles(const double *__restrict__ pos, const double *_
     p.idf[j] = uint32_t(j) | (t < 0 ? kLost : 0u);
 }
 
-__global__ void k_gather_by_id(DevParticles p, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags) {
+// Slot of each particle id (the ids are a permutation of 0..n-1).
+__global__ void k_slot_of_id(const uint32_t *__restrict__ idf, int64_t n, int32_t *__restrict__ slot) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i < n) slot[idf[i] & kIdMask] = int32_t(i);
+}
+
+// One thread per id: scattered reads of its slot, coalesced writes in id
+// order (writing by slot would scatter partial-sector writes instead).
+__global__ void k_gather_by_id(DevParticles p, int64_t n, const int32_t *__restrict__ slot, double *pos, double *vel,
+                               int32_t *tet, uint32_t *flags) {
+    const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int64_t i = slot[id];
     const uint32_t idf = p.idf[i];
-    const int64_t id = idf & kIdMask;
     if (pos) {
         pos[3 * id] = p.x[i];
         pos[3 * id + 1] = p.y[i];
@@ -832,10 +841,15 @@ void launch_init_particles(const double *pos, const double *vel, const int32_t *
     k_init_particles<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, n, p, id_base);
 }
 
-void launch_gather_by_id(const DevParticles &p, int64_t n, double *pos, double *vel, int32_t *tet, uint32_t *flags,
-                         cudaStream_t s) {
+void launch_slot_of_id(const uint32_t *idf, int64_t n, int32_t *slot, cudaStream_t s) {
+    if (n > 0) k_slot_of_id<<<grid_for(n, 256), 256, 0, s>>>(idf, n, slot);
+}
+
+void launch_gather_by_id(const DevParticles &p, int64_t n, int32_t *slot, double *pos, double *vel,
+                         int32_t *tet, uint32_t *flags, cudaStream_t s) {
     if (n <= 0) return;
-    k_gather_by_id<<<grid_for(n, 256), 256, 0, s>>>(p, n, pos, vel, tet, flags);
+    launch_slot_of_id(p.idf, n, slot, s);
+    k_gather_by_id<<<grid_for(n, 256), 256, 0, s>>>(p, n, slot, pos, vel, tet, flags);
 }
 
 int64_t sort_scratch_words(int64_t n_tets) {

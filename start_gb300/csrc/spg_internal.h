@@ -224,8 +224,11 @@ void launch_count_lost(const int32_t *tet, int64_t n, unsigned long long *out, c
 // Installs n particles at slots [id_base, id_base + n) with ids id_base + i.
 void launch_init_particles(const double *pos, const double *vel, const int32_t *tet, int64_t n,
                            DevParticles p, cudaStream_t s, int64_t id_base = 0);
-void launch_gather_by_id(const DevParticles &p, int64_t n, double *pos, double *vel, int32_t *tet,
-                         uint32_t *flags, cudaStream_t s);
+// Slot of each particle id; the gathers below write in id order through it
+// (slot: n words of scratch).
+void launch_slot_of_id(const uint32_t *idf, int64_t n, int32_t *slot, cudaStream_t s);
+void launch_gather_by_id(const DevParticles &p, int64_t n, int32_t *slot, double *pos, double *vel,
+                         int32_t *tet, uint32_t *flags, cudaStream_t s);
 // Re-sort: histogram, exclusive scan, scatter. Writes the number of alive
 // particles to *n_alive_dev. scratch must hold sort_scratch_words(n_tets) ints, 8-byte aligned.
 int64_t sort_scratch_words(int64_t n_tets);
@@ -309,8 +312,8 @@ void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, in
                       const OccList &occ, cudaStream_t s);
 void launch_to_local(const double *pos, const double *vel, const int32_t *tet, const double *cen, int64_t n,
                      DevParticles32 p, cudaStream_t s, int64_t id_base = 0);
-void launch_gather32(const DevParticles32 &p, int64_t n, const double *cen, double *pos, double *vel, int32_t *tet,
-                     uint32_t *flags, cudaStream_t s);
+void launch_gather32(const DevParticles32 &p, int64_t n, int32_t *slot, const double *cen, double *pos, double *vel,
+                     int32_t *tet, uint32_t *flags, cudaStream_t s);
 void launch_resort32(const DevParticles32 &src, DevParticles32 dst, int64_t n, int64_t n_tets, int32_t *scratch,
                      int64_t *n_alive_dev, cudaStream_t s);
 size_t walk_item32_bytes();
