@@ -159,13 +159,16 @@ def build_workload(args):
     return w
 
 
-def cpu_sample(w, n_sample, steps, warmup=0, threads=None):
+def cpu_sample(w, n_sample, steps, warmup=0, threads=None, want_state=False, timed_threads=None):
     """Times the CPU oracle on the first n_sample particles of the workload:
     one untimed deposit + cold solve and `warmup` untimed steps, then `steps`
     timed steps of the full loop (deposit + warm PCG every poisson_every
-    steps, push/walk/collide/settle every step), as the GPU arm does."""
+    steps, push/walk/collide/settle every step), as the GPU arm does.
+    timed_threads: thread count of the timed steps only (the untimed ones use
+    `threads`)."""
     import oracle
 
+    prev = oracle.get_threads()
     if threads:
         oracle.set_threads(threads)
     t0 = time.perf_counter()
@@ -175,18 +178,87 @@ def cpu_sample(w, n_sample, steps, warmup=0, threads=None):
     if warmup > 0:
         o.run(warmup, raise_on_nonconvergence=False)
     s0 = o.stats()["particle_steps"]
+    if timed_threads:
+        oracle.set_threads(timed_threads)
     t0 = time.perf_counter()
     o.run(steps, raise_on_nonconvergence=False)
     dt = time.perf_counter() - t0
-    s1 = o.stats()["particle_steps"]
+    st = o.stats()
+    info = dict(setup_s=t_setup, timed_s=dt, particle_steps=st["particle_steps"] - s0, threads=oracle.get_threads())
+    if want_state:
+        info["state"] = {"counts": o.triangle_counts(), "stats": st, "tet": o.particles()["tet"]}
     o.close()
-    return (s1 - s0) / dt, dict(setup_s=t_setup, timed_s=dt, particle_steps=s1 - s0, threads=oracle.get_threads())
+    oracle.set_threads(prev)
+    return (st["particle_steps"] - s0) / dt, info
 
 
 def cpu_sample_desc(w, n_sample, steps, warmup):
     who = "all" if n_sample >= len(w.pos) else f"{n_sample} of"
     return (f"{who} {len(w.pos)} particles on the full mesh, {warmup} untimed + {steps} timed full-loop steps "
             f"(deposit + warm PCG every {w.params['poisson_every']} steps, push/walk/collide/settle every step)")
+
+
+def host_cpu():
+    """CPU model string, logical cores and OMP_NUM_THREADS of this host."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        import platform
+
+        model = platform.processor() or platform.machine()
+    return {"cpu_model": model, "nproc": os.cpu_count(), "OMP_NUM_THREADS": os.environ.get("OMP_NUM_THREADS")}
+
+
+def surface_bins(mesh, patch=0.01):
+    """Bin of each surface triangle: its surface tag x patch-sized squares."""
+    lo = mesh.nodes.min(0)
+    n = int(np.ceil(float(np.max(mesh.nodes.max(0) - lo)) / patch))
+    ij = np.floor((mesh.triangle_centroids() - lo) / patch).astype(np.int64).clip(0, n - 1)
+    key = mesh.tri_tag.astype(np.int64) * n ** 3 + (ij * np.array([n * n, n, 1])).sum(1)
+    return np.unique(key, return_inverse=True)[1]
+
+
+def chi2_two_sample(a, b):
+    """Chi-square two-sample test of two histograms (bins empty in both dropped)."""
+    from scipy import stats
+
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    keep = (a + b) > 0
+    a, b = a[keep], b[keep]
+    if len(a) < 2 or a.sum() == 0 or b.sum() == 0:
+        return None, 0, None
+    k1, k2 = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    chi2 = float(np.sum((k1 * a - k2 * b) ** 2 / (a + b)))
+    dof = len(a) - 1
+    return chi2, dof, float(stats.chi2.sf(chi2, dof))
+
+
+def compare_forms(ref, other):
+    """Errors of one GPU state against another after the same steps: L1 error
+    of the surface histogram over triangles, landing-position RMS over the
+    particles settled in both, and the potential's max error."""
+    cr, co = ref["counts"].astype(float), other["counts"].astype(float)
+    both = ((ref["flags"] & 1) != 0) & ((other["flags"] & 1) != 0)
+    d = other["pos"][both] - ref["pos"][both]
+    return {"l1_hist_error": float(np.abs(co - cr).sum() / max(cr.sum(), 1.0)),
+            "landing_rms_m": float(np.sqrt(np.mean(np.sum(d * d, axis=1)))) if both.any() else None,
+            "landed_in_both": int(both.sum()),
+            "phi_max_rel_error": float(np.max(np.abs(other["phi"] - ref["phi"])) /
+                                       max(float(np.max(np.abs(ref["phi"]))), 1e-300)),
+            "settled_ref": int(cr.sum()), "settled_other": int(co.sum())}
+
+
+def gpu_state(eng):
+    p = eng.particles()
+    return {"counts": eng.triangle_counts(), "pos": p["pos"], "flags": p["flags"], "tet": p["tet"],
+            "phi": eng.potential(), "stats": eng.stats()}
 
 
 def run_reference(args):
@@ -203,7 +275,8 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded workload generator)",
         "config": config_dict(args, w),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": info.get("threads"), "kind": "port",
-                         "sample": cpu_sample_desc(w, n_sample, steps, args.warmup), "timed_s": info["timed_s"]},
+                         "sample": cpu_sample_desc(w, n_sample, steps, args.warmup), "timed_s": info["timed_s"],
+                         **host_cpu()},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference itself needs CGAL/Trilinos/Gmsh (absent); the timed CPU path is the FP64 "
                 "OpenMP oracle port of its step",
@@ -273,6 +346,77 @@ def config_dict(args, w):
             "timed_steps_start_at": args.warmup}
 
 
+def timed_steps(eng, stream, steps):
+    """Device time (CUDA events on the library's stream) of `steps` steps of
+    spg_run, with the alive-particle steps they processed."""
+    import torch
+
+    s0 = eng.stats()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    eng.run(steps, raise_on_nonconvergence=False)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    s1 = eng.stats()
+    return ev0.elapsed_time(ev1), s1["particle_steps"] - s0["particle_steps"], s0, s1
+
+
+def pinned_io(w):
+    import torch
+
+    n = len(w.pos)
+    pos_h = torch.from_numpy(w.pos).pin_memory().numpy()
+    vel_h = torch.from_numpy(w.vel).pin_memory().numpy()
+    out = {"pos": torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy(),
+           "vel": torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy(),
+           "tet": torch.empty(n, dtype=torch.int32).pin_memory().numpy(),
+           "flags": torch.empty(n, dtype=torch.int32).pin_memory().numpy().view(np.uint32)}
+    return pos_h, vel_h, out
+
+
+def e2e_leg(eng, w, steps, reference_calls):
+    """A whole job through the C ABI with pinned host buffers: upload, `steps`
+    steps with the per-step stats read (the reference's stop check), download
+    of particles and counters; host wall clock. reference_calls: the steps go
+    through the reference-named calls (spg_gather -> spg_solve every
+    poisson_every steps with the density left on the GPU, spg_process every
+    step), as the C++ shim's time loop makes them; otherwise spg_run(1)."""
+    import torch
+
+    pos_h, vel_h, out = pinned_io(w)
+    every = w.params["poisson_every"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.set_particles(pos_h, vel_h)
+    s_start = eng.stats()["particle_steps"]
+    for k in range(steps):
+        if reference_calls:
+            if k % every == 0:
+                eng.gather(want_rho=False)
+                eng.solve(rho=None, want_phi=False, raise_on_nonconvergence=False)
+            st = eng.process(1)  # returns the step's stats (D2H)
+        else:
+            st = eng.run(1, raise_on_nonconvergence=False)
+        if st["n_alive"] == 0:
+            break
+    counts = eng.triangle_counts()
+    eng.particles(out=out)  # D2H straight into the pinned arrays
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    ps = eng.stats()["particle_steps"] - s_start
+    h2d = (pos_h.nbytes + vel_h.nbytes) / steps
+    d2h = (sum(a.nbytes for a in out.values()) + counts.nbytes) / steps + 96
+    calls = ("spg_set_particles; spg_gather(NULL) + spg_solve(NULL) every poisson_every steps, spg_process(1) "
+             "every step; spg_get_triangle_counts, spg_get_particles" if reference_calls else
+             "spg_set_particles; spg_run(1) per step; spg_get_triangle_counts, spg_get_particles")
+    return {"value": ps / t, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "seconds": t,
+            "calls": calls, "note": "job-level: upload, K steps from step 0 (cold first Poisson solve), "
+                                    "per-step stats read, download; host wall clock"}
+
+
 def run_gpu(args):
     import torch
 
@@ -282,46 +426,34 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.init_process_group("nccl")
     torch.cuda.set_device(local)
+    W, K = args.warmup, args.steps
     w = build_workload(args)
     w.params["device"] = local
     eng = StartPIC(w.mesh, w.params)
     setup_ms = eng.setup_times()  # FEM set-up on the GPU, host mesh work, AMG hierarchy
     eng.set_particles(w.pos, w.vel)
     stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=local)
-    eng.run(args.warmup)
+    eng.run(W)
     eng.synchronize()
     # The timed steps run without the per-phase event profiler; the same steps
     # are then replayed from a checkpoint (bit-exact) with it for the breakdown.
     snap = eng.checkpoint()
-    st0 = eng.stats()
     clocks = ClockSampler(local)
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    eng.run(args.steps, raise_on_nonconvergence=False)
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
+    ms, ps, st0, st1 = timed_steps(eng, stream, K)
     if world > 1:
         torch.distributed.barrier()
-    ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
-    st1 = eng.stats()
     eng.restore(snap)
     del snap
     eng.profile_enable(True)
-    eng.run(args.steps, raise_on_nonconvergence=False)
+    eng.run(K, raise_on_nonconvergence=False)
     prof = eng.profile()
     eng.profile_enable(False)
     assert eng.stats()["particle_steps"] == st1["particle_steps"]
-    counts_fp64 = eng.triangle_counts()  # after W + K steps, for the mixed-form comparison
-    state_fp64 = eng.particles() if not args.no_mixed else None
-    phi_fp64 = eng.potential() if not args.no_mixed else None
-    ps = st1["particle_steps"] - st0["particle_steps"]
+    state64 = gpu_state(eng)  # after W + K steps: parity against the oracle and the mixed form
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -350,7 +482,7 @@ def run_gpu(args):
         # DRAM bytes (read + write) of the step kernel pair per alive particle from one ncu capture
         # of the same geometry at 4e6 particles, scaled by the particles one launch processes
         per_particle, src = STEP_TRAFFIC_B[sfx]
-        traffic, traffic_src = per_particle * ps / max(1, args.steps), src
+        traffic, traffic_src = per_particle * ps / max(1, K), src
         binding = STEP_BINDING[sfx]
     roof = {"kernel": name, "phase": dom, "bound": "hbm", "achieved": bw, "peak": peak, "unit": "GB/s",
             "frac": (bw / peak) if bw else None, "traffic": traffic, "traffic_source": traffic_src,
@@ -366,87 +498,49 @@ def run_gpu(args):
                                  if prof["deposit_ms"] > 0 else None)
     breakdown["occupied_tets"] = prof["occupied_tets"]
 
-    # e2e through the C ABI with host buffers (pinned)
-    e2e = None
-    if not args.no_e2e:
-        n = len(w.pos)
-        pos_h = torch.from_numpy(w.pos).pin_memory().numpy()
-        vel_h = torch.from_numpy(w.vel).pin_memory().numpy()
-        out = {"pos": torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy(),
-               "vel": torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy(),
-               "tet": torch.empty(n, dtype=torch.int32).pin_memory().numpy(),
-               "flags": torch.empty(n, dtype=torch.int32).pin_memory().numpy().view(np.uint32)}
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        eng.set_particles(pos_h, vel_h)
-        s_start = eng.stats()["particle_steps"]
-        for _ in range(args.steps):
-            eng.run(1, raise_on_nonconvergence=False)  # returns the step's stats (D2H)
-        counts = eng.triangle_counts()
-        eng.particles(out=out)  # D2H straight into the pinned arrays
-        torch.cuda.synchronize()
-        t_e2e = time.perf_counter() - t0
-        ps_e2e = eng.stats()["particle_steps"] - s_start
-        h2d = (pos_h.nbytes + vel_h.nbytes) / args.steps
-        d2h = (sum(a.nbytes for a in out.values()) + counts.nbytes) / args.steps + 96
-        e2e = {"value": ps_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "seconds": t_e2e, "note": "job-level: upload, K steps from step 0 (cold first Poisson solve), "
-                                         "per-step stats read, download; host wall clock"}
+    # the configured run length of the mixed-form comparison (1,000 steps):
+    # both forms continue from their W + K state, untimed
+    acc_steps = max(args.accuracy_steps, W + K)
+    state64_long = None
+    if not args.no_mixed and not args.no_accuracy and acc_steps > W + K:
+        eng.run(acc_steps - W - K, raise_on_nonconvergence=False)
+        state64_long = gpu_state(eng)
 
+    e2e = e2e_ref = None
+    if not args.no_e2e:
+        e2e = e2e_leg(eng, w, K, reference_calls=False)
+        e2e_ref = e2e_leg(eng, w, K, reference_calls=True)
     eng.close()
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        n_sample = min(args.cpu_sample or len(w.pos), len(w.pos))
-        steps = args.cpu_steps or args.steps
-        v, info = cpu_sample(w, n_sample, steps, args.warmup)
-        cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
-               "sample": cpu_sample_desc(w, n_sample, steps, args.warmup), "timed_s": info["timed_s"],
-               "setup_s": info["setup_s"]}
 
     mixed = None
     if not args.no_mixed:
-        # The mixed-precision form on the same inputs and steps: throughput
-        # and the L1 error of its surface histogram against the FP64 form
-        # after the same W + K steps.
+        # The mixed-precision form on the same inputs and steps: throughput,
+        # and its errors against the FP64 form after the same W + K steps and
+        # after the configured 1,000 steps.
         wm = build_workload(args)
         wm.params["device"] = local
         wm.params["precision"] = 1
         em = StartPIC(wm.mesh, wm.params)
         em.set_particles(wm.pos, wm.vel)
         sm_ = torch.cuda.ExternalStream(em.stream_ptr(), device=local)
-        em.run(args.warmup)
+        em.run(W)
         em.synchronize()
         msnap = em.checkpoint()
-        m0 = em.stats()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(sm_)
-        em.run(args.steps, raise_on_nonconvergence=False)
-        e1.record(sm_)
-        e1.synchronize()
-        mms = e0.elapsed_time(e1)
-        m1 = em.stats()
+        mms, mps, _, _ = timed_steps(em, sm_, K)
         em.restore(msnap)
         del msnap
         em.profile_enable(True)
-        em.run(args.steps, raise_on_nonconvergence=False)
+        em.run(K, raise_on_nonconvergence=False)
         mp = em.profile()
         em.profile_enable(False)
-        cm = em.triangle_counts().astype(float)
-        cf = counts_fp64.astype(float)
-        sm_state = em.particles()
-        phi_m = em.potential()
-        both = ((sm_state["flags"] & 1) != 0) & ((state_fp64["flags"] & 1) != 0)
-        d = sm_state["pos"][both] - state_fp64["pos"][both]
-        land_rms = float(np.sqrt(np.mean(np.sum(d * d, axis=1)))) if both.any() else None
-        phi_err = float(np.max(np.abs(phi_m - phi_fp64)) / max(np.max(np.abs(phi_fp64)), 1e-300))
-        mval = (m1["particle_steps"] - m0["particle_steps"]) / (mms / 1e3)
-        mixed = {"value": mval, "unit": UNIT, "ms_per_step": mms / args.steps, "speedup_vs_fp64": mval / value,
-                 "l1_hist_error_vs_fp64": float(np.abs(cm - cf).sum() / max(cf.sum(), 1.0)),
-                 "landing_rms_m_vs_fp64": land_rms, "landed_in_both": int(both.sum()),
-                 "phi_max_rel_error_vs_fp64": phi_err,
-                 "settled_fp64": int(cf.sum()), "settled_mixed": int(cm.sum()),
+        cmp_short = compare_forms(state64, gpu_state(em))
+        mval = mps / (mms / 1e3)
+        mixed = {"value": mval, "unit": UNIT, "ms_per_step": mms / K, "speedup_vs_fp64": mval / value,
+                 "l1_hist_error_vs_fp64": cmp_short["l1_hist_error"],
+                 "landing_rms_m_vs_fp64": cmp_short["landing_rms_m"], "landed_in_both": cmp_short["landed_in_both"],
+                 "phi_max_rel_error_vs_fp64": cmp_short["phi_max_rel_error"],
+                 "settled_fp64": cmp_short["settled_ref"], "settled_mixed": cmp_short["settled_other"],
+                 "compared_after_steps": W + K,
                  "breakdown_ms": {k: mp[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")},
                  "pcg_iters": mp["pcg_iters"],
                  "step_GBps": mp["step_bytes"] / (mp["step_ms"] / 1e3) / 1e9 if mp["step_ms"] > 0 else None,
@@ -454,18 +548,81 @@ def run_gpu(args):
                  "gpu_launches": mp["kernel_launches"],
                  "dtype": ("f32 state/push/V-cycle, f64 PCG SpMV + vectors + sums" if args.precond != "jacobi"
                            else "f32 state/push/SpMV, f64 refinement + sums")}
+        if state64_long is not None:
+            em.run(acc_steps - W - K, raise_on_nonconvergence=False)
+            acc = compare_forms(state64_long, gpu_state(em))
+            acc["steps"] = acc_steps
+            acc["bar"] = "l1_hist_error <= 0.01"
+            acc["pass"] = acc["l1_hist_error"] <= 0.01
+            mixed["accuracy_full_run"] = acc
         em.close()
+
+    fp64_amg = None
+    if not args.no_fp64_amg and args.precond == "amg32" and args.precision == "fp64":
+        # FP64 throughout: the same FP64 step with the V-cycle in FP64 too
+        wa = build_workload(args)
+        wa.params["device"] = local
+        wa.params["preconditioner"] = 1
+        ea = StartPIC(wa.mesh, wa.params)
+        ea.set_particles(wa.pos, wa.vel)
+        sa = torch.cuda.ExternalStream(ea.stream_ptr(), device=local)
+        ea.run(W)
+        ams, aps, _, ast1 = timed_steps(ea, sa, K)
+        cmp_a = compare_forms(state64, gpu_state(ea))
+        aval = aps / (ams / 1e3)
+        fp64_amg = {"value": aval, "unit": UNIT, "ms_per_step": ams / K, "preconditioner": "amg (FP64 V-cycle)",
+                    "cg_iters_total": ast1["cg_iters_total"], "l1_hist_error_vs_amg32": cmp_a["l1_hist_error"],
+                    "phi_max_rel_error_vs_amg32": cmp_a["phi_max_rel_error"]}
+        if mixed:
+            mixed["speedup_vs_fp64_amg"] = mixed["value"] / aval
+        ea.close()
+
+    cpu = parity = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        n_sample = min(args.cpu_sample or len(w.pos), len(w.pos))
+        steps = args.cpu_steps or K
+        full = n_sample == len(w.pos) and steps == K
+        v, info = cpu_sample(w, n_sample, steps, W, want_state=full)
+        cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
+               "sample": cpu_sample_desc(w, n_sample, steps, W), "timed_s": info["timed_s"],
+               "setup_s": info["setup_s"], **host_cpu()}
+        if full:
+            # the headline run against the oracle on the identical workload and steps
+            so = info["state"]
+            inv = surface_bins(w.mesh, 0.01)
+            chi2, dof, p = chi2_two_sample(np.bincount(inv, weights=state64["counts"].astype(float)),
+                                           np.bincount(inv, weights=so["counts"].astype(float)))
+            cg_, co_ = state64["stats"]["collisions"], so["stats"]["collisions"]
+            parity = {"vs": "FP64 CPU oracle, same workload and seeds", "steps": W + K,
+                      "gpu_preconditioner": args.precond, "oracle_solver": "Jacobi PCG",
+                      "chi2_p": p, "chi2": chi2, "chi2_dof": dof, "bins": "surface tag x 10 mm squares",
+                      "collisions_gpu": int(cg_), "collisions_oracle": int(co_),
+                      "collisions_ratio": cg_ / co_ if co_ else None,
+                      "settled_gpu": int(state64["counts"].sum()), "settled_oracle": int(so["counts"].sum()),
+                      "identical_tet_fraction": float(np.mean(state64["tet"] == so["tet"])),
+                      "bars": "chi2_p > 0.01, collisions within 5 %"}
+            parity["pass"] = bool(p is not None and p > 0.01 and abs(cg_ - co_) <= 0.05 * max(co_, 1))
+        if not args.no_cpu1:
+            # one core, a bounded sample: a tenth of the particles, W untimed
+            # steps on all cores (the cold solve), then 10 timed steps with one
+            # warm solve on one core
+            n1 = min(len(w.pos), max(1, len(w.pos) // 10))
+            v1, i1 = cpu_sample(w, n1, 10, W, timed_threads=1)
+            cpu["one_core"] = {"value": v1, "unit": UNIT, "cores": i1["threads"],
+                               "sample": cpu_sample_desc(w, n1, 10, W), "timed_s": i1["timed_s"]}
+
     grad = None
     if not args.no_grad and rank == 0:
         grad = grad_leg(args, local)
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded workload generator)", "config": config_dict(args, w),
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown, "mixed": mixed, "grad": grad,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "e2e_reference_calls": e2e_ref, "clocks": clk,
+            "gpu_launches": prof["kernel_launches"], "breakdown_ms": breakdown, "parity": parity,
+            "mixed": mixed, "fp64_amg": fp64_amg, "grad": grad,
             "alive_particles": {"start": st0["n_alive"], "end": st1["n_alive"]},
             "setup_ms": setup_ms,
             "cg_iters_last": st1["cg_iters_last"],
@@ -498,6 +655,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the untimed FP64-vs-mixed comparison over the configured run length")
+    ap.add_argument("--accuracy-steps", type=int, default=1000, help="steps of that comparison")
+    ap.add_argument("--no-fp64-amg", action="store_true", help="skip the FP64-V-cycle leg")
+    ap.add_argument("--no-cpu1", action="store_true", help="skip the one-core CPU sample")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the step kernel, if captured")
     args = ap.parse_args()

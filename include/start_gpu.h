@@ -251,11 +251,21 @@ int spg_generate_particles(spg_handle *h, int64_t n, const spg_source *src);
  * draws new numbers from the same seed. */
 int spg_inject_particles(spg_handle *h, int64_t n, const spg_source *src);
 
-/* (a) P1 charge deposit of all alive particles; rho_out [n_nodes] C/m^3 (nullable). */
+/* (a) P1 charge deposit of all alive particles; rho_out [n_nodes] C/m^3 (nullable).
+ * With rho_out NULL the density stays on the device, where the next
+ * spg_solve(h, NULL, ...) uses it: the per-step gather -> solve of
+ * ModelingMainDriver.cpp:146-184 then moves nothing through the host. */
 int spg_gather(spg_handle *h, double *rho_out);
+/* Nodal density [n_nodes] C/m^3 of the handle's current charge (the last
+ * deposit, or the density last given to spg_solve), without depositing again:
+ * the NodeChargeDensitiesMap that gather fills in the reference
+ * (include/ParticleInCellEngine/NodeChargeDensityProcessor.hpp:39-46), read
+ * only when the caller looks at it. SPG_E_STATE before any deposit. */
+int spg_get_charge_density(spg_handle *h, double *rho_out);
 /* (b) Poisson solve K phi = rho*Vdual/eps0 with Dirichlet lifting, warm started
  * from the previous phi; then E per tet. rho_or_null: use this nodal rho
- * instead of the last deposit. Returns SPG_E_NOT_CONVERGED at the cap. */
+ * (host memory, copied up once; the node charges rho*Vdual are formed on the
+ * device) instead of the last deposit. Returns SPG_E_NOT_CONVERGED at the cap. */
 int spg_solve(spg_handle *h, const double *rho_or_null, double *phi_out, int32_t *iters,
               double *relres);
 /* (c)(d)(e) nsteps particle steps with the current E (no deposit, no solve). */
@@ -319,13 +329,24 @@ int spg_profile_reset(spg_handle *h);
  * nothing. It has no counterpart in the reference: it exists for callers that
  * must not call cudaMalloc/cudaFree. That covers a program whose device memory
  * is all owned by its own pool (a PyTorch caching allocator, a fixed arena),
- * and a loop that must not take the device synchronisation an allocation can
- * imply.
+ * and a loop that must not take the device-wide synchronisation that
+ * cudaMalloc/cudaFree can imply. The call itself still synchronises the
+ * stream it is given: every 8 iterations it reads the CG scalars back to the
+ * host to decide whether to go on.
  *
  * row_ptr [n+1], col [nnz], val [nnz], b [n] and x [n] are DEVICE pointers the
- * caller allocated; x holds the initial guess and receives the solution. The
- * stop rule is the one spg_solve uses: ||b - A x||_2 <= rtol ||b||_2, or
- * max_iter iterations (SPG_E_NOT_CONVERGED, x keeps the last iterate).
+ * caller allocated; x holds the initial guess and receives the solution.
+ * Stop rule: ||r_k||_2 <= rtol ||b||_2, where r_k is the CG residual updated
+ * by the recurrence r_{k+1} = r_k - alpha A p_k (equal to b - A x_k up to
+ * rounding), or max_iter iterations.
+ * Results:
+ *   SPG_OK               converged; *iters and *relres = ||r_k|| / ||b||.
+ *                        b = 0 gives x = 0, 0 iterations, relres 0.
+ *   SPG_E_NOT_CONVERGED  max_iter reached, or a CG breakdown (p.Ap <= 0: the
+ *                        matrix is not SPD, or the data hold NaN); the
+ *                        message says which; x keeps the last iterate.
+ *   SPG_E_INVALID        bad sizes or null arrays, or a row with no stored
+ *                        diagonal entry or a zero or non-finite one.
  * stream is a cudaStream_t, or NULL for the default stream.
  *
  * Limit: n <= 131072 rows. Larger n returns SPG_E_INVALID without touching

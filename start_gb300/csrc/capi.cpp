@@ -88,6 +88,8 @@ struct spg_handle {
     uint32_t field_epoch = 0;                 // epoch of the current potential's field
     bool field_full = true;                   // every tet's field is of field_epoch
     bool in_run = false;                      // inside spg_run: solves refresh the occupied tets only
+    bool occ_fresh = false;                   // no particle has moved since the deposit listed the tets
+    int64_t resorted_at = -1;                 // step of the last periodic re-sort
     int32_t *occ_list = nullptr;              // tets holding particles at the last deposit
     unsigned int *occ_n = nullptr;
     uint32_t *occ_gen = nullptr;              // per tet: generation of the list that holds it
@@ -776,6 +778,7 @@ int do_gather(spg_handle *h) {
                         (h->mixed ? 52.0 : 112.0) * double(h->occupied ? h->occupied : h->n_tets) +
                         16.0 * double(h->n_nodes);
     h->charge_valid = true;
+    h->occ_fresh = true;
     return SPG_OK;
 }
 
@@ -1014,6 +1017,7 @@ void free_tracks(spg_handle *h) {
 }
 
 int do_process(spg_handle *h) {
+    h->occ_fresh = false;
     if (h->track_k > 0) {
         const int rc = record_tracks(h);
         if (rc) return rc;
@@ -1069,6 +1073,8 @@ int reset_run_state(spg_handle *h) {
     h->cg_iters_total = 0;
     h->cg_relres_last = 0.0;
     h->charge_valid = false;
+    h->occ_fresh = false;
+    h->resorted_at = -1;
     CK(cudaMemsetAsync(h->ctr, 0, sizeof(DevCounters), h->stream));
     CK(cudaMemsetAsync(h->tri_count, 0, sizeof(unsigned int) * std::max<int64_t>(h->n_tris, 1), h->stream));
     CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
@@ -1595,6 +1601,7 @@ int spg_inject_particles(spg_handle *h, int64_t n, const spg_source *src) {
     if (n < 0 || h->np + n > kMaxParticles) return fail(h, SPG_E_INVALID, "inject_particles: n out of range");
     if (n == 0) return SPG_OK;
     CK(cudaSetDevice(h->device));
+    h->occ_fresh = false;  // the new particles' tets are not on the deposit's list
     cudaStream_t s = h->stream;
     IoStage st;
     int rc = io_stage(h, n, st);
@@ -1712,10 +1719,40 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
     return SPG_OK;
 }
 
+namespace {
+// The periodic re-sort by tet, at the steps that are multiples of
+// resort_every, once per step, by whichever call comes first in that step
+// (spg_run, spg_gather or spg_process). It changes only the memory order.
+int maybe_resort(spg_handle *h) {
+    if (h->prm.resort_every <= 0 || h->step % h->prm.resort_every != 0 || h->resorted_at == h->step) return SPG_OK;
+    h->resorted_at = h->step;
+    return do_resort(h);
+}
+
+// Solve of the deposit just made from this handle's particles: AMG starts
+// from the extrapolation of the last such solves, and the field is computed
+// for the occupied tets only (the walks compute the tets particles enter).
+int solve_run_deposit(spg_handle *h) {
+    if (h->amg || h->amg32) {
+        launch_extrapolate(h->phi, h->phi_prev, h->phi_prev2, h->n_nodes, std::min(kExtrapOrder, h->phi_hist - 1),
+                           h->stream);
+        h->launches += 1;
+        h->phi_hist++;
+    }
+    const bool prev = h->in_run;
+    h->in_run = true;
+    const int rc = do_solve(h);
+    h->in_run = prev;
+    return rc;
+}
+}  // namespace
+
 int spg_gather(spg_handle *h, double *rho_out) {
     if (!h) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
-    int rc = do_gather(h);
+    int rc = h->have_particles ? maybe_resort(h) : SPG_OK;
+    if (rc) return rc;
+    rc = do_gather(h);
     if (rc) return rc;
     if (rho_out) {
         launch_node_rho(h->node_q, h->dual_vol, h->rho, h->n_nodes, h->stream);
@@ -1726,27 +1763,45 @@ int spg_gather(spg_handle *h, double *rho_out) {
     return SPG_OK;
 }
 
-namespace {
-__attribute__((unused)) void node_q_from_rho_host(const std::vector<double> &rho, const std::vector<double> &dv,
-                                                  std::vector<double> &q) {
-    q.resize(rho.size());
-    for (size_t i = 0; i < rho.size(); ++i) q[i] = rho[i] * dv[i];
+int spg_get_charge_density(spg_handle *h, double *rho_out) {
+    if (!h || !rho_out) return SPG_E_INVALID;
+    if (!h->charge_valid) return fail(h, SPG_E_STATE, "get_charge_density: no deposit or given density yet");
+    CK(cudaSetDevice(h->device));
+    launch_node_rho(h->node_q, h->dual_vol, h->rho, h->n_nodes, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rho_out, h->rho, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SPG_OK;
 }
-}  // namespace
 
 int spg_solve(spg_handle *h, const double *rho_or_null, double *phi_out, int32_t *iters, double *relres) {
     if (!h) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
-    h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
-    if (rho_or_null) {
-        std::vector<double> dv(h->n_nodes), q;
-        CK(cudaMemcpy(dv.data(), h->dual_vol, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToHost));
-        node_q_from_rho_host(std::vector<double>(rho_or_null, rho_or_null + h->n_nodes), dv, q);
-        CK(cudaMemcpyAsync(h->node_q, q.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
-        CK(cudaStreamSynchronize(h->stream));
-        h->charge_valid = true;
+    int rc;
+    if (!rho_or_null && h->occ_fresh) {
+        // The solve of this handle's own deposit, with no particle moved since
+        // (the gather -> solve of the reference's time loop): the same solve
+        // spg_run makes, with the extrapolated initial guess and the field of
+        // the occupied tets only.
+        rc = solve_run_deposit(h);
+    } else {
+        h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
+        if (rho_or_null) {
+            // the density goes up once; the node charges are formed on the device
+            CK(cudaMemcpyAsync(h->rho, rho_or_null, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice,
+                               h->stream));
+            launch_node_q_from_rho(h->rho, h->dual_vol, h->node_q, h->n_nodes, h->stream);
+            CK(cudaGetLastError());
+            h->charge_valid = true;
+        }
+        // while the deposit's list of occupied tets still holds every
+        // particle, the field of those tets is enough (the walks compute the
+        // tets particles enter)
+        const bool prev = h->in_run;
+        h->in_run = h->occ_fresh;
+        rc = do_solve(h);
+        h->in_run = prev;
     }
-    int rc = do_solve(h);
     if (iters) *iters = h->cg_iters_last;
     if (relres) *relres = h->cg_relres_last;
     if (rc && rc != SPG_E_NOT_CONVERGED) return rc;
@@ -1763,7 +1818,9 @@ int spg_process(spg_handle *h, int32_t nsteps, spg_stats *stats) {
     if (nsteps < 0) return fail(h, SPG_E_INVALID, "process: nsteps < 0");
     CK(cudaSetDevice(h->device));
     for (int32_t k = 0; k < nsteps; ++k) {
-        int rc = do_process(h);
+        int rc = maybe_resort(h);
+        if (rc) return rc;
+        rc = do_process(h);
         if (rc) return rc;
     }
     return fill_stats(h, stats);
@@ -1781,22 +1838,12 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
     } in_run(h);
     int status = SPG_OK;
     for (int32_t k = 0; k < nsteps; ++k) {
-        int rc;
-        if (h->prm.resort_every > 0 && h->step % h->prm.resort_every == 0) {
-            rc = do_resort(h);
-            if (rc) return rc;
-        }
+        int rc = maybe_resort(h);
+        if (rc) return rc;
         if (h->step % h->prm.poisson_every == 0) {
             rc = do_gather(h);
             if (rc) return rc;
-            if (h->amg || h->amg32) {
-                // initial guess: extrapolation of the last run solves
-                launch_extrapolate(h->phi, h->phi_prev, h->phi_prev2, h->n_nodes,
-                                   std::min(kExtrapOrder, h->phi_hist - 1), h->stream);
-                h->launches += 1;
-                h->phi_hist++;
-            }
-            rc = do_solve(h);
+            rc = solve_run_deposit(h);
             if (rc == SPG_E_NOT_CONVERGED)
                 status = rc;
             else if (rc)
@@ -2007,6 +2054,25 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
         return fail(h, SPG_E_INVALID, "restore: corrupt header");
     const int64_t n = hd.np;
     if (bytes < ckpt_bytes_for(h, n)) return fail(h, SPG_E_INVALID, "restore: buffer too small");
+    {
+        // The particle downloads address particles through the slot of their
+        // id, so a blob whose ids are not a permutation of 0..np-1, or whose
+        // tets are out of range, is refused before anything is copied.
+        const size_t es = h->mixed ? 4 : 8;
+        const char *tp = static_cast<const char *>(buf) + sizeof(hd) + 6 * es * size_t(n);
+        const char *ip = tp + 4 * size_t(n);
+        std::vector<uint8_t> seen(size_t(n), 0);
+        for (int64_t i = 0; i < n; ++i) {
+            int32_t t;
+            uint32_t idf;
+            std::memcpy(&t, tp + 4 * i, 4);
+            std::memcpy(&idf, ip + 4 * i, 4);
+            const uint32_t id = idf & kIdMask;
+            if (t < -1 || t >= h->n_tets || int64_t(id) >= n || seen[id])
+                return fail(h, SPG_E_INVALID, "restore: particle ids or tets are corrupt");
+            seen[id] = 1;
+        }
+    }
     CK(cudaSetDevice(h->device));
     free_tracks(h);  // slots and particle count may change
     {
@@ -2043,6 +2109,8 @@ int spg_restore(spg_handle *h, const void *buf, size_t bytes) {
     h->cg_solves = hd.cg_solves;
     h->cg_relres_last = hd.cg_relres_last;
     h->have_particles = true;
+    h->occ_fresh = false;
+    h->resorted_at = -1;
     if (h->cg_solves == 0) {
         zero_field(h);
     } else {
@@ -2191,6 +2259,7 @@ int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, co
     int rc;
     const int nck = (nsteps + checkpoint_every - 1) / checkpoint_every;
     h->grad_ready = false;
+    h->occ_fresh = false;
     const size_t have = h->mixed ? h->ckpt32.size() : h->ckpt.size();
     if (int(have) < nck || n > h->ckpt_cap) {
         free_particle_set(h->ckpt);
@@ -2270,6 +2339,7 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
     const int W = h->grad_every;
     cudaStream_t s = h->stream;
     int rc;
+    h->occ_fresh = false;
     const int64_t hneed = int64_t(W) * std::max<int64_t>(n, 1);
     if (hneed > h->hist_cap) {
         for (void *q : {(void *)h->hist.tet, (void *)h->hist.vx, (void *)h->hist.vy, (void *)h->hist.vz}) cudaFree(q);

@@ -638,10 +638,13 @@ __global__ void k_init_particles(const double *__restrict__ pos, const double *_
     p.idf[j] = uint32_t(j) | (t < 0 ? kLost : 0u);
 }
 
-// Slot of each particle id (the ids are a permutation of 0..n-1).
+// Slot of each particle id. The ids are a permutation of 0..n-1 (set, inject
+// and restore keep it so); an id out of range is not written.
 __global__ void k_slot_of_id(const uint32_t *__restrict__ idf, int64_t n, int32_t *__restrict__ slot) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n) slot[idf[i] & kIdMask] = int32_t(i);
+    if (i >= n) return;
+    const uint32_t id = idf[i] & kIdMask;
+    if (int64_t(id) < n) slot[id] = int32_t(i);
 }
 
 // One thread per id: scattered reads of its slot, coalesced writes in id

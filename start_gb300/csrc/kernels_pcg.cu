@@ -96,6 +96,14 @@ __global__ void k_node_rho(const double *__restrict__ node_q, const double *__re
     rho[i] = node_q[i] / dual_vol[i];
 }
 
+// Charge of each node from a given nodal density: q = rho V_dual.
+__global__ void k_node_q_from_rho(const double *__restrict__ rho, const double *__restrict__ dual_vol,
+                                  double *__restrict__ node_q, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    node_q[i] = rho[i] * dual_vol[i];
+}
+
 // r = b - A x, z = D^-1 r, p = z; rz = r.z, bb = b.b, rr = r.r
 __global__ void __launch_bounds__(kThreads) k_setup(PcgDev d, const double *__restrict__ b) {
     double rz = 0.0, bb = 0.0;
@@ -468,6 +476,10 @@ void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, c
 
 void launch_node_rho(const double *node_q, const double *dual_vol, double *rho, int64_t n, cudaStream_t s) {
     k_node_rho<<<unsigned((n + 255) / 256), 256, 0, s>>>(node_q, dual_vol, rho, n);
+}
+
+void launch_node_q_from_rho(const double *rho, const double *dual_vol, double *node_q, int64_t n, cudaStream_t s) {
+    if (n > 0) k_node_q_from_rho<<<unsigned((n + 255) / 256), 256, 0, s>>>(rho, dual_vol, node_q, n);
 }
 
 void launch_pcg_setup(const PcgDev &d, const double *b, cudaStream_t s) {

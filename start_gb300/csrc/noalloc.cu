@@ -96,12 +96,23 @@ __device__ __forceinline__ double na_row(const NaArgs &a, const double *__restri
 }
 
 // Jacobi inverse diagonal, r = b - A x, z = D^-1 r, p = z; rz, bb; then rr.
+// A row without a stored diagonal, or with a zero or non-finite one, sets
+// bit 0 of sc->flags and the host refuses the solve.
 __global__ void __launch_bounds__(kNaThreads) k_na_setup(NaArgs a) {
     double rz = 0.0, bb = 0.0;
+    bool bad = false;
     for (int64_t i = int64_t(blockIdx.x) * kNaThreads + threadIdx.x; i < a.n; i += int64_t(gridDim.x) * kNaThreads) {
-        double d = 1.0;
+        double d = 0.0;
+        bool found = false;
         for (int32_t k = a.row_ptr[i]; k < a.row_ptr[i + 1]; ++k)
-            if (a.col[k] == i) d = a.val[k];
+            if (a.col[k] == i) {
+                d = a.val[k];
+                found = true;
+            }
+        if (!found || !(fabs(d) > 0.0) || !isfinite(d)) {
+            bad = true;
+            d = 1.0;
+        }
         const double di = 1.0 / d;
         const double ri = a.b[i] - na_row(a, a.x, i);
         const double zi = ri * di;
@@ -112,6 +123,7 @@ __global__ void __launch_bounds__(kNaThreads) k_na_setup(NaArgs a) {
         rz += ri * zi;
         bb += a.b[i] * a.b[i];
     }
+    if (bad) atomicOr(&a.sc->flags, 1);
     double tot[2];
     if (na_reduce2(rz, bb, a.partials, a.sc, tot)) {
         a.sc->rz = tot[0];
@@ -148,7 +160,7 @@ __global__ void __launch_bounds__(kNaThreads) k_na_spmv_dot(NaArgs a) {
             a.sc->alpha = a.sc->rz / tot[0];
         } else {
             a.sc->alpha = 0.0;
-            a.sc->converged = 2;
+            a.sc->converged = 3;  // breakdown: p.Aq <= 0 (A not SPD on this subspace, or NaN)
         }
     }
 }
@@ -180,6 +192,13 @@ __global__ void __launch_bounds__(kNaThreads) k_na_update(NaArgs a) {
             sc->rz = tot[0];
         }
     }
+}
+
+// b = 0: the solution is x = 0 whatever the initial guess.
+__global__ void __launch_bounds__(kNaThreads) k_na_zero_x(NaArgs a) {
+    if (a.sc->bb != 0.0) return;
+    for (int64_t i = int64_t(blockIdx.x) * kNaThreads + threadIdx.x; i < a.n; i += int64_t(gridDim.x) * kNaThreads)
+        a.x[i] = 0.0;
 }
 
 __global__ void __launch_bounds__(kNaThreads) k_na_pupdate(NaArgs a) {
@@ -261,11 +280,15 @@ extern "C" int spg_pcg_solve_noalloc(int64_t n, const int32_t *row_ptr, const in
     const unsigned blocks = unsigned(want < kNaMaxBlocks ? want : kNaMaxBlocks);
     k_na_setup<<<blocks, kNaThreads, 0, s>>>(a);
     k_na_rr<<<blocks, kNaThreads, 0, s>>>(a);
+    k_na_zero_x<<<blocks, kNaThreads, 0, s>>>(a);
     PcgScalars hs;
     for (;;) {
         e = cudaMemcpyAsync(&hs, a.sc, sizeof(hs), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return na_fail(SPG_E_CUDA, std::string("PCG: ") + cudaGetErrorString(e));
+        if (hs.flags)
+            return na_fail(SPG_E_INVALID,
+                           "spg_pcg_solve_noalloc: a row has no stored diagonal entry, or a zero or non-finite one");
         if (hs.converged) break;
         for (int k = 0; k < kNaChunk; ++k) {
             k_na_spmv_dot<<<blocks, kNaThreads, 0, s>>>(a);
@@ -279,5 +302,9 @@ extern "C" int spg_pcg_solve_noalloc(int64_t n, const int32_t *row_ptr, const in
     if (relres) *relres = hs.bb > 0.0 ? std::sqrt(hs.rr / hs.bb) : 0.0;
     if (hs.converged == 2)
         return na_fail(SPG_E_NOT_CONVERGED, "spg_pcg_solve_noalloc: PCG did not converge within max_iter");
+    if (hs.converged == 3)
+        return na_fail(SPG_E_NOT_CONVERGED,
+                       "spg_pcg_solve_noalloc: CG breakdown (p.Ap <= 0 after " + std::to_string(hs.iters) +
+                           " iterations): the matrix is not SPD, or the data hold NaN");
     return SPG_OK;
 }

@@ -322,7 +322,7 @@ size_t walk_item32_bytes();
 // tol2 is set to rtol^2 by the host and scaled by ||b||^2 in the setup kernel.
 struct PcgScalars {
     double rz, pq, alpha, beta, rr, bb, tol2;
-    int32_t iters, converged, max_iter, pad;
+    int32_t iters, converged, max_iter, flags;  // flags: bad-diagonal mark of the allocation-free solve
     unsigned int ticket;
     unsigned int pad2;
 };
@@ -495,5 +495,7 @@ void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, c
 void launch_pcg_setup(const PcgDev &d, const double *b, cudaStream_t s);
 void launch_pcg_iteration(PcgDev &d, cudaStream_t s);
 void launch_node_rho(const double *node_q, const double *dual_vol, double *rho, int64_t n, cudaStream_t s);
+// node_q = rho * dual_vol (a density given by the caller)
+void launch_node_q_from_rho(const double *rho, const double *dual_vol, double *node_q, int64_t n, cudaStream_t s);
 
 }  // namespace spg

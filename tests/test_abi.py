@@ -97,18 +97,17 @@ def test_struct_layouts_match_header(built):
                      C.sizeof(N.Source)]
 
 
-def test_cpp_shim_compiles():
-    """The reference-named C++ shim (include/start_pic.hpp) compiles against the ABI."""
+def test_cpp_shim_compiles(built):
+    """The reference-named C++ shim (include/start_pic.hpp) and the time-loop
+    driver written against it compile and link against libstart_gpu.so (the
+    GPU test test_gpu_cpp_shim.py runs the same driver)."""
     import subprocess
     import tempfile
 
-    src = r'''
-    #include "start_pic.hpp"
-    int main() {
-      start::ParticleInCellEngine* e = nullptr; (void)e;
-      return 0; }
-    '''
+    lib, _ = built
+    src = ROOT / "tests" / "native" / "pic_loop_driver.cpp"
     with tempfile.TemporaryDirectory() as d:
-        c = Path(d) / "probe.cpp"
-        c.write_text(src)
-        subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), str(c)], check=True)
+        exe = Path(d) / "pic_loop_driver"
+        subprocess.run(["g++", "-std=c++17", "-O0", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"), str(src),
+                        "-L", str(lib.parent), "-lstart_gpu", f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+        assert exe.exists()

@@ -242,6 +242,41 @@ def test_checkpoint_restore_is_exact(libs, precond):
     assert np.array_equal(ca, g.triangle_counts())
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_restore_refuses_corrupt_particles(libs, precision):
+    """A checkpoint whose particle ids are not a permutation of 0..np-1, or
+    whose tets are out of range, is refused before anything is copied: the
+    handle keeps its state and a good blob still restores."""
+    from start_gb300 import StartPIC
+    from start_gb300.engine import PICBaseException
+
+    w = _w0(n=3000, steps=10, precision=precision)
+    g = StartPIC(w.mesh, w.params)
+    g.set_particles(w.pos, w.vel)
+    g.run(5)
+    blob = g.checkpoint()
+    before = g.particles()
+    n, es, hdr = 3000, (4 if precision else 8), 104  # CkptHeader: 13 words of 8 B
+    tet_off = hdr + 6 * es * n
+    idf_off = tet_off + 4 * n
+    ids = np.frombuffer(blob, np.uint32, n, idf_off)
+    dup = bytearray(blob)
+    dup[idf_off + 4 * 7: idf_off + 4 * 8] = ids[3:4].tobytes()  # two particles with one id
+    big = bytearray(blob)
+    big[idf_off: idf_off + 4] = np.uint32(n + 5).tobytes()  # id beyond np
+    bad_tet = bytearray(blob)
+    bad_tet[tet_off: tet_off + 4] = np.int32(g.n_tets).tobytes()
+    for b in (dup, big, bad_tet):
+        with pytest.raises(PICBaseException):
+            g.restore(bytes(b))
+    after = g.particles()
+    for k in before:
+        assert np.array_equal(before[k], after[k])
+    g.restore(blob)
+    g.run(5)
+    g.close()
+
+
 def test_edge_cases(libs):
     from start_gb300 import StartPIC
     from start_gb300.engine import PICBaseException
