@@ -69,6 +69,7 @@ def load(path: str | Path | None = None):
         "spo_collision_probability": (C.c_double, [C.POINTER(N.Params), _pd]),
         "spo_tet_map": (C.c_double, [_pd, _pd, _pd, _pd, _pd]),
         "spo_philox": (None, [_pu32, _pu32, _pu32]),
+        "spo_set_ref_compat": (C.c_int, [_H, C.c_uint32, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -102,6 +103,18 @@ def params_struct(params):
     for k, v in defaults.items():
         setattr(p, k, v)
     return p
+
+
+# Reference-behaviour switches of the oracle (pic_oracle.h, SPO_COMPAT_*): each
+# reproduces one behaviour of the reference's own loop that the build changes.
+PUSH_NEVER = 1          # src/Particle/Particle.cpp:113-155, src/Geometry/Mesh/Cubic/CubicGrid.cpp:149-158
+E_SIGN_SCALE = 2        # src/Geometry/Mesh/Volumetric/VolumetricMesh.cpp:371-375,398
+RHS_RAW_RHO = 4         # src/ParticleInCellEngine/ChargeDensityEquationSolver.cpp:17-29
+DEPOSIT_VOLAVG = 8      # src/ParticleInCellEngine/NodeChargeDensityProcessor.cpp:25-113
+CLOSED_TETS = 16        # src/Geometry/Mesh/Volumetric/VolumetricMesh.cpp:23-33
+SOLVE_EVERY_STEP = 32   # src/ModelingMainDriver.cpp:146-161
+MIXED_UNITS = 64        # src/Particle/Particle.cpp:157-165
+REFERENCE_LOOP = 127    # all of them: the reference's own time loop
 
 
 class Oracle:
@@ -218,6 +231,14 @@ class Oracle:
         phi = np.empty(self.n_nodes)
         self.lib.spo_get_potential(self.h, _ptr(phi, C.c_double))
         return phi
+
+    def set_ref_compat(self, flags, cubature_w0=1.0 / 6.0):
+        """Turns on reference-behaviour switches (PUSH_NEVER, ...); cubature_w0
+        is the weight of cubature point 0 that E_SIGN_SCALE multiplies in
+        (1/6 for the one-point rule on the unit tet)."""
+        rc = self.lib.spo_set_ref_compat(self.h, int(flags), float(cubature_w0))
+        if rc != 0:
+            raise ValueError(self.lib.spo_last_error().decode())
 
     def set_potential(self, phi):
         phi = np.ascontiguousarray(phi, np.float64)

@@ -158,6 +158,13 @@ struct spo_handle {
     // field-cell freezing for spo_grad (0 off, 1 record, 2 replay)
     int freeze = 0;
     std::vector<int32_t> frozen;
+    // reference-behaviour switches (SPO_COMPAT_*), off by default
+    uint32_t compat = 0;
+    double cubature_w0 = 1.0 / 6.0;
+    std::vector<int64_t> nt_start;   // node -> incident tets, CSR, ascending tet id
+    std::vector<int32_t> nt_tets;
+    std::vector<double> rho_map;     // NodeChargeDensitiesMap of the volume-average deposit
+    std::vector<uint8_t> rho_has;    // node has an entry in that map
 };
 
 namespace {
@@ -316,16 +323,22 @@ StepOut step_particle(spo_handle &h, const CollConst &cc, int64_t i, int32_t ece
     const int32_t t = h.pt[i];
     const Tet &T = h.tet[ecell >= 0 ? ecell : t];
     // 4. push: a = qE/m; v- = v + a dt/2; (rotation = identity for B = 0); v = v+ + a dt/2
-    if (!(T.E[0] == 0.0 && T.E[1] == 0.0 && T.E[2] == 0.0)) {
+    // SPO_COMPAT_PUSH_NEVER: the reference finds the pushing tet by particle id
+    // in the tracker filled by gather, whose entries are copies with new ids
+    // (Particle.cpp:113-155, CubicGrid.cpp:149-158), so it never pushes.
+    if (!(h.compat & SPO_COMPAT_PUSH_NEVER) && !(T.E[0] == 0.0 && T.E[1] == 0.0 && T.E[2] == 0.0)) {
         for (int k = 0; k < 3; ++k) {
             const double a = (p.charge * T.E[k]) / p.mass;
             const double half = (a * p.dt) / 2.0;
             v[k] = (v[k] + half) + half;
         }
     }
-    // 6. move
+    // 6. move. SPO_COMPAT_MIXED_UNITS: the reference adds v dt in metres to
+    // coordinates in millimetres (Particle.cpp:157-165), a displacement of
+    // v dt / 1000 in SI.
     const double p0[3] = {x[0], x[1], x[2]};
-    const double p1[3] = {x[0] + v[0] * p.dt, x[1] + v[1] * p.dt, x[2] + v[2] * p.dt};
+    const double dtm = (h.compat & SPO_COMPAT_MIXED_UNITS) ? p.dt * 1e-3 : p.dt;
+    const double p1[3] = {x[0] + v[0] * dtm, x[1] + v[1] * dtm, x[2] + v[2] * dtm};
     if (p1[0] == p0[0] && p1[1] == p0[1] && p1[2] == p0[2]) return o;  // degenerate segment
     // 7. gas collision
     if (p.collision_model != SPG_COLL_NONE) {
@@ -465,16 +478,90 @@ int pcg(spo_handle &h, const std::vector<double> &b, int32_t *iters, double *rel
 }
 
 void compute_E(spo_handle &h) {
+    const bool ref = h.compat & SPO_COMPAT_E_SIGN_SCALE;
     for (int64_t t = 0; t < h.Nt; ++t) {
         const int32_t *n = &h.tn[4 * t];
         const double d1 = h.phi[n[1]] - h.phi[n[0]], d2 = h.phi[n[2]] - h.phi[n[0]], d3 = h.phi[n[3]] - h.phi[n[0]];
         Tet &T = h.tet[t];
-        for (int k = 0; k < 3; ++k) T.E[k] = -((d1 * T.M[k] + d2 * T.M[3 + k]) + d3 * T.M[6 + k]);
+        if (ref) {
+            // VolumetricMesh.cpp:371-375,398: E = + sum phi_i grad(N_i) |det J| w0,
+            // the basis gradients weighted by the measure of cubature point 0
+            const double meas = (6.0 * h.vol[t]) * h.cubature_w0;
+            for (int k = 0; k < 3; ++k) T.E[k] = ((d1 * T.M[k] + d2 * T.M[3 + k]) + d3 * T.M[6 + k]) * meas;
+        } else {
+            for (int k = 0; k < 3; ++k) T.E[k] = -((d1 * T.M[k] + d2 * T.M[3 + k]) + d3 * T.M[6 + k]);
+        }
     }
     h.have_E = true;
 }
 
+// All tets whose closed cell holds p (a point on a face, edge or vertex lies
+// in every tet sharing it), from the location grid.
+void tets_containing(const spo_handle &h, const double p[3], std::vector<int32_t> &out) {
+    out.clear();
+    int c[3];
+    for (int k = 0; k < 3; ++k) {
+        const double u = (p[k] - h.go[k]) / h.gh[k];
+        if (!(u >= 0.0) || u >= double(h.gd[k]) + 1e-9) return;
+        c[k] = std::min(h.gd[k] - 1, int(u));
+    }
+    const int64_t cell = c[0] + int64_t(h.gd[0]) * (c[1] + int64_t(h.gd[1]) * c[2]);
+    for (int64_t k = h.gstart[cell]; k < h.gstart[cell + 1]; ++k) {
+        const int32_t t = h.glist[k];
+        double l[4];
+        bary(h.tet[t], p, l);
+        if (l[0] >= 0.0 && l[1] >= 0.0 && l[2] >= 0.0 && l[3] >= 0.0) out.push_back(t);
+    }
+    std::sort(out.begin(), out.end());
+}
+
+// SPO_COMPAT_DEPOSIT_VOLAVG: NodeChargeDensityProcessor.cpp:25-113 with one
+// chunk (the single-thread std path). The charge of each tet's particles over
+// its volume, rho_t = sum q / V_t; then per node the volume average over its
+// occupied tets, rho_n = sum rho_t V_t / sum V_t, written into a map that
+// lives as long as the run (ModelingMainDriver.cpp:122): a node with no
+// occupied tet keeps its last density. The particle's tet is its walk tet, or
+// with SPO_COMPAT_CLOSED_TETS every tet whose closed cell holds it
+// (VolumetricMesh.cpp:23-33; no break at NodeChargeDensityProcessor.cpp:52-55).
+void deposit_volavg(spo_handle &h) {
+    const double wq = h.prm.weight * h.prm.charge;
+    std::vector<double> tq(h.Nt, 0.0);
+    std::vector<uint8_t> occ(h.Nt, 0);
+    std::vector<int32_t> hold;
+    for (int64_t i = 0; i < h.np; ++i) {
+        if (h.fl[i] & (FLAG_SETTLED | FLAG_LOST)) continue;
+        if (h.compat & SPO_COMPAT_CLOSED_TETS) {
+            tets_containing(h, &h.x[3 * i], hold);
+        } else {
+            hold.assign(1, h.pt[i]);
+        }
+        for (int32_t t : hold) {
+            tq[t] += wq;
+            occ[t] = 1;
+        }
+    }
+    for (int64_t n = 0; n < h.Nn; ++n) {
+        double charge = 0.0, volume = 0.0;
+        for (int64_t k = h.nt_start[n]; k < h.nt_start[n + 1]; ++k) {
+            const int32_t t = h.nt_tets[k];
+            if (!occ[t]) continue;
+            const double rho_t = tq[t] / h.vol[t];
+            charge += rho_t * h.vol[t];
+            volume += h.vol[t];
+        }
+        if (volume > 0.0) {
+            h.rho_map[n] = charge / volume;
+            h.rho_has[n] = 1;
+        }
+    }
+    for (int64_t n = 0; n < h.Nn; ++n) h.node_q[n] = h.rho_has[n] ? h.rho_map[n] * h.dual[n] : 0.0;
+}
+
 void deposit(spo_handle &h) {
+    if (h.compat & SPO_COMPAT_DEPOSIT_VOLAVG) {
+        deposit_volavg(h);
+        return;
+    }
     std::fill(h.node_q.begin(), h.node_q.end(), 0.0);
     const double wq = h.prm.weight * h.prm.charge;
     for (int64_t i = 0; i < h.np; ++i) {
@@ -489,7 +576,18 @@ void deposit(spo_handle &h) {
 int solve_current(spo_handle &h) {
     std::vector<double> b(h.Nn);
     const double inv_eps0 = 1.0 / h.prm.epsilon0;
-    for (int64_t i = 0; i < h.Nn; ++i) b[i] = h.isd[i] ? h.gval[i] : h.node_q[i] * inv_eps0 - h.lift[i];
+    if (h.compat & SPO_COMPAT_RHS_RAW_RHO) {
+        // ChargeDensityEquationSolver.cpp:17-29 and VectorBoundaryConditionsManager.cpp:29-43:
+        // b_i = rho_i (no eps0, no volume) at the free nodes, b_i = V at the
+        // Dirichlet nodes, whose rows are identity rows with their columns kept
+        // (MatrixBoundaryConditionsManager.cpp): the same solution as moving
+        // K_FD g to the right-hand side. A new solver per call starts from
+        // x = 0 (MatrixEquationSolver.cpp:5-11).
+        for (int64_t i = 0; i < h.Nn; ++i) b[i] = h.isd[i] ? h.gval[i] : h.node_q[i] / h.dual[i] - h.lift[i];
+        std::fill(h.phi.begin(), h.phi.end(), 0.0);
+    } else {
+        for (int64_t i = 0; i < h.Nn; ++i) b[i] = h.isd[i] ? h.gval[i] : h.node_q[i] * inv_eps0 - h.lift[i];
+    }
     int32_t it = 0;
     double rr = 0.0;
     const int rc = pcg(h, b, &it, &rr);
@@ -636,11 +734,16 @@ int spo_create(const spg_mesh_desc *d, const spg_params *prm, spo_handle **out) 
     for (int64_t t = 0; t < h->Nt; ++t)
         for (int k = 0; k < 4; ++k) inc[h->tn[4 * t + k]].push_back(int32_t(4 * t + k));
     h->dual.assign(h->Nn, 0.0);
+    h->nt_start.assign(h->Nn + 1, 0);
     for (int64_t n = 0; n < h->Nn; ++n) {
         double s = 0.0;
         for (int32_t e : inc[n]) s += h->vol[e >> 2];
         h->dual[n] = 0.25 * s;
+        h->nt_start[n + 1] = h->nt_start[n] + int64_t(inc[n].size());
     }
+    h->nt_tets.resize(size_t(h->nt_start[h->Nn]));
+    for (int64_t n = 0; n < h->Nn; ++n)
+        for (size_t k = 0; k < inc[n].size(); ++k) h->nt_tets[size_t(h->nt_start[n]) + k] = inc[n][k] >> 2;
     h->rp.assign(h->Nn + 1, 0);
     std::vector<std::map<int32_t, double>> rows(h->Nn);
     h->lift.assign(h->Nn, 0.0);
@@ -845,7 +948,9 @@ int spo_process_range(spo_handle *h, int64_t first, int64_t count) {
 int spo_run(spo_handle *h, int32_t nsteps) {
     int status = SPG_OK;
     for (int32_t s = 0; s < nsteps; ++s) {
-        if (h->step % h->prm.poisson_every == 0) {
+        // SPO_COMPAT_SOLVE_EVERY_STEP: gather and solve at every time moment
+        // (ModelingMainDriver.cpp:146-161)
+        if (h->step % h->prm.poisson_every == 0 || (h->compat & SPO_COMPAT_SOLVE_EVERY_STEP)) {
             deposit(*h);
             const int rc = solve_current(*h);
             if (rc) status = rc;
@@ -1182,5 +1287,17 @@ double spo_tet_map(const double *x0, const double *x1, const double *x2, const d
 }
 
 void spo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox(ctr, key, out); }
+
+int spo_set_ref_compat(spo_handle *h, uint32_t flags, double cubature_w0) {
+    if (!h) return fail(SPG_E_INVALID, "null handle");
+    if (flags & ~uint32_t(SPO_COMPAT_ALL)) return fail(SPG_E_INVALID, "unknown compat flag");
+    if (!(cubature_w0 > 0.0)) return fail(SPG_E_INVALID, "cubature_w0 must be > 0");
+    h->compat = flags;
+    h->cubature_w0 = cubature_w0;
+    h->rho_map.assign(h->Nn, 0.0);
+    h->rho_has.assign(h->Nn, 0);
+    if (h->have_E) compute_E(*h);
+    return SPG_OK;
+}
 
 }  // extern "C"

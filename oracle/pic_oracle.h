@@ -65,6 +65,43 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
  * cells in later calls (the walk, landing and collisions stay live), 0 off. */
 int spo_grad_freeze(spo_handle *h, int mode);
 
+/* Reference-behaviour switches: each reproduces one behaviour of the
+ * reference's own loop that the build changes on purpose. All off by default.
+ *   PUSH_NEVER        no electromagnetic push: the pushing tet is looked up by
+ *                     particle id among tracker copies that carry new ids
+ *                     (src/Particle/Particle.cpp:113-155,
+ *                     src/Geometry/Mesh/Cubic/CubicGrid.cpp:149-158)
+ *   E_SIGN_SCALE      E = + sum phi_i grad(N_i) |det J| w0 per tet, w0 the
+ *                     weight of cubature point 0
+ *                     (src/Geometry/Mesh/Volumetric/VolumetricMesh.cpp:371-375,398)
+ *   RHS_RAW_RHO       right-hand side = nodal density itself (no eps0, no
+ *                     volume), solve from x = 0 every call
+ *                     (src/ParticleInCellEngine/ChargeDensityEquationSolver.cpp:17-29,
+ *                     src/FiniteElementMethod/Solvers/MatrixEquationSolver.cpp:5-11)
+ *   DEPOSIT_VOLAVG    per-tet density, then the volume average over each
+ *                     node's occupied tets into a map kept across steps
+ *                     (src/ParticleInCellEngine/NodeChargeDensityProcessor.cpp:25-113,
+ *                     one chunk: the single-thread semantics)
+ *   CLOSED_TETS       with DEPOSIT_VOLAVG, a particle on a shared face, edge or
+ *                     vertex counts in every tet holding it
+ *                     (VolumetricMesh.cpp:23-33, NodeChargeDensityProcessor.cpp:52-55)
+ *   SOLVE_EVERY_STEP  gather + solve at every step (src/ModelingMainDriver.cpp:146-161)
+ *   MIXED_UNITS       displacement v dt / 1000: metres added to millimetre
+ *                     coordinates (src/Particle/Particle.cpp:157-165) */
+enum {
+    SPO_COMPAT_PUSH_NEVER = 1,
+    SPO_COMPAT_E_SIGN_SCALE = 2,
+    SPO_COMPAT_RHS_RAW_RHO = 4,
+    SPO_COMPAT_DEPOSIT_VOLAVG = 8,
+    SPO_COMPAT_CLOSED_TETS = 16,
+    SPO_COMPAT_SOLVE_EVERY_STEP = 32,
+    SPO_COMPAT_MIXED_UNITS = 64,
+    SPO_COMPAT_ALL = 127
+};
+/* Sets the switches (and the cubature weight for E_SIGN_SCALE, 1/6 for the
+ * one-point rule); clears the volume-average density map. */
+int spo_set_ref_compat(spo_handle *h, uint32_t flags, double cubature_w0);
+
 /* Primitives pinned by the reference's unit tests. */
 void spo_update_position(double *pos3, const double *vel3, double dt);
 /* Segment-triangle intersection: 1 and the point when they meet (a segment
