@@ -186,8 +186,11 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
  * ParticleDynamicUtils.hpp:52-97: points uniform over a disk or a rectangle,
  * directions uniform in a cone or Lambert (cosine) about the normal, energies
  * monoenergetic or Thompson f(E) ~ E/(E+U)^3 truncated at E_max, then the
- * ParticleDisplacer shift (src/Particle/ParticleDisplacer.cpp:20-35):
- * p += d / max|d_k| * displacement. Particle i draws from Philox4x32-10 keyed
+ * ParticleDisplacer shift (src/Particle/ParticleDisplacer.cpp:20-35), the
+ * vector s / max|s_k| * displacement: with the fan law (the reference's point
+ * and surface sources) s is the source's direction or the cell's normal, one
+ * vector for all its particles (:48-133); with the cone and cosine laws s is
+ * each particle's own direction. Particle i draws from Philox4x32-10 keyed
  * by (seed) and counted by (i, block), so a source is reproducible and does
  * not depend on the launch shape. */
 typedef enum spg_source_shape {
@@ -218,7 +221,7 @@ typedef struct spg_source {
     double energy_ev;     /* monoenergetic energy [eV] */
     double binding_ev;    /* Thompson U [eV] */
     double emax_ev;       /* Thompson truncation [eV] */
-    double displacement;  /* shift along the direction [m]; 0.05 mm in the reference */
+    double displacement;  /* largest component of the shift [m]; 0.05 mm in the reference */
     uint64_t seed;
     /* SPG_SRC_CELLS: n_cells cells, cells[6 k .. 6 k + 5] = centre xyz [m], normal xyz (the
      * baseCoordinates of a surface source); host memory, read during the call */

@@ -31,15 +31,23 @@ from .workloads import TI_MASS, _base_params, gas_concentration
 
 class LandingSetup:
     """Geometry, electrodes, parameters and the frozen source uniforms of the
-    landing problem; no device state (the oracle tests reuse it)."""
+    landing problem; no device state (the oracle tests reuse it).
+
+    faces: the box faces (indices into mesh.BOX_FACES) that carry an
+    electrode, one potential each; the other faces are Neumann. With only the
+    two z faces the field is uniform: P1 reproduces the linear potential
+    exactly."""
 
     def __init__(self, n_particles=1_000_000, cells=25, steps=300, seed=1, sigma=0.01, checkpoint_every=32,
-                 collisions=True, energy_ev=1.0, gas_scale=1.0, cg_rtol=1e-12, preconditioner=0, precision=0):
+                 collisions=True, energy_ev=1.0, gas_scale=1.0, cg_rtol=1e-12, preconditioner=0, precision=0,
+                 faces=(0, 1, 2, 3, 4, 5)):
         L = 0.1
         self.mesh = M.kuhn_box((cells,) * 3, (L,) * 3)
+        self.faces = tuple(faces)
         owner = np.full(self.mesh.n_nodes, -1)
         for f, (ax, side) in enumerate(M.BOX_FACES):
-            owner[M.box_face_nodes(self.mesh, ax, side)] = f  # later faces win on shared edges
+            if f in self.faces:
+                owner[M.box_face_nodes(self.mesh, ax, side)] = self.faces.index(f)  # later faces win on edges
         self.owner = owner
         dn = np.nonzero(owner >= 0)[0].astype(np.int32)
         self.mesh.with_dirichlet(dn, np.zeros(len(dn)))
@@ -78,7 +86,7 @@ class LandingSetup:
         return g
 
     def face_sums(self, dJ_dg):
-        return np.array([dJ_dg[self.owner == f].sum() for f in range(6)])
+        return np.array([dJ_dg[self.owner == f].sum() for f in range(len(self.faces))])
 
 
 class LandingProblem(LandingSetup):
@@ -111,14 +119,23 @@ class LandingProblem(LandingSetup):
 
 
 def landing_objective():
-    """torch.autograd.Function over a LandingProblem: params = [V_1..V_6, alpha]."""
+    """torch.autograd.Function over a LandingProblem: params = [V_1..V_k, alpha],
+    one potential per electrode face.
+
+    Its gradient is the pathwise derivative: collision events, random numbers
+    and the cell whose E pushes each particle at each step are held fixed.
+    Where the field is uniform (electrodes on two opposite faces only) it is
+    also the derivative of the live step; with a field that varies from cell to
+    cell, central differences of the live step differ from it by the jumps of
+    the per-cell field (bench.py's grad object records that gap)."""
     import torch
 
     class LandingObjective(torch.autograd.Function):
         @staticmethod
         def forward(ctx, params, problem):
             p = params.detach().cpu().double().numpy()
-            J = problem.forward(p[:6], p[6])
+            nf = len(problem.faces)
+            J = problem.forward(p[:nf], p[nf])
             ctx.problem = problem
             return torch.tensor(J, dtype=params.dtype, device=params.device)
 

@@ -1449,6 +1449,15 @@ void spg_default_source(spg_source *src) {
     src->displacement = 0.05e-3;
 }
 
+namespace {
+// ParticleDisplacer::_calculateDisplacement (src/Particle/ParticleDisplacer.cpp:20-35):
+// dir / max|dir_k| * amount, zero for a direction below machine epsilon.
+void fan_shift(const double dir[3], double amount, double out[3]) {
+    const double m = std::max(std::fabs(dir[0]), std::max(std::fabs(dir[1]), std::fabs(dir[2])));
+    for (int k = 0; k < 3; ++k) out[k] = m < 2.220446049250313e-16 ? 0.0 : (dir[k] / m) * amount;
+}
+}  // namespace
+
 // Validates src and samples n particles with ids id_base .. id_base + n - 1
 // into the device arrays pos, vel (3 n each); tet (n) receives their tets.
 int sample_particles(spg_handle *h, int64_t n, const spg_source *src, int64_t id_base, double *dpos, double *dvel,
@@ -1494,6 +1503,15 @@ int sample_particles(spg_handle *h, int64_t n, const spg_source *src, int64_t id
     c.theta0 = std::acos(std::max(-1.0, std::min(1.0, nv[2])));
     c.phi0 = std::atan2(nv[1], nv[0]);
     c.expansion = src->expansion;
+    {
+        // ParticleDisplacer::displaceParticlesFromPointSources
+        // (src/Particle/ParticleDisplacer.cpp:48-87, :20-35): one shift per
+        // source, along its direction (theta, phi), scaled so that its largest
+        // component is the displacement
+        const double st = std::sin(c.theta0);
+        const double dir[3] = {st * std::cos(c.phi0), st * std::sin(c.phi0), std::cos(c.theta0)};
+        fan_shift(dir, src->displacement, c.fan_shift);
+    }
     c.radius = src->radius;
     c.xlim[0] = src->xlim[0];
     c.xlim[1] = src->xlim[1];
@@ -1517,16 +1535,20 @@ int sample_particles(spg_handle *h, int64_t n, const spg_source *src, int64_t id
         // count splits evenly and the remainder goes one each to cells chosen
         // by a shuffle seeded from the source seed and the first id
         const int k = src->n_cells;
-        std::vector<double> cells(5 * size_t(k));
+        std::vector<double> cells(8 * size_t(k));
         for (int q = 0; q < k; ++q) {
             const double *cc = src->cells + 6 * size_t(q);
             const double m = std::sqrt(cc[3] * cc[3] + cc[4] * cc[4] + cc[5] * cc[5]);
             if (!(m > 0.0)) return fail(h, SPG_E_INVALID, w + ": zero cell normal");
-            cells[5 * q] = cc[0];
-            cells[5 * q + 1] = cc[1];
-            cells[5 * q + 2] = cc[2];
-            cells[5 * q + 3] = std::acos(std::max(-1.0, std::min(1.0, cc[5] / m)));
-            cells[5 * q + 4] = std::atan2(cc[4] / m, cc[3] / m);
+            double *o = cells.data() + 8 * size_t(q);
+            o[0] = cc[0];
+            o[1] = cc[1];
+            o[2] = cc[2];
+            o[3] = std::acos(std::max(-1.0, std::min(1.0, cc[5] / m)));
+            o[4] = std::atan2(cc[4] / m, cc[3] / m);
+            // displaceParticlesFromSurfaceSources (ParticleDisplacer.cpp:90-133):
+            // the cell's normal as given, scaled to the displacement
+            fan_shift(cc + 3, src->displacement, o + 5);
         }
         std::vector<int64_t> count(k, n / k);
         std::vector<int> order(k);

@@ -11,7 +11,10 @@
 //           remainder one each to seed-chosen cells, decided on the host);
 //   fan:    theta = theta0 + (2 u2 - 1) expansion, phi = phi0, about the normal
 //           (theta0, phi0) of the source or of the particle's cell;
-// then the ParticleDisplacer shift p += d / max|d_k| * displacement.
+// then the ParticleDisplacer shift: for the fan law one vector per point
+// source or per cell, along the source's direction or the cell's normal
+// (ParticleDisplacer.cpp:48-133); for the cone and cosine laws
+// p += d / max|d_k| * displacement along the particle's own direction.
 // Particle i takes its uniforms from Philox4x32-10 keyed by the seed and
 // counted by (its id, block, tag), one thread per particle.
 #include <cmath>
@@ -45,6 +48,7 @@ __global__ void k_generate(const __grid_constant__ SourceConst c, int64_t n, dou
     const double u2 = u01_from(r1.v[0], r1.v[1]), u3 = u01_from(r1.v[2], r1.v[3]);
     double p[3];
     double theta0 = c.theta0, phi0 = c.phi0;
+    const double *fan = c.fan_shift;
     if (c.shape == SPG_SRC_CELLS) {
         int lo = 0, hi = c.n_cells - 1;  // the cell with cell_first[k] <= i < cell_first[k + 1]
         while (lo < hi) {
@@ -54,12 +58,13 @@ __global__ void k_generate(const __grid_constant__ SourceConst c, int64_t n, dou
             else
                 hi = mid - 1;
         }
-        const double *cc = c.cells + 5 * lo;
+        const double *cc = c.cells + 8 * lo;
         p[0] = cc[0];
         p[1] = cc[1];
         p[2] = cc[2];
         theta0 = cc[3];
         phi0 = cc[4];
+        fan = cc + 5;
     } else if (c.shape == SPG_SRC_POINT) {
         p[0] = c.centre[0];
         p[1] = c.centre[1];
@@ -103,11 +108,18 @@ __global__ void k_generate(const __grid_constant__ SourceConst c, int64_t n, dou
         const double E = c.binding_j * s / (1.0 - s);
         speed = sqrt(2.0 * E / c.mass);
     }
-    const double m = fmax(fabs(d[0]), fmax(fabs(d[1]), fabs(d[2])));
-    const double shift = m > 2.220446049250313e-16 ? c.displacement / m : 0.0;
-    for (int k = 0; k < 3; ++k) {
-        pos[3 * i + k] = p[k] + d[k] * shift;
-        vel[3 * i + k] = d[k] * speed;
+    if (c.directions == SPG_DIR_FAN) {
+        for (int k = 0; k < 3; ++k) {
+            pos[3 * i + k] = p[k] + fan[k];
+            vel[3 * i + k] = d[k] * speed;
+        }
+    } else {
+        const double m = fmax(fabs(d[0]), fmax(fabs(d[1]), fabs(d[2])));
+        const double shift = m > 2.220446049250313e-16 ? c.displacement / m : 0.0;
+        for (int k = 0; k < 3; ++k) {
+            pos[3 * i + k] = p[k] + d[k] * shift;
+            vel[3 * i + k] = d[k] * speed;
+        }
     }
 }
 

@@ -387,8 +387,10 @@ struct SourceConst {
     int64_t id_base;       // Philox counter of particle i is id_base + i (its particle id)
     double theta0, phi0;   // SPG_DIR_FAN: polar and azimuthal angle of the normal
     double expansion;      // SPG_DIR_FAN: polar spread
-    // SPG_SRC_CELLS: per cell centre xyz, theta0, phi0 (5 doubles), and the
-    // first particle index of each cell (n_cells + 1 prefix offsets)
+    double fan_shift[3];   // SPG_DIR_FAN point source: its one displacement vector
+    // SPG_SRC_CELLS: per cell centre xyz, theta0, phi0 and its displacement
+    // vector (8 doubles), and the first particle index of each cell
+    // (n_cells + 1 prefix offsets)
     int32_t n_cells;
     const double *cells;
     const int64_t *cell_first;

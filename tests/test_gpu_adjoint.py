@@ -130,3 +130,36 @@ def test_fp32_form_gradient_matches_fp64(built, collisions):
     assert abs(n32 - n64) <= 3 and abs(J32 - J64) <= tj * J64, (J32, J64)
     assert np.abs(dV32 - dV64).max() <= tg * np.abs(dV64).max(), (dV32, dV64)
     assert abs(da32 - da64) <= tg * abs(da64), (da32, da64)
+
+
+@pytest.mark.parametrize("collisions", [False, True], ids=["collisionless", "hs"])
+def test_gradient_matches_central_differences_in_a_uniform_field(built, collisions):
+    """GPU-side check against central differences of the GPU's own forward
+    pass. Electrodes on the two z faces only (0 V below, +500 V above; the
+    side faces Neumann): P1 reproduces the linear potential, so E is the same
+    in every tet and the live step has no jump where a push position crosses a
+    cell face. Central differences (h = 1e-3 V, 1e-4 rad) of the live map then
+    equal the pathwise gradient, to 1e-4 relative."""
+    from start_gb300.adjoint import LandingProblem
+
+    p = LandingProblem(n_particles=3000, steps=400, collisions=collisions, cg_rtol=1e-13, faces=(4, 5))
+    p.target = np.array([0.05, 0.05, 0.0])
+    V = np.array([0.0, 500.0])
+    J = p.forward(V, A0)
+    assert p._last[2] >= 2500
+    dV, da, _ = p.backward()
+    E = p.engine.efield()
+    assert np.abs(E - E.mean(axis=0)).max() <= 1e-9 * np.abs(E).max()  # uniform field
+    hv, ha = 1e-3, 1e-4
+    fd = []
+    for f in range(2):
+        e = np.zeros(2)
+        e[f] = hv
+        fd.append((p.forward(V + e, A0) - p.forward(V - e, A0)) / (2 * hv))
+    fd_a = (p.forward(V, A0 + ha) - p.forward(V, A0 - ha)) / (2 * ha)
+    scale = np.abs(dV).max()
+    assert np.abs(np.array(fd) - dV).max() <= 1e-4 * scale, (fd, dV)
+    assert abs(fd_a - da) <= 1e-4 * abs(da), (fd_a, da)
+    assert J > 0.1
+    p.close()
+

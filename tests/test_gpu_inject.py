@@ -2,11 +2,15 @@
 injection (spg_generate_particles / spg_inject_particles):
 
 * a point source with the fan law (ParticleDynamicUtils::calculateVelocityFromEnergy_eV):
-  every particle at the centre plus the displacement, azimuth fixed at the
-  normal's, polar angle uniform in theta0 +- expansion (KS test, p > 1e-3);
+  azimuth fixed at the normal's, polar angle uniform in theta0 +- expansion
+  (KS test, p > 1e-3); every particle at the centre plus one shift along the
+  source's direction (ParticleDisplacer::displaceParticlesFromPointSources),
+  whatever its own direction;
 * a surface-cell source (ParticleGenerator::fromSurfaceSource): the count
   split evenly over the cells, the remainder one each, each particle at its
-  cell's centre moving along the cell normal (expansion 0);
+  cell's centre plus the cell's shift along its normal, bit for bit
+  (displaceParticlesFromSurfaceSources), moving along the cell normal
+  (expansion 0), or spread about it (expansion > 0) with the same shift;
 * injection mid-run (ModelingMainDriver::_spawnParticles): the set grows with
   the next ids, the earlier particles are untouched by the injection, a run
   repeats bit for bit, and tracking continues for the tracked ids."""
@@ -49,9 +53,14 @@ def test_point_source_fan_law(built):
     assert np.allclose(phi, phi0, atol=1e-12)
     assert theta.min() >= th0 - ex - 1e-12 and theta.max() <= th0 + ex + 1e-12
     assert stats.kstest((theta - (th0 - ex)) / (2 * ex), "uniform").pvalue > 1e-3
-    m = np.max(np.abs(d), axis=1, keepdims=True)
-    x0 = p["pos"] - d / m * 0.05e-3
-    assert np.abs(x0 - c).max() <= 1e-15
+    # one shift for the whole source, along its direction (theta0, phi0)
+    assert (p["pos"] == p["pos"][0]).all()
+    s = p["pos"][0] - c
+    dir0 = np.array([np.sin(th0) * np.cos(phi0), np.sin(th0) * np.sin(phi0), np.cos(th0)])
+    assert np.allclose(s, dir0 / np.abs(dir0).max() * 0.05e-3, rtol=1e-12, atol=1e-18)
+    # the particles' own directions spread by +-10 deg: a per-particle shift would differ
+    own = d / np.max(np.abs(d), axis=1, keepdims=True) * 0.05e-3
+    assert np.abs(own - s).max() > 1e-6
     e.close()
 
 
@@ -59,20 +68,24 @@ def test_surface_cells_source(built):
     e = _engine()
     cells = np.array([[0.02, 0.03, 0.0, 0, 0, 1], [0.07, 0.05, 0.0, 0, 0, 2], [0.05, 0.08, 0.0, 1, 0, 1]], float)
     n = 10_001
-    e.generate_particles(n, shape="cells", directions="fan", cells=cells, expansion=0.0, energy_ev=1.0, seed=3)
-    p = e.particles()
-    v = p["vel"]
-    d = v / np.linalg.norm(v, axis=1)[:, None]
-    m = np.max(np.abs(d), axis=1, keepdims=True)
-    x0 = p["pos"] - d / m * 0.05e-3
-    counts = []
-    for c in cells:
-        at = np.all(np.abs(x0 - c[:3]) <= 1e-15, axis=1)
-        nrm = c[3:] / np.linalg.norm(c[3:])
-        assert np.abs(d[at] - nrm).max() <= 1e-12
-        counts.append(int(at.sum()))
-    assert sum(counts) == n
-    assert sorted(counts) == [3333, 3334, 3334]
+    for ex in (0.0, np.deg2rad(20.0)):
+        e.generate_particles(n, shape="cells", directions="fan", cells=cells, expansion=ex, energy_ev=1.0, seed=3)
+        p = e.particles()
+        v = p["vel"]
+        d = v / np.linalg.norm(v, axis=1)[:, None]
+        counts = []
+        for c in cells:
+            # ParticleDisplacer: the cell's normal as given over its largest
+            # component, times 0.05 mm, added to the centre
+            at = np.all(p["pos"] == c[:3] + (c[3:] / np.abs(c[3:]).max()) * 0.05e-3, axis=1)
+            nrm = c[3:] / np.linalg.norm(c[3:])
+            if ex == 0.0:
+                assert np.abs(d[at] - nrm).max() <= 1e-12
+            else:
+                assert np.abs(d[at] - nrm).max() > 0.1  # spread about the normal, same shift
+            counts.append(int(at.sum()))
+        assert sum(counts) == n
+        assert sorted(counts) == [3333, 3334, 3334]
     e.close()
 
 
