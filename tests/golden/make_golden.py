@@ -9,7 +9,11 @@
    collisions. Inputs are stored with the outputs so that the fixtures do not
    depend on the platform's numpy transcendental functions.
 
-Run from the repository root:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Run from the repository root:
+    python tests/golden/make_golden.py REFERENCE_ROOT
+or with REFERENCE_ROOT in the environment variable START_REFERENCE_ROOT. The
+reference tree is needed only for ref_meshes.npz; without one, only the
+oracle fixtures are rewritten.
 """
 from __future__ import annotations
 
@@ -59,9 +63,16 @@ def oracle_case(name, collisions):
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    if ref.exists():
+    import os
+
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("START_REFERENCE_ROOT")
+    if arg:
+        ref = Path(arg)
+        if not (ref / "tests" / "meshes").is_dir():
+            sys.exit(f"{ref} is not a reference tree (no tests/meshes)")
         ref_meshes(ref)
+    else:
+        print("no reference tree given: ref_meshes.npz left as it is")
     oracle_case("collisionless", False)
     oracle_case("hs", True)
     print("written:", sorted(p.name for p in HERE.glob("*.npz")))
