@@ -442,8 +442,10 @@ def e2e_leg(eng, w, steps, reference_calls):
     every = w.params["poisson_every"]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    eng.set_particles(pos_h, vel_h)
+    eng.set_particles(pos_h, vel_h)  # returns after the upload and the location
+    t_up = time.perf_counter()
     s_start = eng.stats()["particle_steps"]
+    t_first = None
     for k in range(steps):
         if reference_calls:
             if k % every == 0:
@@ -452,12 +454,18 @@ def e2e_leg(eng, w, steps, reference_calls):
             st = eng.process(1)  # returns the step's stats (D2H)
         else:
             st = eng.run(1, raise_on_nonconvergence=False)
+        if t_first is None:
+            t_first = time.perf_counter()
         if st["n_alive"] == 0:
             break
+    t_steps = time.perf_counter()
     counts = eng.triangle_counts()
     eng.particles(out=out)  # D2H straight into the pinned arrays
     torch.cuda.synchronize()
-    t = time.perf_counter() - t0
+    t_end = time.perf_counter()
+    t = t_end - t0
+    phases = {"upload_locate_ms": 1e3 * (t_up - t0), "first_step_ms": 1e3 * (t_first - t_up),
+              "other_steps_ms": 1e3 * (t_steps - t_first), "download_ms": 1e3 * (t_end - t_steps)}
     ps = eng.stats()["particle_steps"] - s_start
     h2d = (pos_h.nbytes + vel_h.nbytes) / steps
     d2h = (sum(a.nbytes for a in out.values()) + counts.nbytes) / steps + 96
@@ -465,7 +473,7 @@ def e2e_leg(eng, w, steps, reference_calls):
              "every step; spg_get_triangle_counts, spg_get_particles" if reference_calls else
              "spg_set_particles; spg_run(1) per step; spg_get_triangle_counts, spg_get_particles")
     return {"value": ps / t, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "seconds": t,
-            "calls": calls, "note": "job-level: upload, K steps from step 0 (cold first Poisson solve), "
+            "phases_ms": phases, "calls": calls, "note": "job-level: upload, K steps from step 0 (cold first Poisson solve), "
                                     "per-step stats read, download; host wall clock"}
 
 

@@ -174,7 +174,11 @@ int spg_mesh_info(const spg_handle *h, int64_t info[6]);
 
 /* Uploads particles (SoA-free interleaved xyz). tet may be NULL: the library
  * then locates each particle with a tet walk from a voxel seed; particles
- * outside the mesh are flagged LOST. Resets step, counters and potential. */
+ * outside the mesh are flagged LOST. Resets step, counters and potential: with
+ * an AMG preconditioner the potential restarts from the electrode field (the
+ * potential of the Dirichlet values with no charge, solved in spg_create and
+ * again at the first new particle set after spg_set_dirichlet), otherwise from
+ * the Dirichlet values with zero elsewhere. */
 int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double *vel,
                       const int32_t *tet_or_null);
 /* Any output pointer may be NULL. Arrays are [3*n] / [n], in id order. */

@@ -74,6 +74,10 @@ struct spg_handle {
     uint8_t *is_dir = nullptr;
     int32_t *vox_seed = nullptr;
     std::vector<double> phi_init;  // Dirichlet values, 0 elsewhere
+    // With AMG: the electrode field (the potential of the Dirichlet values
+    // with no charge), the starting potential of every new particle set.
+    double *phi_vac = nullptr;
+    bool vac_valid = false;
 
     // fields
     double *node_q = nullptr, *rho = nullptr, *phi = nullptr, *b = nullptr, *r = nullptr, *z = nullptr,
@@ -1066,7 +1070,30 @@ int fill_stats(spg_handle *h, spg_stats *st) {
     return SPG_OK;
 }
 
+// The electrode field into phi_vac: one solve from the Dirichlet values with
+// no charge. Its iterations are not counted as a run's.
+int solve_vacuum(spg_handle *h) {
+    const int64_t n = h->n_nodes;
+    if (!h->phi_vac) CK(dalloc(&h->phi_vac, n));
+    CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * n, h->stream));
+    h->phi_hist = 0;
+    const bool prev = h->in_run;
+    h->in_run = false;
+    const int rc = do_solve(h);
+    h->in_run = prev;
+    if (rc == SPG_E_NOT_CONVERGED) return SPG_OK;  // not kept: new particle sets start from phi_init
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->phi_vac, h->phi, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    h->vac_valid = true;
+    return SPG_OK;
+}
+
 int reset_run_state(spg_handle *h) {
+    if ((h->amg || h->amg32) && !h->vac_valid) {
+        const int rc = solve_vacuum(h);
+        if (rc) return rc;
+    }
     h->step = 0;
     h->cg_iters_last = 0;
     h->cg_solves = 0;
@@ -1077,7 +1104,11 @@ int reset_run_state(spg_handle *h) {
     h->resorted_at = -1;
     CK(cudaMemsetAsync(h->ctr, 0, sizeof(DevCounters), h->stream));
     CK(cudaMemsetAsync(h->tri_count, 0, sizeof(unsigned int) * std::max<int64_t>(h->n_tris, 1), h->stream));
-    CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+    if (h->vac_valid)  // AMG: a new particle set starts from the electrode field
+        CK(cudaMemcpyAsync(h->phi, h->phi_vac, sizeof(double) * h->n_nodes, cudaMemcpyDeviceToDevice, h->stream));
+    else
+        CK(cudaMemcpyAsync(h->phi, h->phi_init.data(), sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice,
+                           h->stream));
     CK(cudaMemsetAsync(h->node_q, 0, sizeof(double) * h->n_nodes, h->stream));
     zero_field(h);
     h->phi_hist = 0;
@@ -1342,6 +1373,7 @@ int spg_destroy(spg_handle *h) {
     void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
                     h->node_q,   h->rho,      h->phi,      h->phi_prev,  h->phi_prev2,      h->b,         h->r,        h->z,         h->p,
+                    h->phi_vac,
                     h->node_fix, h->efield,   h->tet_stamp, h->occ_list, h->occ_n, h->occ_gen,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
@@ -2254,6 +2286,7 @@ int spg_set_dirichlet(spg_handle *h, const double *g) {
     if (!h || !g) return SPG_E_INVALID;
     CK(cudaSetDevice(h->device));
     h->phi_hist = 0;  // a new state: the next run solve starts from phi itself
+    h->vac_valid = false;  // the electrode field changes: solved again at the next new particle set
     double *dg = nullptr;
     CK(dalloc(&dg, h->n_nodes));
     CK(cudaMemcpyAsync(dg, g, sizeof(double) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
