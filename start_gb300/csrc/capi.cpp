@@ -150,6 +150,12 @@ struct spg_handle {
     // calls so that a copy or an injection allocates nothing once grown.
     unsigned char *io = nullptr;
     size_t io_bytes = 0;
+    // direct host access: the device reads pageable memory through the host
+    // page tables (address translation over the C2C link)
+    bool ats = false;
+    int32_t *id_slot = nullptr;  // slot of each id for direct downloads
+    int64_t id_slot_cap = 0;
+    unsigned long long *io_counter = nullptr;
     double setup_ms[6] = {0, 0, 0, 0, 0, 0};  // spg_setup_times
     int64_t occupied = 0;
     bool have_particles = false;
@@ -235,6 +241,35 @@ struct IoStage {
     int32_t *slot;  // slot of each id (spg_get_particles)
     unsigned long long *counter;
 };
+
+// Device address through which kernels may read the caller's array p: pinned
+// (registered) host memory, managed memory, or, where the device walks the
+// host page tables, pageable memory. nullptr: copy through the staging buffer.
+const void *device_readable(const spg_handle *h, const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeManaged) return p;
+    if (a.type == cudaMemoryTypeUnregistered && h->ats) return p;
+    return nullptr;
+}
+
+// Device address through which kernels may write the caller's array p: pinned
+// or managed memory only (writes to untouched pageable pages would fault them
+// in one by one).
+void *device_writable(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeManaged) return const_cast<void *>(p);
+    return nullptr;
+}
 
 int io_stage(spg_handle *h, int64_t n, IoStage &st) {
     const size_t need = 60 * size_t(n) + 16;
@@ -1205,6 +1240,13 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
     h = H.get();
     h->prm = *params;
     h->device = params->device;
+    {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, params->device) ==
+            cudaSuccess)
+            h->ats = v != 0;
+        cudaGetLastError();
+    }
     h->mixed = params->precision == SPG_MIXED;
     h->pbytes = h->mixed ? 32.0 : 56.0;
     CK(cudaSetDevice(h->device));
@@ -1373,7 +1415,7 @@ int spg_destroy(spg_handle *h) {
     void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
                     h->node_q,   h->rho,      h->phi,      h->phi_prev,  h->phi_prev2,      h->b,         h->r,        h->z,         h->p,
-                    h->phi_vac,
+                    h->phi_vac,  h->id_slot,  h->io_counter,
                     h->node_fix, h->efield,   h->tet_stamp, h->occ_list, h->occ_n, h->occ_gen,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
@@ -1429,7 +1471,22 @@ int spg_set_particles(spg_handle *h, int64_t n, const double *pos, const double 
     h->n_active = n;
     h->init_lost = 0;
     h->occupied = 0;
-    if (n > 0) {
+    const double *rpos = (n > 0 && !tet_or_null) ? static_cast<const double *>(device_readable(h, pos)) : nullptr;
+    const double *rvel = rpos ? static_cast<const double *>(device_readable(h, vel)) : nullptr;
+    if (rpos && rvel) {
+        // the caller's arrays are device-readable: one kernel reads them where
+        // they lie, locates each particle and writes the state, so the transfer
+        // overlaps the location walks
+        if (!h->io_counter) CK(dalloc(&h->io_counter, 2));
+        CK(cudaMemsetAsync(h->io_counter, 0, sizeof(unsigned long long), s));
+        launch_upload(rpos, rvel, n, mesh_dev(h), h->vox_seed, h->vox_oi, h->vox_dims, h->prm.max_crossings,
+                      h->P[0], h->Q[0], h->mixed ? h->cen : nullptr, h->io_counter, s);
+        CK(cudaGetLastError());
+        unsigned long long lost = 0;
+        CK(cudaMemcpyAsync(&lost, h->io_counter, sizeof(lost), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        h->init_lost = int64_t(lost);
+    } else if (n > 0) {
         IoStage st;
         {
             const int rc = io_stage(h, n, st);
@@ -1752,6 +1809,30 @@ int spg_get_particles(spg_handle *h, int64_t n, double *pos, double *vel, int32_
     if (n == 0) return SPG_OK;
     CK(cudaSetDevice(h->device));
     cudaStream_t s = h->stream;
+    {
+        // pinned or managed caller arrays: the gather writes them directly
+        void *wp = pos ? device_writable(pos) : nullptr, *wv = vel ? device_writable(vel) : nullptr;
+        void *wt = tet ? device_writable(tet) : nullptr, *wf = flags ? device_writable(flags) : nullptr;
+        if ((!pos || wp) && (!vel || wv) && (!tet || wt) && (!flags || wf)) {
+            if (n > h->id_slot_cap) {
+                cudaFree(h->id_slot);
+                h->id_slot = nullptr;
+                h->id_slot_cap = 0;
+                CK(dalloc(&h->id_slot, n));
+                h->id_slot_cap = n;
+            }
+            double *dp = static_cast<double *>(wp), *dv = static_cast<double *>(wv);
+            int32_t *dt = static_cast<int32_t *>(wt);
+            uint32_t *df = static_cast<uint32_t *>(wf);
+            if (h->mixed)
+                launch_gather32(h->Q[h->cur], n, h->id_slot, h->cen, dp, dv, dt, df, s);
+            else
+                launch_gather_by_id(h->P[h->cur], n, h->id_slot, dp, dv, dt, df, s);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(s));
+            return SPG_OK;
+        }
+    }
     IoStage st;
     {
         const int rc = io_stage(h, n, st);

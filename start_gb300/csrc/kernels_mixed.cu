@@ -499,27 +499,41 @@ __global__ void k_to_local(const double *__restrict__ pos, const double *__restr
 }
 
 // One thread per id (slot from launch_slot_of_id): coalesced writes in id order.
-__global__ void k_gather32(DevParticles32 p, int64_t n, const int32_t *__restrict__ slot,
-                           const double *__restrict__ cen, double *pos, double *vel, int32_t *tet, uint32_t *flags) {
-    const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    const int64_t i = slot[id];
-    const uint32_t idf = p.idf[i];
-    const int32_t t = p.tet[i];
-    const int64_t tc = t < 0 ? 0 : t;
-    const double ox = t < 0 ? 0.0 : cen[3 * tc], oy = t < 0 ? 0.0 : cen[3 * tc + 1], oz = t < 0 ? 0.0 : cen[3 * tc + 2];
-    if (pos) {
-        pos[3 * id] = ox + double(p.x[i]);
-        pos[3 * id + 1] = oy + double(p.y[i]);
-        pos[3 * id + 2] = oz + double(p.z[i]);
+// One thread per id, writes in id order; the block's xyz triples go out
+// through shared memory as one contiguous run per array (whole lines per warp
+// store, also when the arrays are the caller's pinned host memory).
+__global__ void __launch_bounds__(256) k_gather32(DevParticles32 p, int64_t n, const int32_t *__restrict__ slot,
+                                                  const double *__restrict__ cen, double *pos, double *vel,
+                                                  int32_t *tet, uint32_t *flags) {
+    __shared__ double sp[3 * 256], sv[3 * 256];
+    const int64_t id0 = int64_t(blockIdx.x) * 256;
+    const int64_t id = id0 + threadIdx.x;
+    const int m = n - id0 < 256 ? int(n - id0) : 256;
+    if (id < n) {
+        const int64_t i = slot[id];
+        const uint32_t idf = p.idf[i];
+        const int32_t t = p.tet[i];
+        const int64_t tc = t < 0 ? 0 : t;
+        const double ox = t < 0 ? 0.0 : cen[3 * tc], oy = t < 0 ? 0.0 : cen[3 * tc + 1],
+                     oz = t < 0 ? 0.0 : cen[3 * tc + 2];
+        if (pos) {
+            sp[3 * threadIdx.x] = ox + double(p.x[i]);
+            sp[3 * threadIdx.x + 1] = oy + double(p.y[i]);
+            sp[3 * threadIdx.x + 2] = oz + double(p.z[i]);
+        }
+        if (vel) {
+            sv[3 * threadIdx.x] = p.vx[i];
+            sv[3 * threadIdx.x + 1] = p.vy[i];
+            sv[3 * threadIdx.x + 2] = p.vz[i];
+        }
+        if (tet) tet[id] = t;
+        if (flags) flags[id] = ((idf & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((idf & kLost) ? SPG_FLAG_LOST : 0u);
     }
-    if (vel) {
-        vel[3 * id] = p.vx[i];
-        vel[3 * id + 1] = p.vy[i];
-        vel[3 * id + 2] = p.vz[i];
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * m; k += 256) {
+        if (pos) pos[3 * id0 + k] = sp[k];
+        if (vel) vel[3 * id0 + k] = sv[k];
     }
-    if (tet) tet[id] = t;
-    if (flags) flags[id] = ((idf & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((idf & kLost) ? SPG_FLAG_LOST : 0u);
 }
 
 __global__ void __launch_bounds__(kSortBlock) k_sort_scatter32(DevParticles32 src, DevParticles32 dst, int64_t n,

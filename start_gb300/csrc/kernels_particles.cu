@@ -622,6 +622,72 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t n, MeshDev m, c
     tet_out[i] = w.status == W_INSIDE ? w.tet : -1;
 }
 
+// Upload and location in one pass, reading the caller's position and
+// velocity arrays where they lie (host memory the GPU reaches over the C2C
+// link), so the copy overlaps the location walks: the same tet and state as
+// k_locate followed by k_init_particles (FP64 form) or k_to_local (mixed form,
+// cen != nullptr: FP32 position about the tet's centroid, FP32 velocity).
+__global__ void __launch_bounds__(128) k_upload(const double *__restrict__ pos, const double *__restrict__ vel, int64_t n, MeshDev m,
+                         const int32_t *__restrict__ vox_seed, double ox, double oy, double oz, double ix, double iy,
+                         double iz, int dx, int dy, int dz, int max_cross, DevParticles p, DevParticles32 q,
+                         const double *__restrict__ cen, unsigned long long *lost) {
+    // the block's xyz triples come in as one contiguous run per array (whole
+    // lines per warp load), then each thread takes its particle's
+    __shared__ double sp[3 * 128], sv[3 * 128];
+    const int64_t i0 = int64_t(blockIdx.x) * 128;
+    const int64_t i = i0 + threadIdx.x;
+    const int cnt = n - i0 < 128 ? int(n - i0) : 128;
+    for (int k = threadIdx.x; k < 3 * cnt; k += 128) {
+        sp[k] = pos[3 * i0 + k];
+        sv[k] = vel[3 * i0 + k];
+    }
+    __syncthreads();
+    unsigned is_lost = 0;
+    if (i < n) {
+        const double px = sp[3 * threadIdx.x], py = sp[3 * threadIdx.x + 1], pz = sp[3 * threadIdx.x + 2];
+        const double vx = sv[3 * threadIdx.x], vy = sv[3 * threadIdx.x + 1], vz = sv[3 * threadIdx.x + 2];
+        int32_t t = -1;
+        if (finite_bits(px) && finite_bits(py) && finite_bits(pz)) {
+            const int cx = min(dx - 1, max(0, int(floor((px - ox) * ix))));
+            const int cy = min(dy - 1, max(0, int(floor((py - oy) * iy))));
+            const int cz = min(dz - 1, max(0, int(floor((pz - oz) * iz))));
+            const int seed = vox_seed[cx + int64_t(dx) * (cy + int64_t(dy) * cz)];
+            const int4 tn = __ldg(m.tet_nodes + seed);
+            double c[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                c[k] = 0.25 * (((m.node_xyz[3 * tn.x + k] + m.node_xyz[3 * tn.y + k]) + m.node_xyz[3 * tn.z + k]) +
+                               m.node_xyz[3 * tn.w + k]);
+            const WalkOut w = walk64(m, seed, c[0], c[1], c[2], px, py, pz, max_cross, false);
+            t = w.status == W_INSIDE ? w.tet : -1;
+        }
+        is_lost = t < 0 ? 1u : 0u;
+        const uint32_t idf = uint32_t(i) | (t < 0 ? kLost : 0u);
+        if (cen) {
+            const int64_t tc = t < 0 ? 0 : t;
+            q.x[i] = float(px - (t < 0 ? 0.0 : cen[3 * tc]));
+            q.y[i] = float(py - (t < 0 ? 0.0 : cen[3 * tc + 1]));
+            q.z[i] = float(pz - (t < 0 ? 0.0 : cen[3 * tc + 2]));
+            q.vx[i] = float(vx);
+            q.vy[i] = float(vy);
+            q.vz[i] = float(vz);
+            q.tet[i] = t;
+            q.idf[i] = idf;
+        } else {
+            p.x[i] = px;
+            p.y[i] = py;
+            p.z[i] = pz;
+            p.vx[i] = vx;
+            p.vy[i] = vy;
+            p.vz[i] = vz;
+            p.tet[i] = t;
+            p.idf[i] = idf;
+        }
+    }
+    const unsigned s = __reduce_add_sync(kFull, is_lost);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(lost, (unsigned long long)s);
+}
+
 __global__ void k_init_particles(const double *__restrict__ pos, const double *__restrict__ vel,
                                  const int32_t *__restrict__ tet, int64_t n, DevParticles p, int64_t id_base) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -647,26 +713,37 @@ __global__ void k_slot_of_id(const uint32_t *__restrict__ idf, int64_t n, int32_
     if (int64_t(id) < n) slot[id] = int32_t(i);
 }
 
-// One thread per id: scattered reads of its slot, coalesced writes in id
-// order (writing by slot would scatter partial-sector writes instead).
-__global__ void k_gather_by_id(DevParticles p, int64_t n, const int32_t *__restrict__ slot, double *pos, double *vel,
-                               int32_t *tet, uint32_t *flags) {
-    const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    const int64_t i = slot[id];
-    const uint32_t idf = p.idf[i];
-    if (pos) {
-        pos[3 * id] = p.x[i];
-        pos[3 * id + 1] = p.y[i];
-        pos[3 * id + 2] = p.z[i];
+// One thread per id: scattered reads of its slot, writes in id order. The
+// block's xyz triples go through shared memory and out as one contiguous run
+// per array, so each warp store covers whole lines (the arrays may be the
+// caller's pinned host memory, written over the C2C link).
+__global__ void __launch_bounds__(256) k_gather_by_id(DevParticles p, int64_t n, const int32_t *__restrict__ slot,
+                                                      double *pos, double *vel, int32_t *tet, uint32_t *flags) {
+    __shared__ double sp[3 * 256], sv[3 * 256];
+    const int64_t id0 = int64_t(blockIdx.x) * 256;
+    const int64_t id = id0 + threadIdx.x;
+    const int m = n - id0 < 256 ? int(n - id0) : 256;
+    if (id < n) {
+        const int64_t i = slot[id];
+        const uint32_t idf = p.idf[i];
+        if (pos) {
+            sp[3 * threadIdx.x] = p.x[i];
+            sp[3 * threadIdx.x + 1] = p.y[i];
+            sp[3 * threadIdx.x + 2] = p.z[i];
+        }
+        if (vel) {
+            sv[3 * threadIdx.x] = p.vx[i];
+            sv[3 * threadIdx.x + 1] = p.vy[i];
+            sv[3 * threadIdx.x + 2] = p.vz[i];
+        }
+        if (tet) tet[id] = p.tet[i];
+        if (flags) flags[id] = ((idf & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((idf & kLost) ? SPG_FLAG_LOST : 0u);
     }
-    if (vel) {
-        vel[3 * id] = p.vx[i];
-        vel[3 * id + 1] = p.vy[i];
-        vel[3 * id + 2] = p.vz[i];
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * m; k += 256) {
+        if (pos) pos[3 * id0 + k] = sp[k];
+        if (vel) vel[3 * id0 + k] = sv[k];
     }
-    if (tet) tet[id] = p.tet[i];
-    if (flags) flags[id] = ((idf & kSettled) ? SPG_FLAG_SETTLED : 0u) | ((idf & kLost) ? SPG_FLAG_LOST : 0u);
 }
 
 // ------------------------------------------------------------------ re-sort
@@ -844,6 +921,14 @@ void launch_init_particles(const double *pos, const double *vel, const int32_t *
     k_init_particles<<<grid_for(n, 256), 256, 0, s>>>(pos, vel, tet, n, p, id_base);
 }
 
+void launch_upload(const double *pos, const double *vel, int64_t n, const MeshDev &m, const int32_t *vox_seed,
+                   const double *oi, const int32_t *dims, int max_cross, const DevParticles &p,
+                   const DevParticles32 &q, const double *cen, unsigned long long *lost, cudaStream_t s) {
+    if (n <= 0) return;
+    k_upload<<<grid_for(n, 128), 128, 0, s>>>(pos, vel, n, m, vox_seed, oi[0], oi[1], oi[2], oi[3], oi[4], oi[5],  // 128: staging
+                                               dims[0], dims[1], dims[2], max_cross, p, q, cen, lost);
+}
+
 void launch_slot_of_id(const uint32_t *idf, int64_t n, int32_t *slot, cudaStream_t s) {
     if (n > 0) k_slot_of_id<<<grid_for(n, 256), 256, 0, s>>>(idf, n, slot);
 }
@@ -852,7 +937,7 @@ void launch_gather_by_id(const DevParticles &p, int64_t n, int32_t *slot, double
                          int32_t *tet, uint32_t *flags, cudaStream_t s) {
     if (n <= 0) return;
     launch_slot_of_id(p.idf, n, slot, s);
-    k_gather_by_id<<<grid_for(n, 256), 256, 0, s>>>(p, n, slot, pos, vel, tet, flags);
+    k_gather_by_id<<<grid_for(n, 256), 256, 0, s>>>(p, n, slot, pos, vel, tet, flags);  // 256: the staging size
 }
 
 int64_t sort_scratch_words(int64_t n_tets) {

@@ -286,6 +286,14 @@ struct DevParticles32 {
     uint32_t *idf;
 };
 
+// Upload and location in one kernel from device-readable caller arrays of n
+// particles (ids 0..n-1): the FP64 form's state into p (cen == nullptr) or
+// the mixed form's into q (cen: FP64 centroids); lost (zeroed by the caller)
+// receives the count of particles outside the mesh.
+void launch_upload(const double *pos, const double *vel, int64_t n, const MeshDev &m, const int32_t *vox_seed,
+                   const double *oi, const int32_t *dims, int max_cross, const DevParticles &p,
+                   const DevParticles32 &q, const double *cen, unsigned long long *lost, cudaStream_t s);
+
 struct MeshDev32 {
     const TetRec32 *rec;
     const TetRec *rec64;  // FP64 map for near-zero barycentric tests
