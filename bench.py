@@ -348,14 +348,27 @@ def grad_leg(args, local):
            "checkpoint_every": lp.every, "half_angle_deg": 30.0, "sigma_m": lp.sigma,
            "timing": "host wall clock, median of 3, synchronised"}
     out.update(measure(V, (0.05, 0.05, 0.0)))
+    # the same with the recovered field's gradient in the backward pass
+    e.grad_field_gradient(True)
+    fg = measure(V, (0.05, 0.05, 0.0))
+    e.grad_field_gradient(False)
+    out["field_gradient"] = {k: fg[k] for k in ("dJ_dV", "dJ_dalpha", "grad_forward_ms", "backward_ms", "cost_ratio")}
     if not args.no_grad_fd:
-        out["live_fd"] = live_fd_gaps(lp, V, a0, out["dJ_dV"], out["dJ_dalpha"])
-        # the same without gas: only the per-cell field jumps remain
-        lq = LandingProblem(n_particles=args.grad_particles, steps=300, collisions=False)
+        grads = {"pathwise": (out["dJ_dV"], out["dJ_dalpha"]), "field_gradient": (fg["dJ_dV"], fg["dJ_dalpha"])}
+        out["live_fd"] = live_fd_gaps(lp, V, a0, grads, ((1e-3, 1e-4), (1.0, 1e-2)))
+        # 400 steps without gas: every ion lands, so J's count does not change
+        # under the perturbation, and no collision decision can flip; only
+        # the per-cell field's jumps separate the live map from the gradients
+        lq = LandingProblem(n_particles=args.grad_particles, steps=400, collisions=False)
         lq.target = np.array([0.05, 0.05, 0.0])
-        lq.forward(V, a0)
-        dVq, daq, _ = lq.backward()
-        out["live_fd_collisionless"] = live_fd_gaps(lq, V, a0, dVq, daq)
+        gq = {}
+        for name, on in (("pathwise", False), ("field_gradient", True)):
+            lq.engine.grad_field_gradient(on)
+            lq.forward(V, a0)
+            dVq, daq, _ = lq.backward()
+            gq[name] = (dVq.tolist(), daq)
+        out["live_fd_400steps_no_gas"] = live_fd_gaps(lq, V, a0, gq, ((1.0, 1e-2),))
+        out["live_fd_400steps_no_gas"]["n_landed"] = int(lq._last[2])
         lq.close()
     V_stated = np.random.default_rng(1).uniform(-100.0, 100.0, 6)
     out["as_stated"] = measure(V_stated, (0.05, 0.05, 0.1))
@@ -363,26 +376,27 @@ def grad_leg(args, local):
     return out
 
 
-def live_fd_gaps(lp, V, a0, dV, da):
+def live_fd_gaps(lp, V, a0, grads, steps):
     """Central differences of the live forward pass (nothing frozen) against
-    the pathwise gradient (dV, da), at the step sizes of the configuration
-    (1e-3 V, 1e-4 rad) and at larger ones (1 V, 1e-2 rad) that average over
-    many of the jump events the pathwise derivative leaves out: pushes that
-    change cell, and, with gas, collision decisions u0 < P that flip."""
-    g = np.asarray(dV, float)
-    res = {"pathwise_dJ_dV": g.tolist(), "pathwise_dJ_dalpha": da,
-           "note": "relative gap = max |fd - pathwise| / max |pathwise|"}
-    for hv, ha in ((1e-3, 1e-4), (1.0, 1e-2)):
+    each gradient in grads ({name: (dJ/dV, dJ/dalpha)}), at each (h_V, h_rad)
+    in steps. Small steps see few of the jumps the gradients leave out
+    (pushes that change cell, collision decisions that flip, ions that land or
+    not by the last step), each of which moves J by about 1/N; larger steps
+    average over many."""
+    res = {"note": "relative gap = max |fd - gradient| / max |fd| (potentials), |fd - gradient| / |fd| (alpha)"}
+    for hv, ha in steps:
         fd = []
-        for f in range(len(g)):
-            dv = np.zeros(len(g))
+        for f in range(len(V)):
+            dv = np.zeros(len(V))
             dv[f] = hv
             fd.append((lp.forward(V + dv, a0) - lp.forward(V - dv, a0)) / (2 * hv))
+        fd = np.array(fd)
         fd_a = (lp.forward(V, a0 + ha) - lp.forward(V, a0 - ha)) / (2 * ha)
-        res[f"h_{hv:g}V_{ha:g}rad"] = {
-            "dJ_dV": fd, "dJ_dalpha": fd_a,
-            "rel_gap_V": float(np.max(np.abs(np.array(fd) - g)) / np.max(np.abs(g))),
-            "rel_gap_alpha": abs(fd_a - da) / abs(da)}
+        r = {"dJ_dV": fd.tolist(), "dJ_dalpha": fd_a}
+        for name, (dV, da) in grads.items():
+            r[f"rel_gap_V_{name}"] = float(np.max(np.abs(fd - np.asarray(dV))) / np.max(np.abs(fd)))
+            r[f"rel_gap_alpha_{name}"] = abs(fd_a - da) / abs(fd_a)
+        res[f"h_{hv:g}V_{ha:g}rad"] = r
     return res
 
 

@@ -62,6 +62,7 @@ def load(path: str | Path | None = None):
         "spo_set_dirichlet": (C.c_int, [_H, _pd]),
         "spo_grad": (C.c_int, [_H, C.c_int32, _pd, C.c_double, _pd, C.POINTER(C.c_int64), _pd, _pd, _pd]),
         "spo_grad_freeze": (C.c_int, [_H, C.c_int]),
+        "spo_grad_field_gradient": (C.c_int, [_H, C.c_int]),
         "spo_update_position": (None, [_pd, _pd, C.c_double]),
         "spo_segment_triangle": (C.c_int, [_pd, _pd, _pd, _pd, _pd, _pd]),
         "spo_gas_concentration": (C.c_double, [C.c_double, C.c_double]),
@@ -275,6 +276,9 @@ class Oracle:
         if rc:
             raise RuntimeError(self.lib.spo_last_error().decode())
         return J.value, nl.value, dg, dx, dv
+
+    def grad_field_gradient(self, on=True):
+        self.lib.spo_grad_field_gradient(self.h, 1 if on else 0)
 
     def grad_freeze(self, mode):
         """0 off, 1 record the field cells of the next grad(), 2 replay them."""

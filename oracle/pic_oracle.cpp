@@ -157,6 +157,8 @@ struct spo_handle {
     bool have_E = false;
     // field-cell freezing for spo_grad (0 off, 1 record, 2 replay)
     int freeze = 0;
+    // spo_grad adds the gradient of the recovered continuous field (see spo_grad_field_gradient)
+    bool field_gradient = false;
     std::vector<int32_t> frozen;
     // reference-behaviour switches (SPO_COMPAT_*), off by default
     uint32_t compat = 0;
@@ -1100,6 +1102,36 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
     // particle adjoint
     std::vector<double> gE(3 * h->Nt, 0.0), ax(3 * n, 0.0), av(3 * n, 0.0);
     const double cq = p.charge / p.mass * p.dt;
+    // gradient of the recovered field per tet: nodal E as the volume average of
+    // the incident tets' E, interpolated linearly: G_t[d][c] = sum_i E_i[d] dlambda_i/dx_c
+    std::vector<double> G;
+    if (h->field_gradient) {
+        std::vector<double> En(3 * h->Nn, 0.0), Wn(h->Nn, 0.0);
+        for (int64_t t = 0; t < h->Nt; ++t)
+            for (int k = 0; k < 4; ++k) {
+                const int32_t nd = h->tn[4 * t + k];
+                for (int c = 0; c < 3; ++c) En[3 * nd + c] += h->vol[t] * h->tet[t].E[c];
+                Wn[nd] += h->vol[t];
+            }
+        for (int64_t nd = 0; nd < h->Nn; ++nd)
+            for (int c = 0; c < 3; ++c) En[3 * nd + c] /= Wn[nd];
+        G.assign(9 * h->Nt, 0.0);
+        for (int64_t t = 0; t < h->Nt; ++t) {
+            const Tet &T = h->tet[t];
+            double gl[4][3];
+            for (int c = 0; c < 3; ++c) {
+                gl[1][c] = T.M[c];
+                gl[2][c] = T.M[3 + c];
+                gl[3][c] = T.M[6 + c];
+                gl[0][c] = -(gl[1][c] + gl[2][c] + gl[3][c]);
+            }
+            for (int k = 0; k < 4; ++k) {
+                const double *e = &En[3 * h->tn[4 * t + k]];
+                for (int d = 0; d < 3; ++d)
+                    for (int c = 0; c < 3; ++c) G[9 * t + 3 * d + c] += e[d] * gl[k][c];
+            }
+        }
+    }
     for (int64_t i = 0; i < n; ++i) {
         const int N = land_step[i];
         if (N < 0) continue;
@@ -1155,6 +1187,11 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
                 gE[3 * t + c] += cq * b[c];
                 V[c] = b[c];
             }
+            if (!G.empty() && !ez) {
+                // the pushed velocity depends on the position through the field
+                const double *g = &G[9 * size_t(t)];
+                for (int c = 0; c < 3; ++c) A[c] += cq * (g[c] * b[0] + g[3 + c] * b[1] + g[6 + c] * b[2]);
+            }
         }
         for (int c = 0; c < 3; ++c) {
             ax[3 * i + c] = A[c];
@@ -1190,6 +1227,11 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
         for (const auto &e : h->elim[f]) dJ_dg[e.first] -= e.second * mu[f];
     if (dJ_dx0) std::copy(ax.begin(), ax.end(), dJ_dx0);
     if (dJ_dv0) std::copy(av.begin(), av.end(), dJ_dv0);
+    return SPG_OK;
+}
+
+int spo_grad_field_gradient(spo_handle *h, int on) {
+    h->field_gradient = on != 0;
     return SPG_OK;
 }
 

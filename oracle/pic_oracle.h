@@ -65,6 +65,11 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
  * cells in later calls (the walk, landing and collisions stay live), 0 off. */
 int spo_grad_freeze(spo_handle *h, int mode);
 
+/* With on != 0, spo_grad also carries the sensitivity of the push to the
+ * particle's position, through the gradient of a continuous field recovered
+ * from the per-tet E (nodal volume averages, linear in each tet). */
+int spo_grad_field_gradient(spo_handle *h, int on);
+
 /* Reference-behaviour switches: each reproduces one behaviour of the
  * reference's own loop that the build changes on purpose. All off by default.
  *   PUSH_NEVER        no electromagnetic push: the pushing tet is looked up by

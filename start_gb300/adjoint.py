@@ -16,8 +16,9 @@ The map differentiated is the step with the collision events, the random
 numbers and the cell whose E pushes a particle at each step held fixed (the
 pathwise derivative). The live step also moves when a push position crosses a
 cell face, where the per-cell constant field jumps; central differences of the
-live map include those jumps and differ from the pathwise gradient by the
-discretisation of E (about 20 % at h = 4 mm on this problem).
+live map include those jumps. With field_gradient the backward pass adds the
+push's dependence on the position through a continuous field recovered from
+the per-tet E, which accounts for most of them.
 """
 from __future__ import annotations
 
@@ -36,14 +37,22 @@ class LandingSetup:
     faces: the box faces (indices into mesh.BOX_FACES) that carry an
     electrode, one potential each; the other faces are Neumann. With only the
     two z faces the field is uniform: P1 reproduces the linear potential
-    exactly."""
+    exactly.
+
+    field_gradient: the backward pass also carries the push's dependence on
+    the particle's position through the gradient of a continuous field
+    recovered from the per-tet E (spg_grad_field_gradient). Off, the gradient
+    is the exact derivative of the map with the pushing cells held fixed; on,
+    it follows central differences of the live step much more closely where
+    the field varies from cell to cell."""
 
     def __init__(self, n_particles=1_000_000, cells=25, steps=300, seed=1, sigma=0.01, checkpoint_every=32,
                  collisions=True, energy_ev=1.0, gas_scale=1.0, cg_rtol=1e-12, preconditioner=0, precision=0,
-                 faces=(0, 1, 2, 3, 4, 5)):
+                 faces=(0, 1, 2, 3, 4, 5), field_gradient=False):
         L = 0.1
         self.mesh = M.kuhn_box((cells,) * 3, (L,) * 3)
         self.faces = tuple(faces)
+        self.field_gradient = field_gradient
         owner = np.full(self.mesh.n_nodes, -1)
         for f, (ax, side) in enumerate(M.BOX_FACES):
             if f in self.faces:
@@ -95,6 +104,7 @@ class LandingProblem(LandingSetup):
     def __init__(self, *args, **kw):
         super().__init__(*args, **kw)
         self.engine = StartPIC(self.mesh, self.params)
+        self.engine.grad_field_gradient(self.field_gradient)
         self._last = None
 
     def forward(self, V, alpha):

@@ -197,6 +197,9 @@ struct spg_handle {
     int64_t ckpt_cap = 0, land_cap = 0, hist_cap = 0;  // particles (x window steps for hist) allocated
     double grad_inv_n = 0.0;                            // 1 / landed count of the last forward
     bool grad_ready = false;
+    // spg_grad_field_gradient: per-tet gradient of the recovered field and its scratch
+    bool grad_fg = false;
+    double *grad_G = nullptr, *grad_En = nullptr;
 };
 
 namespace {
@@ -1415,7 +1418,7 @@ int spg_destroy(spg_handle *h) {
     void *ptrs[] = {h->rec,      h->screen,   h->nbr,      h->ftri,     h->tet_nodes, h->node_xyz, h->row_ptr,   h->col,
                     h->val,      h->inv_diag, h->is_dir,   h->dir_value, h->lift,     h->dual_vol,  h->vox_seed,
                     h->node_q,   h->rho,      h->phi,      h->phi_prev,  h->phi_prev2,      h->b,         h->r,        h->z,         h->p,
-                    h->phi_vac,  h->id_slot,  h->io_counter,
+                    h->phi_vac,  h->id_slot,  h->io_counter, h->grad_G, h->grad_En,
                     h->node_fix, h->efield,   h->tet_stamp, h->occ_list, h->occ_n, h->occ_gen,   h->slice_ptr, h->scol,   h->sval,
                     h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
@@ -2383,6 +2386,12 @@ int spg_set_dirichlet(spg_handle *h, const double *g) {
     return SPG_OK;
 }
 
+int spg_grad_field_gradient(spg_handle *h, int32_t on) {
+    if (!h) return SPG_E_INVALID;
+    h->grad_fg = on != 0;
+    return SPG_OK;
+}
+
 int spg_grad_forward(spg_handle *h, int32_t nsteps, int32_t checkpoint_every, const double target[3], double sigma,
                      double *J, int64_t *n_landed) {
     if (!h || !target || !(sigma > 0.0) || nsteps < 1 || checkpoint_every < 1)
@@ -2490,6 +2499,27 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
     CK(cudaMemsetAsync(h->adj_x, 0, sizeof(double) * 3 * n, s));
     CK(cudaMemsetAsync(h->adj_v, 0, sizeof(double) * 3 * n, s));
     CK(cudaMemsetAsync(h->gE, 0, sizeof(double) * 3 * h->n_tets, s));
+    const double *G = nullptr;
+    if (h->grad_fg) {
+        // the gradient of the recovered field, from the E every tet has now
+        // (the forward's field; completed first where a run left it partial)
+        if (!h->grad_G) {
+            CK(dalloc(&h->grad_G, 9 * h->n_tets));
+            CK(dalloc(&h->grad_En, 4 * h->n_nodes));
+        }
+        if (!h->field_full) {
+            const FieldArgs f = field_args(h);
+            if (h->mixed)
+                launch_field32_full(f, h->n_tets, s);
+            else
+                launch_field64_full(f, h->n_tets, s);
+            h->field_full = true;
+        }
+        launch_field_gradient(h->tet_nodes, h->rec, h->efield, h->n_tets, h->n_nodes, h->grad_En,
+                              h->grad_En + 3 * h->n_nodes, h->grad_G, s);
+        CK(cudaGetLastError());
+        G = h->grad_G;
+    }
     DevParticles &work = h->P[1 - h->cur];
     DevParticles32 &work32 = h->Q[1 - h->cur];
     const int nck = (h->grad_steps + W - 1) / W;
@@ -2515,10 +2545,10 @@ int spg_grad_backward(spg_handle *h, double *dJ_dg, double *dJ_dx0, double *dJ_d
         c.step = h->grad_step0;  // absolute step of k = 0 (landing steps and Philox counters are absolute)
         if (h->mixed)
             launch_backward32(work32, n, mesh_dev32(h), h->hist, k0, k1, h->land, h->gr, h->grad_inv_n, h->adj_x,
-                              h->adj_v, h->gE, c, s);
+                              h->adj_v, h->gE, c, s, G);
         else
             launch_backward(work, n, h->hist, k0, k1, h->rec, h->land, h->gr, h->grad_inv_n, h->adj_x, h->adj_v,
-                            h->gE, c, s);
+                            h->gE, c, s, G);
         CK(cudaGetLastError());
     }
     CK(cudaMemsetAsync(h->lam, 0, sizeof(double) * h->n_nodes, s));

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(128) k_backward(const DevParticles p, int64_t 
                                                   const TetRec *__restrict__ rec, const LandRec *__restrict__ land,
                                                   const double *__restrict__ gr, double gscale, double *__restrict__ ax,
                                                   double *__restrict__ av, double *__restrict__ gE, StepConst c,
-                                                  double cq) {
+                                                  double cq, const double *__restrict__ G) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const LandRec L = land[i];
@@ -184,6 +184,14 @@ __global__ void __launch_bounds__(128) k_backward(const DevParticles p, int64_t 
         Vx = bx;
         Vy = by;
         Vz = bz;
+        if (G && !R.ezero) {
+            // the pushed velocity depends on the position through the recovered
+            // field: abar_x += cq G^T abar_va, G[3 d + c] = dE_d / dx_c
+            const double *g = G + 9 * int64_t(t);
+            Ax += cq * (g[0] * bx + g[3] * by + g[6] * bz);
+            Ay += cq * (g[1] * bx + g[4] * by + g[7] * bz);
+            Az += cq * (g[2] * bx + g[5] * by + g[8] * bz);
+        }
     }
     if (run >= 0) {
         atomicAdd(gE + 3 * run, cq * sx);
@@ -196,6 +204,53 @@ __global__ void __launch_bounds__(128) k_backward(const DevParticles p, int64_t 
     av[3 * i] = Vx;
     av[3 * i + 1] = Vy;
     av[3 * i + 2] = Vz;
+}
+
+// Gradient of a continuous field recovered from the per-tet E: the nodal
+// field is the volume average of the incident tets' E, interpolated linearly
+// in each tet, so its gradient is constant per tet:
+// G_t[3 d + c] = sum_i E_node(i)[d] dlambda_i / dx_c. The volume of a tet is
+// 1 / (6 |det M|) with M its barycentric map.
+__global__ void k_node_field(const int4 *__restrict__ tet_nodes, const TetRec *__restrict__ rec,
+                             const double *__restrict__ E, int64_t nt, double *__restrict__ En, double *__restrict__ Wn) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const double *M = rec[t].M;
+    const double det = M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) +
+                       M[2] * (M[3] * M[7] - M[4] * M[6]);
+    const double vol = 1.0 / (6.0 * fabs(det));
+    const int4 tn = tet_nodes[t];
+    const int nd[4] = {tn.x, tn.y, tn.z, tn.w};
+    for (int k = 0; k < 4; ++k) {
+        for (int c = 0; c < 3; ++c) atomicAdd(En + 3 * int64_t(nd[k]) + c, vol * E[3 * t + c]);
+        atomicAdd(Wn + nd[k], vol);
+    }
+}
+
+__global__ void k_tet_field_gradient(const int4 *__restrict__ tet_nodes, const TetRec *__restrict__ rec,
+                                     const double *__restrict__ En, const double *__restrict__ Wn, int64_t nt,
+                                     double *__restrict__ G) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const double *M = rec[t].M;
+    double gl[4][3];
+    for (int c = 0; c < 3; ++c) {
+        gl[1][c] = M[c];
+        gl[2][c] = M[3 + c];
+        gl[3][c] = M[6 + c];
+        gl[0][c] = -(gl[1][c] + gl[2][c] + gl[3][c]);
+    }
+    const int4 tn = tet_nodes[t];
+    const int nd[4] = {tn.x, tn.y, tn.z, tn.w};
+    double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k) {
+        const double w = 1.0 / Wn[nd[k]];
+        for (int d = 0; d < 3; ++d) {
+            const double e = En[3 * int64_t(nd[k]) + d] * w;
+            for (int c = 0; c < 3; ++c) g[3 * d + c] += e * gl[k][c];
+        }
+    }
+    for (int q = 0; q < 9; ++q) G[9 * t + q] = g[q];
 }
 
 // dJ/dphi from dJ/dE: E = -sum_r (phi_{r+1} - phi_0) M_r.
@@ -285,10 +340,10 @@ void launch_objective(const DevParticles &p, int64_t n, const LandRec *land, con
 }
 void launch_backward(const DevParticles &p, int64_t n, const AdjHist &h, int k0, int k1, const TetRec *rec,
                      const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
-                     const StepConst &c, cudaStream_t s) {
+                     const StepConst &c, cudaStream_t s, const double *G) {
     if (n > 0)
         k_backward<<<grid_for(n, 128), 128, 0, s>>>(p, n, h, k0, k1, rec, land, gr, gscale, ax, av, gE, c,
-                                                     c.charge / c.mass * c.dt);
+                                                     c.charge / c.mass * c.dt, G);
 }
 void launch_gE_to_nodes(const int4 *tet_nodes, const TetRec *rec, const double *gE, int64_t nt, double *lam,
                         cudaStream_t s) {
@@ -315,4 +370,15 @@ void launch_gather_adj(const DevParticles &p, int64_t n, const double *ax, const
     if (n > 0) k_gather_adj<<<grid_for(n, 256), 256, 0, s>>>(p, n, ax, av, dx, dv);
 }
 
+void launch_field_gradient(const int4 *tet_nodes, const TetRec *rec, const double *E, int64_t nt, int64_t nn,
+                           double *En, double *Wn, double *G, cudaStream_t s) {
+    cudaMemsetAsync(En, 0, sizeof(double) * 3 * nn, s);
+    cudaMemsetAsync(Wn, 0, sizeof(double) * nn, s);
+    if (nt <= 0) return;
+    const unsigned grid = unsigned((nt + 255) / 256);
+    k_node_field<<<grid, 256, 0, s>>>(tet_nodes, rec, E, nt, En, Wn);
+    k_tet_field_gradient<<<grid, 256, 0, s>>>(tet_nodes, rec, En, Wn, nt, G);
+}
+
 }  // namespace spg
+

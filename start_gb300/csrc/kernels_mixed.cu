@@ -596,7 +596,8 @@ __global__ void k_objective32(MixedArgs a, const LandRec *__restrict__ land, dou
 __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int k0, int k1,
                                                     const LandRec *__restrict__ land, const double *__restrict__ gr,
                                                     double gscale, double *__restrict__ ax, double *__restrict__ av,
-                                                    double *__restrict__ gE, StepConst c, double cq) {
+                                                    double *__restrict__ gE, StepConst c, double cq,
+                                                    const double *__restrict__ G) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int64_t n = a.n;
@@ -668,6 +669,14 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
         Vx = bx;
         Vy = by;
         Vz = bz;
+        if (G && !R.ezero) {
+            // the pushed velocity's dependence on the position through the
+            // recovered field: abar_x += cq G^T abar_va
+            const double *g = G + 9 * int64_t(t);
+            Ax += cq * (g[0] * bx + g[3] * by + g[6] * bz);
+            Ay += cq * (g[1] * bx + g[4] * by + g[7] * bz);
+            Az += cq * (g[2] * bx + g[5] * by + g[8] * bz);
+        }
     }
     if (run >= 0) {
         atomicAdd(gE + 3 * run, cq * sx);
@@ -748,10 +757,10 @@ void launch_objective32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, 
 
 void launch_backward32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const AdjHist &h, int k0, int k1,
                        const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
-                       const StepConst &c, cudaStream_t s) {
+                       const StepConst &c, cudaStream_t s, const double *G) {
     if (n > 0)
         k_backward32<<<grid_for(n, 128), 128, 0, s>>>(make_args(p, n, m), h, k0, k1, land, gr, gscale, ax, av, gE, c,
-                                                       c.charge / c.mass * c.dt);
+                                                       c.charge / c.mass * c.dt, G);
 }
 
 void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, const double *av, double *dx,

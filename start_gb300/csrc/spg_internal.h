@@ -176,9 +176,17 @@ struct AdjHist {
 void launch_record(const DevParticles &p, int64_t n, const AdjHist &h, int k, cudaStream_t s);
 void launch_objective(const DevParticles &p, int64_t n, const LandRec *land, const double *target, double sigma,
                       double *gr, double *sums, cudaStream_t s);
+// G (nullable): per-tet gradient of the recovered field (launch_field_gradient);
+// with it the position adjoint also carries the push's dependence on the
+// particle's position.
 void launch_backward(const DevParticles &p, int64_t n, const AdjHist &h, int k0, int k1, const TetRec *rec,
                      const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
-                     const StepConst &c, cudaStream_t s);
+                     const StepConst &c, cudaStream_t s, const double *G = nullptr);
+// G[9 t + 3 d + c] = dE_d/dx_c of the continuous field whose nodal values are
+// the volume averages of the incident tets' E (E: 3 per tet); En (3 nn) and
+// Wn (nn) are scratch.
+void launch_field_gradient(const int4 *tet_nodes, const TetRec *rec, const double *E, int64_t nt, int64_t nn,
+                           double *En, double *Wn, double *G, cudaStream_t s);
 void launch_gE_to_nodes(const int4 *tet_nodes, const TetRec *rec, const double *gE, int64_t nt, double *lam,
                         cudaStream_t s);
 void launch_adj_rhs(const double *lam, const uint8_t *is_dir, double *b, double *x, int64_t nn, cudaStream_t s);
@@ -313,7 +321,7 @@ void launch_objective32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, 
                         const double *target, double sigma, double *gr, double *sums, cudaStream_t s);
 void launch_backward32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const AdjHist &h, int k0, int k1,
                        const LandRec *land, const double *gr, double gscale, double *ax, double *av, double *gE,
-                       const StepConst &c, cudaStream_t s);
+                       const StepConst &c, cudaStream_t s, const double *G = nullptr);
 void launch_gather_adj32(const DevParticles32 &p, int64_t n, const double *ax, const double *av, double *dx,
                          double *dv, cudaStream_t s);
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,

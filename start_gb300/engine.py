@@ -356,6 +356,11 @@ class StartPIC:
                                                N.as_ptr(dv, C.c_double) if particles else None, C.byref(it)))
         return g, dx, dv, it.value
 
+    def grad_field_gradient(self, on=True):
+        """Whether grad_backward also carries the push's dependence on the
+        position through the recovered field's gradient (spg_grad_field_gradient)."""
+        self._check(self.lib.spg_grad_field_gradient(self.h, 1 if on else 0))
+
     def synchronize(self):
         self._check(self.lib.spg_synchronize(self.h))
 

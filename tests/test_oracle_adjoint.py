@@ -71,3 +71,44 @@ def test_gradient_is_gauge_invariant(landing):
     """Raising every electrode by the same amount leaves E unchanged."""
     prob, (J, nl, dV, da) = landing
     assert abs(dV.sum()) <= 1e-9 * np.abs(dV).sum()
+
+
+def test_field_gradient_follows_live_central_differences(built):
+    """The oracle with the recovered field's gradient in its adjoint, against
+    central differences of its live step (nothing frozen): six electrodes,
+    no gas, 1e5 ions, 400 steps so that every ion lands, h = 1 V. The
+    pathwise gradient is about 18 % off, this one about 5 %."""
+    s = LandingSetup(n_particles=100_000, steps=400, collisions=False, cg_rtol=1e-13)
+    s.target = np.array([0.05, 0.05, 0.0])
+    o = O.Oracle(s.mesh, s.params)
+
+    def setup(V):
+        o.set_dirichlet(s.dirichlet_values(V))
+        x0, v0, _, _ = s.initial_state(A0)
+        o.set_particles(x0, v0)
+        o.solve(np.zeros(s.mesh.n_nodes))
+
+    def live_J(V):
+        setup(V)
+        o.process(s.steps)
+        p = o.particles()
+        d = p["pos"][(p["flags"] & 1) != 0] - s.target
+        return float(np.mean(np.exp(-np.sum(d * d, axis=1) / (2 * s.sigma ** 2))))
+
+    grads = []
+    for fg in (False, True):
+        o.grad_field_gradient(fg)
+        setup(V0)
+        J, nl, dg, _, _ = o.grad(s.steps, s.target, s.sigma)
+        assert nl >= 99_990
+        grads.append(s.face_sums(dg))
+    fd = []
+    for f in range(6):
+        e = np.zeros(6)
+        e[f] = 1.0
+        fd.append((live_J(V0 + e) - live_J(V0 - e)) / 2.0)
+    fd = np.array(fd)
+    gap0, gap1 = (np.max(np.abs(fd - g)) / np.max(np.abs(fd)) for g in grads)
+    assert gap1 <= 0.10 and gap1 <= 0.6 * gap0, (gap0, gap1)
+    o.close()
+
