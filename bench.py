@@ -602,12 +602,23 @@ def run_gpu(args):
         msnap = em.checkpoint()
         mms, mps, _, _ = timed_steps(em, sm_, K)
         em.restore(msnap)
-        del msnap
         em.profile_enable(True)
         em.run(K, raise_on_nonconvergence=False)
         mp = em.profile()
         em.profile_enable(False)
-        cmp_short = compare_forms(state64, gpu_state(em))
+        mstate = gpu_state(em)
+        # the same steps one launch per step (no segments): time and identity
+        em.restore(msnap)
+        del msnap
+        em.set_step_segments(1)
+        sms_, sps_, _, _ = timed_steps(em, sm_, K)
+        sstate = gpu_state(em)
+        em.set_step_segments(32)
+        single = {"ms_per_step": sms_ / K, "value": sps_ / (sms_ / 1e3),
+                  "identical_to_segments": bool(all(np.array_equal(mstate[k], sstate[k])
+                                                    for k in ("counts", "pos", "flags", "tet", "phi"))
+                                                and mstate["stats"] == sstate["stats"])}
+        cmp_short = compare_forms(state64, mstate)
         mval = mps / (mms / 1e3)
         mixed = {"value": mval, "unit": UNIT, "ms_per_step": mms / K, "speedup_vs_fp64": mval / value,
                  "l1_hist_error_vs_fp64": cmp_short["l1_hist_error"],
@@ -620,6 +631,7 @@ def run_gpu(args):
                  "step_GBps": mp["step_bytes"] / (mp["step_ms"] / 1e3) / 1e9 if mp["step_ms"] > 0 else None,
                  "pcg_GBps": mp["pcg_bytes"] / (mp["pcg_ms"] / 1e3) / 1e9 if mp["pcg_ms"] > 0 else None,
                  "gpu_launches": mp["kernel_launches"],
+                 "one_launch_per_step": single,
                  "dtype": ("f32 state/push/V-cycle, f64 PCG SpMV + vectors + sums" if args.precond != "jacobi"
                            else "f32 state/push/SpMV, f64 refinement + sums")}
         if state64_long is not None:

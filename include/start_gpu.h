@@ -282,6 +282,15 @@ int spg_process(spg_handle *h, int32_t nsteps, spg_stats *stats);
 int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats);
 /* Re-sorts particles by tet now (settled/lost particles move to the end). */
 int spg_resort(spg_handle *h);
+/* No counterpart in the reference (an execution choice, not a result). In the
+ * mixed form spg_run and spg_process run the steps between two events of the
+ * loop (a solve, a re-sort, the end of the call) as segments of up to
+ * max_steps steps: one pass keeps each particle in registers until a move
+ * needs the exact tet walk, the walk runs batched, and the walked particles
+ * resume from the next step. Results are bit-identical to one launch per
+ * step (max_steps = 1). Default 32; SPG_E_INVALID outside 1..64. The FP64
+ * form and runs with trajectory sampling always step one launch per step. */
+int spg_set_step_segments(spg_handle *h, int32_t max_steps);
 
 int spg_get_stats(spg_handle *h, spg_stats *stats);
 int spg_get_triangle_counts(spg_handle *h, uint64_t *counts /* [n_triangles] */);

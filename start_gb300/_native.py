@@ -120,6 +120,7 @@ SIGNATURES = {
     "spg_get_particles": (C.c_int, [_H, C.c_int64, _pd, _pd, _pi32, C.POINTER(C.c_uint32)]),
     "spg_gather": (C.c_int, [_H, _pd]),
     "spg_grad_field_gradient": (C.c_int, [_H, C.c_int32]),
+    "spg_set_step_segments": (C.c_int, [_H, C.c_int32]),
     "spg_get_charge_density": (C.c_int, [_H, _pd]),
     "spg_solve": (C.c_int, [_H, _pd, _pd, _pi32, _pd]),
     "spg_process": (C.c_int, [_H, C.c_int32, C.POINTER(Stats)]),

@@ -128,6 +128,7 @@ struct spg_handle {
     double pbytes = 56.0;  // bytes per particle in HBM
     TetRec32 *rec32 = nullptr;
     double *cen = nullptr;  // 3 per tet
+    float *cen_lo = nullptr;  // 3 per tet: cen - float(cen)
     DevParticles32 Q[2]{};
     float *sval32 = nullptr, *inv_diag32 = nullptr;
     float *e32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr;
@@ -143,6 +144,13 @@ struct spg_handle {
     DevCounters *ctr = nullptr;
     WalkItem *walkq = nullptr;       // capacity cap (particles)
     unsigned int *walkq_n = nullptr;
+    // segmented steps of the mixed form: at most seg_max steps per segment
+    // (1: one launch per step); resumed-particle list and per-round counters
+    int seg_max = 32;
+    int2 *seg_rq = nullptr;
+    int64_t seg_rq_cap = 0;
+    unsigned int *seg_qn = nullptr;
+    int seg_qn_cap = 0;
     int64_t *n_alive_dev = nullptr;
     int32_t *sort_scratch = nullptr;
     // Staging for particles that cross the host boundary or come from a
@@ -325,6 +333,7 @@ MeshDev32 mesh_dev32(const spg_handle *h) {
     m.rec = h->rec32;
     m.rec64 = h->rec;
     m.cen = h->cen;
+    m.cen_lo = h->cen_lo;
     m.nbr = h->nbr;
     m.ftri = h->ftri;
     m.tet_nodes = h->tet_nodes;
@@ -1082,6 +1091,67 @@ int do_process(spg_handle *h) {
     return SPG_OK;
 }
 
+// Steps h->step .. h->step + l - 1 of the mixed form as one segment (nothing
+// of the time loop falls between them).
+int do_segment32(spg_handle *h, int l) {
+    h->occ_fresh = false;
+    if (h->seg_rq_cap < h->cap) {
+        cudaFree(h->seg_rq);
+        h->seg_rq = nullptr;
+        h->seg_rq_cap = 0;
+        CK(dalloc(&h->seg_rq, size_t(std::max<int64_t>(h->cap, 1))));
+        h->seg_rq_cap = h->cap;
+    }
+    if (h->seg_qn_cap < 2 * l + 1) {
+        cudaFree(h->seg_qn);
+        h->seg_qn = nullptr;
+        h->seg_qn_cap = 0;
+        CK(dalloc(&h->seg_qn, size_t(2 * h->seg_max + 1)));
+        h->seg_qn_cap = 2 * h->seg_max + 1;
+    }
+    StepConst c = step_const(h);
+    ev_begin(h, h->ev_step);
+    const int nl = launch_segment32(h->Q[h->cur], h->n_active, mesh_dev32(h), c, l, h->tri_count, h->walkq,
+                                    h->seg_rq, h->seg_qn, h->ctr, field_args(h), h->stream);
+    ev_end(h, h->ev_step);
+    h->launches += nl;
+    CK(cudaGetLastError());
+    if (h->prof)
+        h->step_bytes += double(l) * 92.0 * double(h->occupied ? h->occupied : std::min(h->n_tets, h->n_active));
+    h->step += l;
+    return SPG_OK;
+}
+
+// l steps with nothing of the time loop between them: segments of at most
+// seg_max steps in the mixed form (without trajectory sampling, which records
+// every step), single steps otherwise.
+int do_steps(spg_handle *h, int l) {
+    if (h->mixed && h->track_k == 0 && h->seg_max > 1 && l > 1) {
+        while (l > 0) {
+            const int m = std::min(l, h->seg_max);
+            const int rc = do_segment32(h, m);
+            if (rc) return rc;
+            l -= m;
+        }
+        return SPG_OK;
+    }
+    for (int k = 0; k < l; ++k) {
+        const int rc = do_process(h);
+        if (rc) return rc;
+    }
+    return SPG_OK;
+}
+
+// Steps from h->step to the next step at which the time loop does more than
+// step (a re-sort, or with `solves` a deposit and solve), at most `left`.
+int steps_to_event(const spg_handle *h, int64_t left, bool solves) {
+    int64_t l = left;
+    const int64_t s = h->step;
+    if (solves && h->prm.poisson_every > 0) l = std::min(l, h->prm.poisson_every - s % h->prm.poisson_every);
+    if (h->prm.resort_every > 0) l = std::min(l, h->prm.resort_every - s % h->prm.resort_every);
+    return int(std::max<int64_t>(l, 1));
+}
+
 int read_counters(spg_handle *h, DevCounters &c) {
     CK(cudaMemcpyAsync(&c, h->ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1331,6 +1401,7 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         // FP32 maps about the centroid, FP64 centroids, FP32 inner-solver arrays
         std::vector<TetRec32> r32(hm.n_tets);
         std::vector<double> cen(3 * hm.n_tets);
+        std::vector<float> cen_lo(3 * hm.n_tets);
         for (int64_t t = 0; t < hm.n_tets; ++t) {
             for (int c = 0; c < 3; ++c) {
                 double acc = 0.0;
@@ -1342,11 +1413,13 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
             for (int c = 0; c < 3; ++c) {
                 q.H[c] = 0.0f;
                 q.cen[c] = float(cen[3 * t + c]);
+                cen_lo[3 * t + c] = float(cen[3 * t + c] - double(q.cen[c]));
             }
             q.ezero = 1u;
         }
         CK(upload(&h->rec32, r32, s));
         CK(upload(&h->cen, cen, s));
+        CK(upload(&h->cen_lo, cen_lo, s));
         std::vector<float> id32(inv_diag.begin(), inv_diag.end());
         CK(upload(&h->inv_diag32, id32, s));
         CK(dalloc(&h->e32, hm.n_nodes));
@@ -1420,13 +1493,13 @@ int spg_destroy(spg_handle *h) {
                     h->node_q,   h->rho,      h->phi,      h->phi_prev,  h->phi_prev2,      h->b,         h->r,        h->z,         h->p,
                     h->phi_vac,  h->id_slot,  h->io_counter, h->grad_G, h->grad_En,
                     h->node_fix, h->efield,   h->tet_stamp, h->occ_list, h->occ_n, h->occ_gen,   h->slice_ptr, h->scol,   h->sval,
-                    h->rec32,    h->cen,      h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
+                    h->rec32,    h->cen,      h->cen_lo,   h->sval32,   h->inv_diag32, h->e32,     h->r32,       h->z32,
                     h->p32,      h->q32,      h->partials32, h->sc32,
                     h->elim_rp,  h->elim_row, h->elim_col, h->elim_val, h->land, h->gr, h->adj_x, h->adj_v,
                     h->gE,       h->lam,      h->mu,       h->dJdg,    h->sums, h->hist.tet, h->hist.vx,
                     h->hist.vy,  h->hist.vz,  h->tri_scratch, h->ctr_scratch,
                     h->q,        h->partials, h->sc,       h->tri_count, h->ctr,      h->n_alive_dev, h->sort_scratch, h->walkq_n,
-                    h->io};
+                    h->io,       h->seg_rq,   h->seg_qn};
     for (void *ptr : ptrs) cudaFree(ptr);
     for (EventSeries *s : {&h->ev_step, &h->ev_dep, &h->ev_pcg, &h->ev_ef, &h->ev_sort}) ev_destroy(*s);
     for (void *ptr : h->amg_alloc) cudaFree(ptr);
@@ -1955,11 +2028,13 @@ int spg_process(spg_handle *h, int32_t nsteps, spg_stats *stats) {
     if (!h->have_particles) return fail(h, SPG_E_STATE, "process: no particles set");
     if (nsteps < 0) return fail(h, SPG_E_INVALID, "process: nsteps < 0");
     CK(cudaSetDevice(h->device));
-    for (int32_t k = 0; k < nsteps; ++k) {
+    for (int32_t k = 0; k < nsteps;) {
         int rc = maybe_resort(h);
         if (rc) return rc;
-        rc = do_process(h);
+        const int l = steps_to_event(h, nsteps - k, false);
+        rc = do_steps(h, l);
         if (rc) return rc;
+        k += l;
     }
     return fill_stats(h, stats);
 }
@@ -1975,7 +2050,7 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
         ~InRun() { h->in_run = false; }
     } in_run(h);
     int status = SPG_OK;
-    for (int32_t k = 0; k < nsteps; ++k) {
+    for (int32_t k = 0; k < nsteps;) {
         int rc = maybe_resort(h);
         if (rc) return rc;
         if (h->step % h->prm.poisson_every == 0) {
@@ -1987,8 +2062,10 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
             else if (rc)
                 return rc;
         }
-        rc = do_process(h);
+        const int l = steps_to_event(h, nsteps - k, true);
+        rc = do_steps(h, l);
         if (rc) return rc;
+        k += l;
     }
     int rc = fill_stats(h, stats);
     return rc ? rc : status;
@@ -2383,6 +2460,13 @@ int spg_set_dirichlet(spg_handle *h, const double *g) {
     for (int64_t i = 0; i < h->n_nodes; ++i)
         if (isd[i]) h->phi_init[i] = g[i];
     cudaFree(dg);
+    return SPG_OK;
+}
+
+int spg_set_step_segments(spg_handle *h, int32_t max_steps) {
+    if (!h) return SPG_E_INVALID;
+    if (max_steps < 1 || max_steps > 64) return fail(h, SPG_E_INVALID, "set_step_segments: 1 <= max_steps <= 64");
+    h->seg_max = max_steps;
     return SPG_OK;
 }
 

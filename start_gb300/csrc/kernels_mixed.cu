@@ -8,8 +8,10 @@
 // cancellation:
 //   * a barycentric coordinate within 1e-5 of zero is recomputed in FP64
 //     (the FP64 map of the plain form, x promoted to FP64);
-//   * a face crossing re-bases the position into the neighbour's frame in
-//     FP64: x' = x + (c_old - c_new), then rounds to FP32;
+//   * a face crossing re-bases the position into the neighbour's frame,
+//     x' = x + (c_old - c_new), with the centroids as FP32 pairs and
+//     error-free sums: the FP32 rounding of the exact sum, as an FP64 sum
+//     would give it, without the FP64 pipe;
 //   * the deposit accumulates in 64-bit fixed point (exact).
 // Every other operation (push, move, collision, exit parameter) is FP32,
 // which on GB300 issues ~60x faster than FP64.
@@ -78,7 +80,8 @@ struct MixedArgs {
     int64_t n;
     const TetRec32 *rec;
     const TetRec *rec64;
-    const double *cen;  // 3 per tet
+    const double *cen;    // 3 per tet
+    const float *cen_lo;  // 3 per tet: cen - hi, hi the record's FP32 centroid
     const int4 *nbr, *ftri, *tet_nodes;
     int64_t n_tets;
 };
@@ -94,12 +97,50 @@ __device__ __forceinline__ bool inside32(const MixedArgs &a, const Geo32 &g, int
     return l[0] >= 0.0f && l[1] >= 0.0f && l[2] >= 0.0f && l[3] >= 0.0f;
 }
 
-// Re-base a local position from tet a to tet b: x + (c_a - c_b) in FP64.
-__device__ __forceinline__ void rebase(const double *__restrict__ cen, int ta, int tb, float &x, float &y,
-                                       float &z) {
-    x = float(double(x) + (cen[3 * ta] - cen[3 * tb]));
-    y = float(double(y) + (cen[3 * ta + 1] - cen[3 * tb + 1]));
-    z = float(double(z) + (cen[3 * ta + 2] - cen[3 * tb + 2]));
+// Centroid of a tet as an unevaluated FP32 pair: c = hi + lo to about 2^-48
+// relative (hi is the FP32 centroid of the tet's record).
+struct Cen2 {
+    float hx, hy, hz, lx, ly, lz;
+};
+
+__device__ __forceinline__ Cen2 load_cen2(const TetRec32 *__restrict__ rec, const float *__restrict__ cen_lo, int t) {
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(rec + t) + 3);
+    return Cen2{c.x, c.y, c.z, __ldg(cen_lo + 3 * t), __ldg(cen_lo + 3 * t + 1), __ldg(cen_lo + 3 * t + 2)};
+}
+
+// Offset c_a - c_b of one coordinate as a pair (s, e): Knuth's TwoSum gives
+// s + e = ah - bh exactly, the low parts are added to e.
+__device__ __forceinline__ void cen_diff(float ah, float al, float bh, float bl, float &s, float &e) {
+    s = ah - bh;
+    const float bb = s - ah;
+    e = ((ah - (s - bb)) + (-bh - bb)) + (al - bl);
+}
+
+// x + (s + e) rounded once in effect: TwoSum(x, s), then the low parts.
+// Equal to the FP32 rounding of the exact sum except within ~2^-48 |c| of a
+// rounding midpoint, so the re-based position is as good as one formed in
+// FP64, with FP32 operations only.
+__device__ __forceinline__ float add2(float x, float s, float e) {
+    const float t = x + s;
+    const float bb = t - x;
+    const float err = (x - (t - bb)) + (s - bb);
+    return t + (err + e);
+}
+
+// Re-base the local positions p0, p1 from tet a's frame to tet b's:
+// p + (c_a - c_b).
+__device__ __forceinline__ void rebase2(const Cen2 &a, const Cen2 &b, float &p0x, float &p0y, float &p0z, float &p1x,
+                                        float &p1y, float &p1z) {
+    float s, e;
+    cen_diff(a.hx, a.lx, b.hx, b.lx, s, e);
+    p0x = add2(p0x, s, e);
+    p1x = add2(p1x, s, e);
+    cen_diff(a.hy, a.ly, b.hy, b.ly, s, e);
+    p0y = add2(p0y, s, e);
+    p1y = add2(p1y, s, e);
+    cen_diff(a.hz, a.lz, b.hz, b.lz, s, e);
+    p0z = add2(p0z, s, e);
+    p1z = add2(p1z, s, e);
 }
 
 struct Walk32 {
@@ -109,8 +150,9 @@ struct Walk32 {
 };
 
 // Segment walk in local frames: p0, p1 are given in tet t's frame and are
-// re-based on every crossing. Same exit rule as the FP64 walk (smallest
-// crossing parameter among faces with lambda(p1) < 0, entry face excluded).
+// re-based on every crossing (FP32 pair arithmetic). Same exit rule as the
+// FP64 walk (smallest crossing parameter among faces with lambda(p1) < 0,
+// entry face excluded).
 __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float p0y, float p0z, float p1x,
                                       float p1y, float p1z, int max_cross) {
     Walk32 o;
@@ -121,6 +163,7 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
     int enter = -1;
     Geo32 g;
     load_geo32(a.rec, t, g);
+    Cen2 ca = load_cen2(a.rec, a.cen_lo, t);
     for (;;) {
         float l1[4];
         if (inside32(a, g, t, p1x, p1y, p1z, l1)) {
@@ -175,8 +218,9 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
         }
         o.crossings++;
         const int tn = nb >> 2;
-        rebase(a.cen, t, tn, p0x, p0y, p0z);
-        rebase(a.cen, t, tn, p1x, p1y, p1z);
+        const Cen2 cb = load_cen2(a.rec, a.cen_lo, tn);
+        rebase2(ca, cb, p0x, p0y, p0z, p1x, p1y, p1z);
+        ca = cb;
         t = tn;
         enter = nb & 3;
         load_geo32(a.rec, t, g);
@@ -206,10 +250,11 @@ __device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t i
     return true;
 }
 
-// Collision in FP32 (same Philox streams and laws as the FP64 form).
-__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, float &vx, float &vy, float &vz) {
+// Collision of step `step` in FP32 (same Philox streams and laws as the FP64 form).
+__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, float &vx, float &vy,
+                                          float &vz) {
     float xc, xs, cp, sp;
-    if (!collision_event32(c, id, uint64_t(c.step), vx, vy, vz, xc, xs, cp, sp)) return false;
+    if (!collision_event32(c, id, step, vx, vy, vz, xc, xs, cp, sp)) return false;
     const float mcp = c.mass_cp_f, mct = c.mass_ct_f;
     const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
     const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
@@ -327,7 +372,7 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
                 a.p.y[i] = ny;
                 a.p.z[i] = nz;
             }
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, idf & kIdMask, vx, vy, vz) ? 1u : 0u;
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, idf & kIdMask, uint64_t(c.step), vx, vy, vz) ? 1u : 0u;
         }
         a.p.vx[i] = vx;
         a.p.vy[i] = vy;
@@ -412,6 +457,243 @@ __global__ void __launch_bounds__(128) k_walk_queue32(MixedArgs a, int max_cross
         if (s2) atomicAdd(&ctr->lost, s2);
         if (s3) atomicAdd(&ctr->capped, s3);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Segmented step: every step between two events of the time loop (a solve,
+// a re-sort, the end of the call) in one pass over the particles. A particle
+// keeps its state and its tet's record in registers and leaves the pass at
+// the first step whose move needs the exact walk; it is queued with that
+// step's index, the walk kernel walks it, and a resume pass runs it on from
+// the next step. Each pass reads only fields that earlier launches wrote (a
+// walk computes the field of the tet it enters; the particle is stepped
+// there in the next launch), and every particle goes through the same FP32
+// operations in the same order as in single steps, so the result is
+// bit-identical to stepping one step per launch.
+
+constexpr int kMaxSegment = 64;  // steps per segment at most
+
+struct SegItem32 {  // a move of step s0 + step that needs the walk
+    int32_t i, step;
+    float x0, y0, z0;
+};
+
+struct SegQueues {
+    SegItem32 *wq;           // walk items of the current round (at most one per particle)
+    int2 *rq;                // resumed particles: {index, first step}
+    unsigned int *wq_n;      // [L + 1]: walk items of round r
+    unsigned int *rq_n;      // [L]: resumed particles of round r
+    int L;                   // steps of the segment (steps s0 .. s0 + L - 1)
+};
+
+__device__ __forceinline__ void queue_seg32(SegItem32 *__restrict__ q, unsigned int *__restrict__ qn, int64_t i,
+                                            int j, float x, float y, float z) {
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(qn, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    SegItem32 &w = q[base + __popc(act & ((1u << lane) - 1u))];
+    w.i = int32_t(i);
+    w.step = j;
+    w.x0 = x;
+    w.y0 = y;
+    w.z0 = z;
+}
+
+// Steps j0 .. L - 1 of particle i (state w, alive) in registers: the
+// operations of k_step32 for each step. Leaves at the segment's end, when the
+// particle is lost, when it stays put for good (too slow or outside the
+// modelling box: nothing changes it any more) or with its move queued for
+// the walk (round r's items go to wq_n[r]).
+__device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst &c, int64_t i, const Words32 &w,
+                                            int j0, const SegQueues &sq, unsigned int *__restrict__ qn,
+                                            unsigned &processed, unsigned &coll, unsigned &lost) {
+    const float4 *rp = reinterpret_cast<const float4 *>(a.rec + w.t);
+    const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
+    const Geo32 g{{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x}};
+    const bool push = !__float_as_uint(r3.w);
+    const float hx = r2.y, hy = r2.z, hz = r2.w;
+    const uint32_t id = w.idf & kIdMask;
+    float x = w.x, y = w.y, z = w.z, vx = w.vx, vy = w.vy, vz = w.vz;
+    const float vmin = c.vmin_f, dt = c.dt_f;
+    bool dirty = false;
+    for (int j = j0; j < sq.L; ++j) {
+        processed++;
+        const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
+        const float gx = r3.x + x, gy = r3.y + y, gz = r3.z + z;
+        const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
+                            gz >= c.lo_f[2] && gz <= c.hi_f[2];
+        if (slow || !in_box) {
+            processed += unsigned(sq.L - 1 - j);
+            break;
+        }
+        if (push) {
+            vx = (vx + hx) + hx;
+            vy = (vy + hy) + hy;
+            vz = (vz + hz) + hz;
+            dirty = true;
+        }
+        const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
+        if (nx == x && ny == y && nz == z) continue;
+        const uint64_t step = uint64_t(c.step) + uint64_t(j);
+        if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
+            a.p.idf[i] = w.idf | kLost;
+            lost++;
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, vx, vy, vz) ? 1u : 0u;
+            a.p.x[i] = x;
+            a.p.y[i] = y;
+            a.p.z[i] = z;
+            a.p.vx[i] = vx;
+            a.p.vy[i] = vy;
+            a.p.vz[i] = vz;
+            return;
+        }
+        float l[4];
+        bary32(g, nx, ny, nz, l);
+        const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
+        if (!(mn > kNearZero)) {
+            queue_seg32(sq.wq, qn, i, j, x, y, z);
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, vx, vy, vz) ? 1u : 0u;
+            a.p.x[i] = nx;
+            a.p.y[i] = ny;
+            a.p.z[i] = nz;
+            a.p.vx[i] = vx;
+            a.p.vy[i] = vy;
+            a.p.vz[i] = vz;
+            return;
+        }
+        x = nx;
+        y = ny;
+        z = nz;
+        if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, vx, vy, vz) ? 1u : 0u;
+        dirty = true;
+    }
+    if (dirty) {
+        a.p.x[i] = x;
+        a.p.y[i] = y;
+        a.p.z[i] = z;
+        a.p.vx[i] = vx;
+        a.p.vy[i] = vy;
+        a.p.vz[i] = vz;
+    }
+}
+
+__device__ __forceinline__ void add_step_counters(DevCounters *ctr, unsigned processed, unsigned coll,
+                                                  unsigned lost) {
+    const unsigned long long s0 = __reduce_add_sync(kFull, processed), s1 = __reduce_add_sync(kFull, coll);
+    const unsigned long long s2 = __reduce_add_sync(kFull, lost);
+    if ((threadIdx.x & 31) == 0) {
+        if (s0) atomicAdd(&ctr->processed, s0);
+        if (s1) atomicAdd(&ctr->collisions, s1);
+        if (s2) atomicAdd(&ctr->lost, s2);
+    }
+}
+
+// The segment's first pass over every particle (grid-stride, the next
+// particle's words loaded before the current one is stepped).
+__global__ void __launch_bounds__(256, 3) k_seg32(MixedArgs a, StepConst c, SegQueues sq, DevCounters *ctr) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    unsigned processed = 0, coll = 0, lost = 0;
+    Words32 cur{};
+    if (i < a.n) cur = load_words32(a.p, i);
+    for (; i < a.n; i += stride) {
+        Words32 nxt{};
+        if (i + stride < a.n) nxt = load_words32(a.p, i + stride);
+        if (!(cur.idf & kDead)) seg_steps32(a, c, i, cur, 0, sq, sq.wq_n, processed, coll, lost);
+        cur = nxt;
+    }
+    add_step_counters(ctr, processed, coll, lost);
+}
+
+// Round r's walks (the queued moves, each of its own step); a particle still
+// inside with steps left is listed for the resume pass of round r.
+__global__ void __launch_bounds__(128) k_seg_walk32(MixedArgs a, int max_cross, SegQueues sq, int r,
+                                                    unsigned int *__restrict__ tri_count, DevCounters *ctr,
+                                                    const __grid_constant__ FieldArgs f) {
+    const unsigned nq = sq.wq_n[r];
+    unsigned cross = 0, settled = 0, lost = 0, capped = 0;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const SegItem32 it = sq.wq[q];
+        const int64_t i = it.i;
+        const int t = a.p.tet[i];
+        const Walk32 w = walk32(a, t, it.x0, it.y0, it.z0, a.p.x[i], a.p.y[i], a.p.z[i], max_cross);
+        cross += unsigned(w.crossings);
+        a.p.x[i] = w.hx;
+        a.p.y[i] = w.hy;
+        a.p.z[i] = w.hz;
+        const uint32_t idf = a.p.idf[i];
+        if (w.status == W_SURFACE) {
+            atomicAdd(tri_count + w.tri, 1u);
+            a.p.idf[i] = idf | kSettled;
+            settled++;
+        } else if (w.status != W_INSIDE) {
+            a.p.idf[i] = idf | kLost;
+            lost++;
+            if (w.status == W_CAP) capped++;
+        }
+        if (w.tet != t) {
+            a.p.tet[i] = w.tet;
+            if (w.status == W_INSIDE) refresh_tet(f.stamp, f.epoch, w.tet, [&f](int tt) { field_of_tet32(f, tt); });
+        }
+        if (w.status == W_INSIDE && it.step + 1 < sq.L) {
+            const unsigned act = __activemask();
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(act) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(sq.rq_n + r, unsigned(__popc(act)));
+            base = __shfl_sync(act, base, leader);
+            sq.rq[base + __popc(act & ((1u << lane) - 1u))] = make_int2(int(i), it.step + 1);
+        }
+    }
+    const unsigned long long s0 = __reduce_add_sync(kFull, cross), s1 = __reduce_add_sync(kFull, settled);
+    const unsigned long long s2 = __reduce_add_sync(kFull, lost), s3 = __reduce_add_sync(kFull, capped);
+    if ((threadIdx.x & 31) == 0) {
+        if (s0) atomicAdd(&ctr->crossings, s0);
+        if (s1) atomicAdd(&ctr->settled, s1);
+        if (s2) atomicAdd(&ctr->lost, s2);
+        if (s3) atomicAdd(&ctr->capped, s3);
+    }
+}
+
+// Round r's resume pass: the walked particles run on in registers from the
+// step after their walk; their next walk goes to round r + 1. Each block
+// orders its 256 items by first step (a counting sort in shared memory), so
+// the lanes of a warp run nearly the same steps.
+__global__ void __launch_bounds__(256, 3) k_seg_resume32(MixedArgs a, StepConst c, SegQueues sq, int r,
+                                                         DevCounters *ctr) {
+    __shared__ int2 items[256];
+    __shared__ unsigned int cnt[kMaxSegment + 1];
+    const unsigned nr = sq.rq_n[r];
+    unsigned processed = 0, coll = 0, lost = 0;
+    for (unsigned base = blockIdx.x * 256u; base < nr; base += gridDim.x * 256u) {
+        for (int k = threadIdx.x; k <= sq.L; k += 256) cnt[k] = 0;
+        __syncthreads();
+        const unsigned q = base + threadIdx.x;
+        const int2 it = q < nr ? sq.rq[q] : make_int2(-1, sq.L);
+        const unsigned rank = atomicAdd(&cnt[it.y], 1u);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned acc = 0;
+            for (int k = 0; k <= sq.L; ++k) {
+                const unsigned v = cnt[k];
+                cnt[k] = acc;
+                acc += v;
+            }
+        }
+        __syncthreads();
+        items[cnt[it.y] + rank] = it;
+        __syncthreads();
+        const int2 mine = items[threadIdx.x];
+        if (mine.x >= 0) {
+            const Words32 w = load_words32(a.p, mine.x);
+            seg_steps32(a, c, mine.x, w, mine.y, sq, sq.wq_n + r + 1, processed, coll, lost);
+        }
+        __syncthreads();
+    }
+    add_step_counters(ctr, processed, coll, lost);
 }
 
 // round(x * 2^k) of a float with integer ops (round half away from zero).
@@ -709,6 +991,7 @@ MixedArgs make_args(const DevParticles32 &p, int64_t n, const MeshDev32 &m) {
     a.rec = m.rec;
     a.rec64 = m.rec64;
     a.cen = m.cen;
+    a.cen_lo = m.cen_lo;
     a.nbr = m.nbr;
     a.ftri = m.ftri;
     a.tet_nodes = m.tet_nodes;
@@ -736,6 +1019,45 @@ void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const
     k_step32<<<grid, 256, 0, s>>>(a, c, static_cast<WalkItem32 *>(wq), wq_n, ctr);
     k_walk_queue32<<<152 * 8, 128, 0, s>>>(a, c.max_cross, static_cast<WalkItem32 *>(wq), wq_n, tri_count, ctr,
                                             land, c.step, f);
+}
+
+int launch_segment32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c, int L,
+                     unsigned int *tri_count, void *wq, int2 *rq, unsigned int *q_n, DevCounters *ctr,
+                     const FieldArgs &f, cudaStream_t s) {
+    if (n <= 0 || L <= 0 || L > kMaxSegment) return 0;
+    const MixedArgs a = make_args(p, n, m);
+    SegQueues sq;
+    sq.wq = static_cast<SegItem32 *>(wq);
+    sq.rq = rq;
+    sq.wq_n = q_n;
+    sq.rq_n = q_n + L + 1;
+    sq.L = L;
+    cudaMemsetAsync(q_n, 0, sizeof(unsigned int) * size_t(2 * L + 1), s);
+    // one wave of each kernel: SMs x resident blocks (same on every device of this build)
+    static int seg_blocks = 0, walk_blocks = 0, resume_blocks = 0;
+    if (!seg_blocks) {
+        int dev = 0, sms = 0, b0 = 0, b1 = 0, b2 = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_seg32, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_seg_walk32, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_seg_resume32, 256, 0);
+        walk_blocks = std::max(1, sms * std::max(1, b1));
+        resume_blocks = std::max(1, sms * std::max(1, b2));
+        seg_blocks = std::max(1, sms * std::max(1, b0));
+    }
+    const unsigned grid = unsigned(std::min<int64_t>(grid_for(n, 256), seg_blocks));
+    k_seg32<<<grid, 256, 0, s>>>(a, c, sq, ctr);
+    int launches = 1;
+    for (int r = 0; r < L; ++r) {
+        k_seg_walk32<<<walk_blocks, 128, 0, s>>>(a, c.max_cross, sq, r, tri_count, ctr, f);
+        ++launches;
+        if (r + 1 < L) {
+            k_seg_resume32<<<resume_blocks, 256, 0, s>>>(a, c, sq, r, ctr);
+            ++launches;
+        }
+    }
+    return launches;
 }
 
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,

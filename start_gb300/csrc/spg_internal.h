@@ -306,6 +306,7 @@ struct MeshDev32 {
     const TetRec32 *rec;
     const TetRec *rec64;  // FP64 map for near-zero barycentric tests
     const double *cen;    // FP64 centroids, 3 per tet
+    const float *cen_lo;  // 3 per tet: cen - float(cen), for re-basing in FP32 pairs
     const int4 *nbr, *ftri, *tet_nodes;
     int64_t n_tets;
 };
@@ -315,6 +316,14 @@ void launch_step32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const
                    unsigned int *tri_count, void *wq, unsigned int *wq_n, DevCounters *ctr, const FieldArgs &f,
                    cudaStream_t s, LandRec *land = nullptr);
 void launch_refresh32(const DevParticles32 &p, int64_t n, const FieldArgs &f, cudaStream_t s);
+// Steps c.step .. c.step + L - 1 of the mixed form with nothing between them
+// (no solve, re-sort, track record or landing record), bit-identical to L
+// launch_step32 calls: wq holds n items of 20 B, rq n int2, q_n 2 L + 1
+// counters. Returns the number of kernels launched.
+int launch_segment32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const StepConst &c, int L,
+                     unsigned int *tri_count, void *wq, int2 *rq, unsigned int *q_n, DevCounters *ctr,
+                     const FieldArgs &f, cudaStream_t s);
+
 // adjoint of the FP32 form (kernels_mixed.cu)
 void launch_record32(const DevParticles32 &p, int64_t n, const AdjHist &h, int k, cudaStream_t s);
 void launch_objective32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, const LandRec *land,

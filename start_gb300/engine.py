@@ -361,6 +361,12 @@ class StartPIC:
         position through the recovered field's gradient (spg_grad_field_gradient)."""
         self._check(self.lib.spg_grad_field_gradient(self.h, 1 if on else 0))
 
+    def set_step_segments(self, max_steps):
+        """Steps of the mixed form between two events of the loop run as
+        segments of up to max_steps steps (1: one launch per step); the
+        results do not depend on it (spg_set_step_segments)."""
+        self._check(self.lib.spg_set_step_segments(self.h, int(max_steps)))
+
     def synchronize(self):
         self._check(self.lib.spg_synchronize(self.h))
 

@@ -1,0 +1,111 @@
+"""Segmented steps of the mixed form (spg_set_step_segments) against one
+launch per step.
+
+A segment runs every step between two events of the time loop (a solve, a
+re-sort, the end of the call) with each particle in registers until a move
+needs the exact walk; the walk runs batched and the particle resumes from
+the next step. The operations per particle and step are those of the single
+step, so the bar is identity: every position, velocity, tet id and flag,
+every triangle counter and every cumulative counter equal, bit for bit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+VHS = 2
+
+
+def _pair(w, seg):
+    from start_gb300 import StartPIC
+
+    out = []
+    for m in (1, seg):
+        g = StartPIC(w.mesh, dict(w.params, precision=1))
+        g.set_step_segments(m)
+        g.set_particles(w.pos, w.vel)
+        out.append(g)
+    return out
+
+
+def _same(a, b, stats_a, stats_b):
+    pa, pb = a.particles(), b.particles()
+    for k in ("pos", "vel", "tet", "flags"):
+        assert np.array_equal(pa[k], pb[k]), k
+    assert np.array_equal(a.triangle_counts(), b.triangle_counts())
+    for k in ("step", "n_alive", "n_settled", "n_lost", "particle_steps", "collisions", "crossings", "cg_iters_total"):
+        assert stats_a[k] == stats_b[k], (k, stats_a[k], stats_b[k])
+
+
+@pytest.mark.parametrize("collisions", [False, True], ids=["collisionless", "hs"])
+def test_run_segments_identical_w0(built, collisions):
+    """Workload 0 geometry, 200 steps (solve every 10, re-sort every 20)."""
+    from start_gb300.workloads import workload0
+
+    w = workload0(n_particles=20000, collisions=collisions, steps=200)
+    w.params.update(cg_rtol=1e-12, resort_every=20)
+    if collisions:
+        w.params["gas_concentration"] *= 50.0
+    a, b = _pair(w, 32)
+    sa, sb = a.run(200), b.run(200)
+    assert sa["crossings"] > 2000 and sa["n_settled"] > 1000, sa
+    if collisions:
+        assert sa["collisions"] > 10000
+    _same(a, b, sa, sb)
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("seg", [3, 32])
+def test_run_segments_identical_vhs_reduced_w1(built, seg):
+    """Thompson energies, cosine directions, VHS argon (x10): 300 steps;
+    segments of 3 split every 10-step span into 3 + 3 + 3 + 1."""
+    from start_gb300.workloads import workload1
+
+    w = workload1(n_particles=100000, cells=20, steps=300)
+    w.params.update(cg_rtol=1e-12, collision_model=VHS)
+    w.params["gas_concentration"] *= 10.0
+    a, b = _pair(w, seg)
+    sa, sb = a.run(150), b.run(150)
+    _same(a, b, sa, sb)
+    sa, sb = a.run(150), b.run(150)
+    assert sa["collisions"] > 1000 and sa["crossings"] > 100000, sa
+    _same(a, b, sa, sb)
+    a.close()
+    b.close()
+
+
+def test_process_segments_identical(built):
+    """spg_process over re-sort boundaries, from a given potential (no solve):
+    47 steps with re-sorts every 20 steps (segments 20, 20, 7 after the
+    first step's own)."""
+    from start_gb300.workloads import workload0
+
+    w = workload0(n_particles=30000, collisions=True, steps=47)
+    w.params.update(resort_every=20)
+    w.params["gas_concentration"] *= 50.0
+    a, b = _pair(w, 32)
+    phi = np.random.default_rng(5).uniform(-300.0, 300.0, a.n_nodes)
+    for g in (a, b):
+        g.set_potential(phi)
+    a.process(1)
+    b.process(1)
+    sa, sb = a.process(46), b.process(46)
+    assert sa["crossings"] > 1000
+    _same(a, b, sa, sb)
+    a.close()
+    b.close()
+
+
+def test_segment_setting_checked(built):
+    from start_gb300 import StartPIC
+    from start_gb300.engine import PICBaseException
+    from start_gb300.workloads import workload0
+
+    w = workload0(n_particles=10, collisions=False, steps=1)
+    g = StartPIC(w.mesh, dict(w.params, precision=1))
+    for bad in (0, -3, 65):
+        with pytest.raises(PICBaseException):
+            g.set_step_segments(bad)
+    g.set_step_segments(64)
+    g.close()
