@@ -83,6 +83,15 @@ void draws(uint64_t step, uint32_t draw, uint32_t id, uint64_t seed, uint32_t ou
     philox(c, k, out);
 }
 
+// Collision test of a step: u0 = w 2^-32 with w word (step & 3) of block
+// (step >> 2, draw 2), one block per four steps of a particle. A collision's
+// angle draws: block (step, draw 1), u1 from words 0-1, u2 from words 2-3.
+double decision_u0(uint64_t step, uint32_t id, uint64_t seed) {
+    uint32_t r[4];
+    draws(step >> 2, 2u, id, seed, r);
+    return double(r[step & 3]) * (1.0 / 4294967296.0);
+}
+
 // ---------------------------------------------------------------- geometry
 // Barycentric map of a tet: lambda_{1..3} = M (p - x0); rows of M are
 // (b x c)/det, (c x a)/det, (a x b)/det with a,b,c the edge vectors from x0.
@@ -345,14 +354,10 @@ StepOut step_particle(spo_handle &h, const CollConst &cc, int64_t i, int32_t ece
     // 7. gas collision
     if (p.collision_model != SPG_COLL_NONE) {
         const double P = probability(p, cc, v);
-        uint32_t r[4];
-        draws(uint64_t(h.step), 0u, uint32_t(i), p.seed, r);
-        const double u0 = u01(r[0], r[1]);
-        if (u0 < P) {
-            const double u1 = u01(r[2], r[3]);
-            uint32_t r2[4];
-            draws(uint64_t(h.step), 1u, uint32_t(i), p.seed, r2);
-            scatter(p, cc, v, u1, u01(r2[0], r2[1]));
+        if (decision_u0(uint64_t(h.step), uint32_t(i), p.seed) < P) {
+            uint32_t r[4];
+            draws(uint64_t(h.step), 1u, uint32_t(i), p.seed, r);
+            scatter(p, cc, v, u01(r[0], r[1]), u01(r[2], r[3]));
             o.coll = 1;
         }
     }
@@ -1166,13 +1171,11 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
                 }
             } else {
                 if (p.collision_model != SPG_COLL_NONE) {
-                    uint32_t r[4];
-                    draws(uint64_t(step0 + k), 0u, uint32_t(i), p.seed, r);
-                    if (u01(r[0], r[1]) < probability(p, cc, va)) {
-                        const double u1 = u01(r[2], r[3]);
-                        uint32_t r2[4];
-                        draws(uint64_t(step0 + k), 1u, uint32_t(i), p.seed, r2);
-                        const double u2 = u01(r2[0], r2[1]);
+                    if (decision_u0(uint64_t(step0 + k), uint32_t(i), p.seed) < probability(p, cc, va)) {
+                        uint32_t r[4];
+                        draws(uint64_t(step0 + k), 1u, uint32_t(i), p.seed, r);
+                        const double u1 = u01(r[0], r[1]);
+                        const double u2 = u01(r[2], r[3]);
                         const double xc = p.collision_model == SPG_COLL_HS ? -1.0 + 2.0 * u1 : u1;
                         const double xs = std::sqrt(1.0 - xc * xc), ph = (2.0 * PI) * u2;
                         const double nh[3] = {xs * std::cos(ph), xs * std::sin(ph), xc};

@@ -227,18 +227,24 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
     }
 }
 
-// FP32 collision decision of step `step` (u0 < P) and, on a hit, the
-// scattering direction's cosine xc, sine xs and azimuth (cos, sin).
-__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, float vx, float vy,
-                                                  float vz, float &xc, float &xs, float &cp, float &sp) {
-    const Philox4 r = collision_draw(step, 0u, id, c.seed_lo, c.seed_hi);
+// Decision word of step `step` (one Philox block per four steps).
+__device__ __forceinline__ uint32_t decision_word(const StepConst &c, uint32_t id, uint64_t step) {
+    return decision_block(step, id, c.seed_lo, c.seed_hi).v[step & 3];
+}
+
+// FP32 collision decision of step `step` (u0 < P, u0 the top 24 bits of the
+// step's decision word w) and, on a hit, the scattering direction's cosine
+// xc, sine xs and azimuth (cos, sin).
+__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, uint32_t w,
+                                                  float vx, float vy, float vz, float &xc, float &xs, float &cp,
+                                                  float &sp) {
     const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
     const float P = c.kp_f * exp2f(c.pexp_f * log2f(v2));
-    const float u0 = float(r.v[0] >> 8) * 5.9604644775390625e-8f;
+    const float u0 = float(w >> 8) * 5.9604644775390625e-8f;
     if (!(u0 < P)) return false;
-    const float u1 = float(r.v[2] >> 8) * 5.9604644775390625e-8f;
-    const Philox4 r2 = collision_draw(step, 1u, id, c.seed_lo, c.seed_hi);
-    const float u2 = float(r2.v[0] >> 8) * 5.9604644775390625e-8f;
+    const Philox4 r = collision_draw(step, 1u, id, c.seed_lo, c.seed_hi);
+    const float u1 = float(r.v[0] >> 8) * 5.9604644775390625e-8f;
+    const float u2 = float(r.v[2] >> 8) * 5.9604644775390625e-8f;
     if (c.model == SPG_COLL_HS)
         xc = -1.0f + 2.0f * u1;
     else if (c.model == SPG_COLL_VHS)
@@ -250,11 +256,12 @@ __device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t i
     return true;
 }
 
-// Collision of step `step` in FP32 (same Philox streams and laws as the FP64 form).
-__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, float &vx, float &vy,
-                                          float &vz) {
+// Collision of step `step` in FP32 (same Philox streams and laws as the FP64
+// form); w is the step's decision word.
+__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, uint32_t w, float &vx,
+                                          float &vy, float &vz) {
     float xc, xs, cp, sp;
-    if (!collision_event32(c, id, step, vx, vy, vz, xc, xs, cp, sp)) return false;
+    if (!collision_event32(c, id, step, w, vx, vy, vz, xc, xs, cp, sp)) return false;
     const float mcp = c.mass_cp_f, mct = c.mass_ct_f;
     const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
     const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
@@ -372,7 +379,11 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
                 a.p.y[i] = ny;
                 a.p.z[i] = nz;
             }
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, idf & kIdMask, uint64_t(c.step), vx, vy, vz) ? 1u : 0u;
+            if (c.model != SPG_COLL_NONE) {
+                const uint32_t id = idf & kIdMask;
+                coll += collide32(c, id, uint64_t(c.step), decision_word(c, id, uint64_t(c.step)), vx, vy, vz) ? 1u
+                                                                                                               : 0u;
+            }
         }
         a.p.vx[i] = vx;
         a.p.vy[i] = vy;
@@ -519,6 +530,17 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
     float x = w.x, y = w.y, z = w.z, vx = w.vx, vy = w.vy, vz = w.vz;
     const float vmin = c.vmin_f, dt = c.dt_f;
     bool dirty = false;
+    // the decision block of the last four-step group tested (block_of: its count)
+    Philox4 blk{};
+    uint64_t block_of = ~uint64_t(0);
+    auto word = [&](uint64_t step) {
+        if ((step >> 2) != block_of) {
+            block_of = step >> 2;
+            blk = decision_block(step, id, c.seed_lo, c.seed_hi);
+        }
+        const uint32_t k = uint32_t(step & 3);
+        return k == 0 ? blk.v[0] : (k == 1 ? blk.v[1] : (k == 2 ? blk.v[2] : blk.v[3]));
+    };
     for (int j = j0; j < sq.L; ++j) {
         processed++;
         const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
@@ -541,7 +563,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
             a.p.idf[i] = w.idf | kLost;
             lost++;
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, vx, vy, vz) ? 1u : 0u;
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, word(step), vx, vy, vz) ? 1u : 0u;
             a.p.x[i] = x;
             a.p.y[i] = y;
             a.p.z[i] = z;
@@ -555,7 +577,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
         if (!(mn > kNearZero)) {
             queue_seg32(sq.wq, qn, i, j, x, y, z);
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, vx, vy, vz) ? 1u : 0u;
+            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, word(step), vx, vy, vz) ? 1u : 0u;
             a.p.x[i] = nx;
             a.p.y[i] = ny;
             a.p.z[i] = nz;
@@ -567,7 +589,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         x = nx;
         y = ny;
         z = nz;
-        if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, vx, vy, vz) ? 1u : 0u;
+        if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, word(step), vx, vy, vz) ? 1u : 0u;
         dirty = true;
     }
     if (dirty) {
@@ -924,7 +946,9 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
             bz = sdt * Az;
         } else {
             float xc, xs, cp, sp;
-            if (c.model != SPG_COLL_NONE && collision_event32(c, id, uint64_t(c.step + k), vx, vy, vz, xc, xs, cp, sp)) {
+            const uint64_t sk = uint64_t(c.step + k);
+            if (c.model != SPG_COLL_NONE &&
+                collision_event32(c, id, sk, decision_word(c, id, sk), vx, vy, vz, xc, xs, cp, sp)) {
                 // v' = m_cp v + m_ct |v| n:  J^T a = m_cp a + m_ct v/|v| (n . a)
                 const double vm = sqrt(wx * wx + wy * wy + wz * wz);
                 const double na = (double(xs * cp) * Vx + double(xs * sp) * Vy + double(xc) * Vz) * mct / vm;

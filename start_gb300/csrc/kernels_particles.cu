@@ -276,16 +276,18 @@ __device__ __noinline__ void scatter64(const StepConst c, double u1, double u2, 
     vz = ez + cmz;
 }
 
-// Gas collision decision and scattering. Draw u0 (53-bit) decides; the FP32
-// screen compares the interval of u0 known from its top 24 bits with
-// P_f (1 -+ 1e-4). P_f = kp (v^2)^pexp from 20-bit velocity components has a
-// relative error below 2e-5, so a decided screen agrees with u0 < P in FP64.
+// Gas collision decision and scattering. The step's decision word w gives
+// u0 = w 2^-32; the FP32 screen compares the interval of u0 known from its
+// top 24 bits with P_f (1 -+ 1e-4). P_f = kp (v^2)^pexp from 20-bit velocity
+// components has a relative error below 2e-5, so a decided screen agrees
+// with u0 < P in FP64.
 __device__ __forceinline__ bool collide(const StepConst &c, uint32_t id, double &vx, double &vy, double &vz) {
-    const Philox4 r = collision_draw(uint64_t(c.step), 0u, id, c.seed_lo, c.seed_hi);
+    const uint64_t step = uint64_t(c.step);
+    const uint32_t w = decision_block(step, id, c.seed_lo, c.seed_hi).v[step & 3];
     const float fx = hi_float(vx), fy = hi_float(vy), fz = hi_float(vz);
     const float v2 = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
     const float pf = c.kp_f * exp2f(c.pexp_f * log2f(v2));
-    const float ulo = float(r.v[0] >> 8) * 5.9604644775390625e-8f;  // 2^-24
+    const float ulo = float(w >> 8) * 5.9604644775390625e-8f;  // 2^-24
     const float uhi = ulo + 5.9604644775390625e-8f;
     bool hit;
     if (uhi < pf * (1.0f - 1e-4f))
@@ -293,11 +295,10 @@ __device__ __forceinline__ bool collide(const StepConst &c, uint32_t id, double 
     else if (ulo > pf * (1.0f + 1e-4f))
         hit = false;
     else
-        hit = u01_from(r.v[0], r.v[1]) < probability64(c, vx, vy, vz);
+        hit = u0_from(w) < probability64(c, vx, vy, vz);
     if (!hit) return false;
-    const double u1 = u01_from(r.v[2], r.v[3]);
-    const Philox4 r2 = collision_draw(uint64_t(c.step), 1u, id, c.seed_lo, c.seed_hi);
-    scatter64(c, u1, u01_from(r2.v[0], r2.v[1]), vx, vy, vz);
+    const Philox4 r = collision_draw(step, 1u, id, c.seed_lo, c.seed_hi);
+    scatter64(c, u01_from(r.v[0], r.v[1]), u01_from(r.v[2], r.v[3]), vx, vy, vz);
     return true;
 }
 

@@ -58,4 +58,14 @@ SPG_HD Philox4 collision_draw(uint64_t step, uint32_t draw, uint32_t id, uint32_
     return philox4x32_10(c, id, seed_lo);
 }
 
+// The collision tests of a particle's steps 4m .. 4m + 3 share one block
+// (draw 2 of count m): word (step & 3) is the test's 32-bit uniform
+// u0 = word * 2^-32. A collision's two angle draws are block (step, draw 1):
+// u1 from words 0-1, u2 from words 2-3.
+SPG_HD Philox4 decision_block(uint64_t step, uint32_t id, uint32_t seed_lo, uint32_t seed_hi) {
+    return collision_draw(step >> 2, 2u, id, seed_lo, seed_hi);
+}
+
+SPG_HD double u0_from(uint32_t w) { return double(w) * (1.0 / 4294967296.0); }
+
 }  // namespace spg
