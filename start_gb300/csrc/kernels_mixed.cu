@@ -541,6 +541,25 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         const uint32_t k = uint32_t(step & 3);
         return k == 0 ? blk.v[0] : (k == 1 ? blk.v[1] : (k == 2 ? blk.v[2] : blk.v[3]));
     };
+    // Screen of the collision test: P_f grows with v^2 (exponent pexp >= 0),
+    // so u0 >= pb, pb = P_f at a bound v2b of v^2 raised by 1e-4 (far above
+    // the few-ulp error of log2f / exp2f), decides "no collision" without
+    // evaluating P_f; below it the exact test of the single step runs. The
+    // bound is four times the v^2 at which it was last formed.
+    const bool screen = c.pexp_f >= 0.0f;
+    float v2b = -1.0f, pb = 0.0f;
+    auto collide = [&](uint64_t step) -> unsigned {
+        const uint32_t wd = word(step);
+        if (screen) {
+            const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+            if (!(v2 <= v2b)) {
+                v2b = 4.0f * v2;
+                pb = (c.kp_f * exp2f(c.pexp_f * log2f(v2b))) * 1.0001f;
+            }
+            if (!(float(wd >> 8) * 5.9604644775390625e-8f < pb)) return 0u;
+        }
+        return collide32(c, id, step, wd, vx, vy, vz) ? 1u : 0u;
+    };
     for (int j = j0; j < sq.L; ++j) {
         processed++;
         const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
@@ -563,7 +582,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
             a.p.idf[i] = w.idf | kLost;
             lost++;
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, word(step), vx, vy, vz) ? 1u : 0u;
+            if (c.model != SPG_COLL_NONE) coll += collide(step);
             a.p.x[i] = x;
             a.p.y[i] = y;
             a.p.z[i] = z;
@@ -577,7 +596,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
         if (!(mn > kNearZero)) {
             queue_seg32(sq.wq, qn, i, j, x, y, z);
-            if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, word(step), vx, vy, vz) ? 1u : 0u;
+            if (c.model != SPG_COLL_NONE) coll += collide(step);
             a.p.x[i] = nx;
             a.p.y[i] = ny;
             a.p.z[i] = nz;
@@ -589,7 +608,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         x = nx;
         y = ny;
         z = nz;
-        if (c.model != SPG_COLL_NONE) coll += collide32(c, id, step, word(step), vx, vy, vz) ? 1u : 0u;
+        if (c.model != SPG_COLL_NONE) coll += collide(step);
         dirty = true;
     }
     if (dirty) {

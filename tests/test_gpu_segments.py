@@ -37,14 +37,16 @@ def _same(a, b, stats_a, stats_b):
         assert stats_a[k] == stats_b[k], (k, stats_a[k], stats_b[k])
 
 
-@pytest.mark.parametrize("collisions", [False, True], ids=["collisionless", "hs"])
-def test_run_segments_identical_w0(built, collisions):
+@pytest.mark.parametrize("model", [0, 1, 3], ids=["collisionless", "hs", "vss"])
+def test_run_segments_identical_w0(built, model):
     """Workload 0 geometry, 200 steps (solve every 10, re-sort every 20)."""
     from start_gb300.workloads import workload0
 
+    collisions = model != 0
     w = workload0(n_particles=20000, collisions=collisions, steps=200)
     w.params.update(cg_rtol=1e-12, resort_every=20)
     if collisions:
+        w.params.update(collision_model=model)
         w.params["gas_concentration"] *= 50.0
     a, b = _pair(w, 32)
     sa, sb = a.run(200), b.run(200)
