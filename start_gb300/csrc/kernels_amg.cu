@@ -8,6 +8,7 @@
 // Operators with short rows are stored SELL-32 with one thread per row (level
 // 0 shares the solver's matrix); long rows (coarse operators, restriction)
 // CSR with 4-32 lanes per row. No atomics, so z = M^-1 r is deterministic.
+#include "pdl.cuh"
 #include "sell.cuh"
 #include "spg_internal.h"
 
@@ -18,7 +19,11 @@ namespace {
 constexpr int kT = 256;
 
 // converged: 1 or 2 (plain PCG), or 3 (inner cap of the mixed form)
-__device__ __forceinline__ bool done(const PcgScalars *sc) { return sc && *(volatile const int *)&sc->converged; }
+// (Every V-cycle kernel starts here: pdl_sync orders it after its predecessor.)
+__device__ __forceinline__ bool done(const PcgScalars *sc) {
+    pdl_sync();
+    return sc && *(volatile const int *)&sc->converged;
+}
 
 // Row `row` of M x, xf(c) = x[c]. G = 0: SELL-32, the calling thread owns
 // the row. G > 0: CSR, the G lanes of a group (lane = lane index within the
@@ -239,20 +244,20 @@ inline unsigned blocks_for(int64_t n, int g = 0) {
     return unsigned((threads + kT - 1) / kT);
 }
 
-#define SPG_AMG_DISPATCH(g, KERNEL, GRIDN, ...)                                          \
-    switch (g) {                                                                         \
-    case 4: KERNEL<T, 4><<<blocks_for(GRIDN, 4), kT, 0, s>>>(__VA_ARGS__); break;       \
-    case 8: KERNEL<T, 8><<<blocks_for(GRIDN, 8), kT, 0, s>>>(__VA_ARGS__); break;       \
-    case 16: KERNEL<T, 16><<<blocks_for(GRIDN, 16), kT, 0, s>>>(__VA_ARGS__); break;    \
-    case 32: KERNEL<T, 32><<<blocks_for(GRIDN, 32), kT, 0, s>>>(__VA_ARGS__); break;    \
-    default: KERNEL<T, 0><<<blocks_for(GRIDN, 0), kT, 0, s>>>(__VA_ARGS__); break;      \
+#define SPG_AMG_DISPATCH(g, KERNEL, GRIDN, ...)                                             \
+    switch (g) {                                                                            \
+    case 4: launch_pdl(KERNEL<T, 4>, blocks_for(GRIDN, 4), kT, s, __VA_ARGS__); break;     \
+    case 8: launch_pdl(KERNEL<T, 8>, blocks_for(GRIDN, 8), kT, s, __VA_ARGS__); break;     \
+    case 16: launch_pdl(KERNEL<T, 16>, blocks_for(GRIDN, 16), kT, s, __VA_ARGS__); break;  \
+    case 32: launch_pdl(KERNEL<T, 32>, blocks_for(GRIDN, 32), kT, s, __VA_ARGS__); break;  \
+    default: launch_pdl(KERNEL<T, 0>, blocks_for(GRIDN, 0), kT, s, __VA_ARGS__); break;    \
     }
 
 template <class T>
 void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalars *sc, cudaStream_t s) {
     const AmgLevelDevT<T> &L = a.lev[l];
     if (l == a.levels - 1) {
-        k_coarse<T><<<unsigned((a.nc * 32 + kT - 1) / kT), kT, 0, s>>>(a.coarse_inv, a.nc, b, xa, sc);
+        launch_pdl(k_coarse<T>, unsigned((a.nc * 32 + kT - 1) / kT), kT, s, a.coarse_inv, a.nc, b, xa, sc);
         return;
     }
     T *xb = L.x[1];
@@ -267,7 +272,7 @@ void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalar
         return;
     }
     if (L.degree == 1) {
-        k_jacobi0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
+        launch_pdl(k_jacobi0<T>, blocks_for(L.n), kT, s, L, b, xa, sc);
         SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xa, sc)
         SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
         vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
@@ -275,7 +280,7 @@ void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalar
         SPG_AMG_DISPATCH(ga, k_jacobi_step, L.n, L, b, xb, xa, sc)
         return;
     }
-    k_cheb0<T><<<blocks_for(L.n), kT, 0, s>>>(L, b, xa, sc);
+    launch_pdl(k_cheb0<T>, blocks_for(L.n), kT, s, L, b, xa, sc);
     SPG_AMG_DISPATCH(ga, k_cheb_step, L.n, L, b, xa, xb, L.cheb_a, L.cheb_b, sc)
     SPG_AMG_DISPATCH(ga, k_resid, L.n, L, b, xb, sc)
     SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "pdl.cuh"
 #include "sell.cuh"
 #include "spg_internal.h"
 
@@ -106,6 +107,7 @@ __global__ void k_node_q_from_rho(const double *__restrict__ rho, const double *
 
 // r = b - A x, z = D^-1 r, p = z; rz = r.z, bb = b.b, rr = r.r
 __global__ void __launch_bounds__(kThreads) k_setup(PcgDev d, const double *__restrict__ b) {
+    pdl_sync();
     double rz = 0.0, bb = 0.0;
     __shared__ double s_rr[kThreads / 32];
     double rr = 0.0;
@@ -149,6 +151,7 @@ __global__ void __launch_bounds__(kThreads) k_setup(PcgDev d, const double *__re
 
 // q = A p; pq = p.q; alpha = rz / pq
 __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgDev d) {
+    pdl_sync();
     if (d.sc->converged) return;
     double pq = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
@@ -171,6 +174,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgDev d) {
 
 // x += alpha p; r -= alpha q; z = D^-1 r; rz' = r.z, rr = r.r; beta = rz'/rz
 __global__ void __launch_bounds__(kThreads) k_update(PcgDev d) {
+    pdl_sync();
     if (d.sc->converged) return;
     const double alpha = d.sc->alpha;
     double rz = 0.0, rr = 0.0;
@@ -201,6 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_update(PcgDev d) {
 
 // p = z + beta p
 __global__ void __launch_bounds__(kThreads) k_pupdate(PcgDev d) {
+    pdl_sync();
     if (d.sc->converged) return;
     const double beta = d.sc->beta;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads)
@@ -215,6 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_pupdate(PcgDev d) {
 // r = b - A x; bb = b.b, rr = r.r (z = M^-1 r follows as a V-cycle)
 template <bool M>
 __global__ void __launch_bounds__(kThreads) k_setup_amg(PcgDev d, const double *__restrict__ b, float *__restrict__ r32) {
+    pdl_sync();
     double bb = 0.0, rr = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
         const double bi = b[i];
@@ -241,6 +247,7 @@ __global__ void __launch_bounds__(kThreads) k_setup_amg(PcgDev d, const double *
 // x += alpha p; r -= alpha q; rr = r.r and the stop test
 template <bool M>
 __global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d, float *__restrict__ r32) {
+    pdl_sync();
     if (d.sc->converged) return;
     const double alpha = d.sc->alpha;
     double rr = 0.0;
@@ -266,6 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_update_amg(PcgDev d, float *__rest
 // rz' = r.z (z from the V-cycle); first: p = z; else beta = rz'/rz
 template <bool M>
 __global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, const float *__restrict__ z32, int first) {
+    pdl_sync();
     if (d.sc->converged) return;
     double rz = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
@@ -287,6 +295,7 @@ __global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, const float *__re
 
 // p = z32 + beta p (mixed form)
 __global__ void __launch_bounds__(kThreads) k_pupdate_m(PcgDev d, const float *__restrict__ z32) {
+    pdl_sync();
     if (d.sc->converged) return;
     const double beta = d.sc->beta;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads)
@@ -322,6 +331,7 @@ __device__ bool block_reduce2_w(float a, float b, double *partials, PcgScalars *
 // Outer step: r = b - A x in FP64, rr = r.r, bb = b.b; start the inner solve:
 // e = 0, r32 = r, z = D^-1 r32, p = z, rz = r32.z.
 __global__ void __launch_bounds__(kThreads) k_refine_setup(PcgDev d, PcgDev32 f, const double *__restrict__ b) {
+    pdl_sync();
     double rr = 0.0, bb = 0.0;
     float rz = 0.0f;
     __shared__ double s_rz[kThreads / 32];
@@ -367,6 +377,7 @@ __global__ void __launch_bounds__(kThreads) k_refine_setup(PcgDev d, PcgDev32 f,
 }
 
 __global__ void __launch_bounds__(kThreads) k_spmv_dot32(PcgDev32 f) {
+    pdl_sync();
     if (f.sc->converged) return;
     float pq = 0.0f;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < f.n; i += int64_t(gridDim.x) * kThreads) {
@@ -388,6 +399,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot32(PcgDev32 f) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_update32(PcgDev32 f) {
+    pdl_sync();
     if (f.sc->converged) return;
     const float alpha = float(f.sc->alpha);
     float rz = 0.0f, rr = 0.0f;
@@ -417,6 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_update32(PcgDev32 f) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_pupdate32(PcgDev32 f) {
+    pdl_sync();
     if (f.sc->converged) return;
     const float beta = float(f.sc->beta);
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < f.n; i += int64_t(gridDim.x) * kThreads)
@@ -483,42 +496,42 @@ void launch_node_q_from_rho(const double *rho, const double *dual_vol, double *n
 }
 
 void launch_pcg_setup(const PcgDev &d, const double *b, cudaStream_t s) {
-    k_setup<<<d.grid.setup, kThreads, 0, s>>>(d, b);
+    launch_pdl(k_setup, d.grid.setup, kThreads, s, d, b);
 }
 
 void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s) {
-    k_setup_amg<false><<<d.grid.setup, kThreads, 0, s>>>(d, b, nullptr);
+    launch_pdl(k_setup_amg<false>, d.grid.setup, kThreads, s, d, b, nullptr);
     launch_amg_vcycle(a, d.r, d.z, d.sc, s);
-    k_rz_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr, 1);
+    launch_pdl(k_rz_amg<false>, d.grid.update, kThreads, s, d, nullptr, 1);
 }
 
 void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s) {
-    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
-    k_update_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr);
+    launch_pdl(k_spmv_dot, d.grid.spmv, kThreads, s, d);
+    launch_pdl(k_update_amg<false>, d.grid.update, kThreads, s, d, nullptr);
     launch_amg_vcycle(a, d.r, d.z, d.sc, s);
-    k_rz_amg<false><<<d.grid.update, kThreads, 0, s>>>(d, nullptr, 0);
-    k_pupdate<<<d.grid.pupdate, kThreads, 0, s>>>(d);
+    launch_pdl(k_rz_amg<false>, d.grid.update, kThreads, s, d, nullptr, 0);
+    launch_pdl(k_pupdate, d.grid.pupdate, kThreads, s, d);
 }
 
 void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
                                 cudaStream_t s) {
-    k_setup_amg<true><<<d.grid.setup, kThreads, 0, s>>>(d, b, r32);
+    launch_pdl(k_setup_amg<true>, d.grid.setup, kThreads, s, d, b, r32);
     launch_amg_vcycle(a, r32, z32, d.sc, s);
-    k_rz_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, z32, 1);
+    launch_pdl(k_rz_amg<true>, d.grid.update, kThreads, s, d, z32, 1);
 }
 
 void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {
-    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
-    k_update_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, r32);
+    launch_pdl(k_spmv_dot, d.grid.spmv, kThreads, s, d);
+    launch_pdl(k_update_amg<true>, d.grid.update, kThreads, s, d, r32);
     launch_amg_vcycle(a, r32, z32, d.sc, s);
-    k_rz_amg<true><<<d.grid.update, kThreads, 0, s>>>(d, z32, 0);
-    k_pupdate_m<<<d.grid.pupdate, kThreads, 0, s>>>(d, z32);
+    launch_pdl(k_rz_amg<true>, d.grid.update, kThreads, s, d, z32, 0);
+    launch_pdl(k_pupdate_m, d.grid.pupdate, kThreads, s, d, z32);
 }
 
 void launch_pcg_iteration(PcgDev &d, cudaStream_t s) {
-    k_spmv_dot<<<d.grid.spmv, kThreads, 0, s>>>(d);
-    k_update<<<d.grid.update, kThreads, 0, s>>>(d);
-    k_pupdate<<<d.grid.pupdate, kThreads, 0, s>>>(d);
+    launch_pdl(k_spmv_dot, d.grid.spmv, kThreads, s, d);
+    launch_pdl(k_update, d.grid.update, kThreads, s, d);
+    launch_pdl(k_pupdate, d.grid.pupdate, kThreads, s, d);
 }
 
 // Entries that are exactly zero off the diagonal are left out (the P1
@@ -581,13 +594,13 @@ void build_sell32(int64_t n, const int64_t *row_ptr, const int32_t *col, const d
 namespace spg {
 
 void launch_refine_setup(const PcgDev &d, const PcgDev32 &f, const double *b, cudaStream_t s) {
-    k_refine_setup<<<f.grid.setup, kThreads, 0, s>>>(d, f, b);
+    launch_pdl(k_refine_setup, f.grid.setup, kThreads, s, d, f, b);
 }
 
 void launch_pcg32_iteration(PcgDev32 &f, cudaStream_t s) {
-    k_spmv_dot32<<<f.grid.spmv, kThreads, 0, s>>>(f);
-    k_update32<<<f.grid.update, kThreads, 0, s>>>(f);
-    k_pupdate32<<<f.grid.pupdate, kThreads, 0, s>>>(f);
+    launch_pdl(k_spmv_dot32, f.grid.spmv, kThreads, s, f);
+    launch_pdl(k_update32, f.grid.update, kThreads, s, f);
+    launch_pdl(k_pupdate32, f.grid.pupdate, kThreads, s, f);
 }
 
 PcgGrid pcg_grid32(int64_t n) {
