@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "pdl.cuh"
 #include "philox.h"
 #include "deposit.cuh"
 #include "field.cuh"
@@ -654,6 +655,7 @@ __global__ void __launch_bounds__(256, 3) k_seg32(MixedArgs a, StepConst c, SegQ
 __global__ void __launch_bounds__(128) k_seg_walk32(MixedArgs a, int max_cross, SegQueues sq, int r,
                                                     unsigned int *__restrict__ tri_count, DevCounters *ctr,
                                                     const __grid_constant__ FieldArgs f) {
+    pdl_sync();
     const unsigned nq = sq.wq_n[r];
     unsigned cross = 0, settled = 0, lost = 0, capped = 0;
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
@@ -707,6 +709,7 @@ __global__ void __launch_bounds__(256, 3) k_seg_resume32(MixedArgs a, StepConst 
                                                          DevCounters *ctr) {
     __shared__ int2 items[256];
     __shared__ unsigned int cnt[kMaxSegment + 1];
+    pdl_sync();
     const unsigned nr = sq.rq_n[r];
     unsigned processed = 0, coll = 0, lost = 0;
     for (unsigned base = blockIdx.x * 256u; base < nr; base += gridDim.x * 256u) {
@@ -1093,10 +1096,10 @@ int launch_segment32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, con
     k_seg32<<<grid, 256, 0, s>>>(a, c, sq, ctr);
     int launches = 1;
     for (int r = 0; r < L; ++r) {
-        k_seg_walk32<<<walk_blocks, 128, 0, s>>>(a, c.max_cross, sq, r, tri_count, ctr, f);
+        launch_pdl(k_seg_walk32, walk_blocks, 128, s, a, c.max_cross, sq, r, tri_count, ctr, f);
         ++launches;
         if (r + 1 < L) {
-            k_seg_resume32<<<resume_blocks, 256, 0, s>>>(a, c, sq, r, ctr);
+            launch_pdl(k_seg_resume32, resume_blocks, 256, s, a, c, sq, r, ctr);
             ++launches;
         }
     }
