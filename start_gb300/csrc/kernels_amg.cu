@@ -48,7 +48,21 @@ __device__ __forceinline__ T mat_row_f(const DevSellT<T> &M, X xf, int64_t row, 
             a0 = fma(v2, x2, a0);
             a1 = fma(v3, x3, a1);
         }
-        for (; k < k1; k += G) a0 = fma(__ldg(M.sval + k), xf(__ldg(M.scol + k)), a0);
+        // the last (at most three) entries of this lane: their column and value
+        // loads issued together, then the gathers, then the sums
+        int32_t cr[3];
+        T vr[3], xr[3];
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            const int64_t kk = k + int64_t(u) * G;
+            cr[u] = kk < k1 ? __ldg(M.scol + kk) : -1;
+            vr[u] = kk < k1 ? __ldg(M.sval + kk) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 3; ++u) xr[u] = cr[u] >= 0 ? xf(cr[u]) : T(0);
+#pragma unroll
+        for (int u = 0; u < 3; ++u)
+            if (cr[u] >= 0) a0 = fma(vr[u], xr[u], a0);
         T s = a0 + a1;
 #pragma unroll
         for (int off = G / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, G);
