@@ -702,40 +702,18 @@ __global__ void __launch_bounds__(128) k_seg_walk32(MixedArgs a, int max_cross, 
 }
 
 // Round r's resume pass: the walked particles run on in registers from the
-// step after their walk; their next walk goes to round r + 1. Each block
-// orders its 256 items by first step (a counting sort in shared memory), so
-// the lanes of a warp run nearly the same steps.
+// step after their walk; their next walk goes to round r + 1. (Ordering each
+// block's items by first step, so that a warp's lanes run the same steps,
+// cost more in block barriers than it saved in idle lanes.)
 __global__ void __launch_bounds__(256, 3) k_seg_resume32(MixedArgs a, StepConst c, SegQueues sq, int r,
                                                          DevCounters *ctr) {
-    __shared__ int2 items[256];
-    __shared__ unsigned int cnt[kMaxSegment + 1];
     pdl_sync();
     const unsigned nr = sq.rq_n[r];
     unsigned processed = 0, coll = 0, lost = 0;
-    for (unsigned base = blockIdx.x * 256u; base < nr; base += gridDim.x * 256u) {
-        for (int k = threadIdx.x; k <= sq.L; k += 256) cnt[k] = 0;
-        __syncthreads();
-        const unsigned q = base + threadIdx.x;
-        const int2 it = q < nr ? sq.rq[q] : make_int2(-1, sq.L);
-        const unsigned rank = atomicAdd(&cnt[it.y], 1u);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned acc = 0;
-            for (int k = 0; k <= sq.L; ++k) {
-                const unsigned v = cnt[k];
-                cnt[k] = acc;
-                acc += v;
-            }
-        }
-        __syncthreads();
-        items[cnt[it.y] + rank] = it;
-        __syncthreads();
-        const int2 mine = items[threadIdx.x];
-        if (mine.x >= 0) {
-            const Words32 w = load_words32(a.p, mine.x);
-            seg_steps32(a, c, mine.x, w, mine.y, sq, sq.wq_n + r + 1, processed, coll, lost);
-        }
-        __syncthreads();
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nr; q += gridDim.x * blockDim.x) {
+        const int2 it = sq.rq[q];
+        const Words32 w = load_words32(a.p, it.x);
+        seg_steps32(a, c, it.x, w, it.y, sq, sq.wq_n + r + 1, processed, coll, lost);
     }
     add_step_counters(ctr, processed, coll, lost);
 }
