@@ -522,7 +522,11 @@ void pcg_iteration_any(spg_handle *h, PcgDev &d) {
     else
         launch_pcg_iteration(d, h->stream);
 }
-int pcg_iter_launches(const spg_handle *h) { return (h->amg || h->amg32) ? 4 + h->amg_launches : 3; }
+// (with the FP32 V-cycle the last level-0 step and r.z are one kernel where level 0 allows it)
+int pcg_rz_fused(const spg_handle *h) { return h->amg32 && amg_last_step_fusable(h->amgd32) ? 1 : 0; }
+int pcg_iter_launches(const spg_handle *h) {
+    return (h->amg || h->amg32) ? 4 + h->amg_launches - pcg_rz_fused(h) : 3;
+}
 int pcg_chunk(const spg_handle *h) { return (h->amg || h->amg32) ? 2 : kPcgChunk; }
 
 // Allocates both particle buffers (and the walk queue) for n particles.
@@ -952,7 +956,7 @@ int do_solve_mixed_amg(spg_handle *h) {
     PcgDev d = pcg_dev(h);
     ev_begin(h, h->ev_pcg);
     launch_pcg_setup_amg_mixed(d, h->amgd32, h->b, h->r32, h->z32, h->stream);
-    h->launches += 2 + h->amg_launches;
+    h->launches += 2 + h->amg_launches - pcg_rz_fused(h);
     const int chunk = pcg_chunk(h);
     if (!h->pcg32_graph) {
         cudaGraph_t g = nullptr;

@@ -267,8 +267,11 @@ inline unsigned blocks_for(int64_t n, int g = 0) {
     default: launch_pdl(KERNEL<T, 0>, blocks_for(GRIDN, 0), kT, s, __VA_ARGS__); break;    \
     }
 
+// skip_last: level 0's last Jacobi step (x1 = L.x[1] -> z) is left to the
+// caller, which fuses it with the PCG's r.z (FP32 degree-1 level 0 only).
 template <class T>
-void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalars *sc, cudaStream_t s) {
+void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalars *sc, cudaStream_t s,
+                  bool skip_last = false) {
     const AmgLevelDevT<T> &L = a.lev[l];
     if (l == a.levels - 1) {
         launch_pdl(k_coarse<T>, unsigned((a.nc * 32 + kT - 1) / kT), kT, s, a.coarse_inv, a.nc, b, xa, sc);
@@ -282,6 +285,7 @@ void vcycle_level(const AmgDevT<T> &a, int l, const T *b, T *xa, const PcgScalar
         SPG_AMG_DISPATCH(L.R.g, k_restrict, L.R.n, L.R, L.r, N.b, sc)
         vcycle_level<T>(a, l + 1, N.b, N.x[0], sc, s);
         SPG_AMG_DISPATCH(L.P.g, k_prolong_j, L.P.n, L, b, N.x[0], xb, sc)
+        if (skip_last) return;
         SPG_AMG_DISPATCH(ga, k_jacobi_step, L.n, L, b, xb, xa, sc)
         return;
     }
@@ -312,6 +316,12 @@ void launch_amg_vcycle(const AmgDev &a, const double *r, double *z, const PcgSca
 
 void launch_amg_vcycle(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s) {
     vcycle_level<float>(a, 0, r, z, sc, s);
+}
+
+bool amg_last_step_fusable(const AmgDev32 &a) { return a.levels > 1 && a.lev[0].degree == 1 && a.lev[0].A.g == 0; }
+
+void launch_amg_vcycle_but_last(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s) {
+    vcycle_level<float>(a, 0, r, z, sc, s, true);
 }
 
 }  // namespace spg

@@ -293,6 +293,33 @@ __global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, const float *__re
     }
 }
 
+// The V-cycle's last level-0 Jacobi step z32 = x1 + D^-1 (r32 - A x1) / theta
+// (k_jacobi_step's arithmetic) fused with k_rz_amg: rz' = r.z (FP64 r, z
+// promoted), first: p = z; else beta = rz'/rz.
+template <int First>
+__global__ void __launch_bounds__(kThreads) k_jacobi_rz(PcgDev d, const AmgLevelDevT<float> L,
+                                                        const float *__restrict__ r32, float *__restrict__ z32) {
+    pdl_sync();
+    if (d.sc->converged) return;
+    const float *xin = L.x[1];
+    double rz = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
+        const float ax = spmv_row_sell<float>(L.A.slice_ptr, L.A.scol, L.A.sval, xin, i);
+        const float rr = r32[i] - ax;
+        const float zi = xin[i] + float(L.inv_theta) * (L.dinv[i] * rr);
+        z32[i] = zi;
+        const double zd = double(zi);
+        rz += d.r[i] * zd;
+        if (First) d.p[i] = zd;
+    }
+    double tot[2];
+    if (block_reduce2(rz, 0.0, d.partials, d.sc, tot)) {
+        PcgScalars *sc = d.sc;
+        if (!First) sc->beta = tot[0] / sc->rz;
+        sc->rz = tot[0];
+    }
+}
+
 // p = z32 + beta p (mixed form)
 __global__ void __launch_bounds__(kThreads) k_pupdate_m(PcgDev d, const float *__restrict__ z32) {
     pdl_sync();
@@ -513,18 +540,31 @@ void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s) {
     launch_pdl(k_pupdate, d.grid.pupdate, kThreads, s, d);
 }
 
+// z32 = M^-1 r32 and r.z: the V-cycle's last step fused with the sum where
+// level 0 allows it, else the whole V-cycle and k_rz_amg.
+static void vcycle_rz(PcgDev d, const AmgDev32 &a, float *r32, float *z32, int first, cudaStream_t s) {
+    if (amg_last_step_fusable(a)) {
+        launch_amg_vcycle_but_last(a, r32, z32, d.sc, s);
+        if (first)
+            launch_pdl(k_jacobi_rz<1>, d.grid.update, kThreads, s, d, a.lev[0], r32, z32);
+        else
+            launch_pdl(k_jacobi_rz<0>, d.grid.update, kThreads, s, d, a.lev[0], r32, z32);
+    } else {
+        launch_amg_vcycle(a, r32, z32, d.sc, s);
+        launch_pdl(k_rz_amg<true>, d.grid.update, kThreads, s, d, z32, first);
+    }
+}
+
 void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
                                 cudaStream_t s) {
     launch_pdl(k_setup_amg<true>, d.grid.setup, kThreads, s, d, b, r32);
-    launch_amg_vcycle(a, r32, z32, d.sc, s);
-    launch_pdl(k_rz_amg<true>, d.grid.update, kThreads, s, d, z32, 1);
+    vcycle_rz(d, a, r32, z32, 1, s);
 }
 
 void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {
     launch_pdl(k_spmv_dot, d.grid.spmv, kThreads, s, d);
     launch_pdl(k_update_amg<true>, d.grid.update, kThreads, s, d, r32);
-    launch_amg_vcycle(a, r32, z32, d.sc, s);
-    launch_pdl(k_rz_amg<true>, d.grid.update, kThreads, s, d, z32, 0);
+    vcycle_rz(d, a, r32, z32, 0, s);
     launch_pdl(k_pupdate_m, d.grid.pupdate, kThreads, s, d, z32);
 }
 

@@ -507,6 +507,10 @@ using AmgDev32 = AmgDevT<float>;
 // the inner cap of the mixed form, also stops it).
 void launch_amg_vcycle(const AmgDev &a, const double *r, double *z, const PcgScalars *sc, cudaStream_t s);
 void launch_amg_vcycle(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s);
+// The FP32 V-cycle without level 0's last Jacobi step, which the mixed PCG
+// then runs fused with r.z (possible when level 0 is degree 1 in SELL-32).
+bool amg_last_step_fusable(const AmgDev32 &a);
+void launch_amg_vcycle_but_last(const AmgDev32 &a, const float *r, float *z, const PcgScalars *sc, cudaStream_t s);
 // PCG with the V-cycle: setup and one iteration (spmv_dot, update, V-cycle,
 // r.z and beta, p update).
 void launch_pcg_setup_amg(const PcgDev &d, const AmgDev &a, const double *b, cudaStream_t s);
