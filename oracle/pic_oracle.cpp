@@ -83,13 +83,28 @@ void draws(uint64_t step, uint32_t draw, uint32_t id, uint64_t seed, uint32_t ou
     philox(c, k, out);
 }
 
-// Collision test of a step: u0 = w 2^-32 with w word (step & 3) of block
-// (step >> 2, draw 2), one block per four steps of a particle. A collision's
-// angle draws: block (step, draw 1), u1 from words 0-1, u2 from words 2-3.
-double decision_u0(uint64_t step, uint32_t id, uint64_t seed) {
+// Collision test of a step with probability P (q = 1/256): the step is a
+// candidate when its byte (step & 15) of block (step >> 4, draw 2) is zero;
+// P <= q: a collision iff a candidate and u_acc < 256 P (block (step, draw
+// 3)); P > q: iff a candidate or else u_f < (P - q) / (1 - q) (block (step,
+// draw 4)). Each step collides with probability P, independently. A
+// collision's angle draws: block (step, draw 1), u1 from words 0-1, u2 from
+// words 2-3.
+bool collides(uint64_t step, uint32_t id, uint64_t seed, double P) {
+    uint32_t b[4];
+    draws(step >> 4, 2u, id, seed, b);
+    const uint32_t k = uint32_t(step & 15u);
+    const uint32_t byte = (b[k >> 2] >> (8u * (k & 3u))) & 0xffu;
+    const double q = 1.0 / 256.0;
     uint32_t r[4];
-    draws(step >> 2, 2u, id, seed, r);
-    return double(r[step & 3]) * (1.0 / 4294967296.0);
+    if (P <= q) {
+        if (byte != 0u) return false;
+        draws(step, 3u, id, seed, r);
+        return u01(r[0], r[1]) < P * 256.0;
+    }
+    if (byte == 0u) return true;
+    draws(step, 4u, id, seed, r);
+    return u01(r[0], r[1]) < (P - q) / (1.0 - q);
 }
 
 // ---------------------------------------------------------------- geometry
@@ -354,7 +369,7 @@ StepOut step_particle(spo_handle &h, const CollConst &cc, int64_t i, int32_t ece
     // 7. gas collision
     if (p.collision_model != SPG_COLL_NONE) {
         const double P = probability(p, cc, v);
-        if (decision_u0(uint64_t(h.step), uint32_t(i), p.seed) < P) {
+        if (collides(uint64_t(h.step), uint32_t(i), p.seed, P)) {
             uint32_t r[4];
             draws(uint64_t(h.step), 1u, uint32_t(i), p.seed, r);
             scatter(p, cc, v, u01(r[0], r[1]), u01(r[2], r[3]));
@@ -1171,7 +1186,7 @@ int spo_grad(spo_handle *h, int32_t nsteps, const double *target, double sigma, 
                 }
             } else {
                 if (p.collision_model != SPG_COLL_NONE) {
-                    if (decision_u0(uint64_t(step0 + k), uint32_t(i), p.seed) < probability(p, cc, va)) {
+                    if (collides(uint64_t(step0 + k), uint32_t(i), p.seed, probability(p, cc, va))) {
                         uint32_t r[4];
                         draws(uint64_t(step0 + k), 1u, uint32_t(i), p.seed, r);
                         const double u1 = u01(r[0], r[1]);

@@ -682,6 +682,23 @@ StepConst step_const(const spg_handle *h) {
                        p.dt);
         c.pexp_f = float(0.5 - c.expo);
     }
+    // the FP32 probability is increasing in v^2 (pexp > 0) with a relative
+    // error far below the 2e-4 margin; rounded down to a float
+    {
+        const double q = 1.0 / 256.0 * (1.0 - 2e-4), kp = double(c.kp_f), pe = double(c.pexp_f);
+        double v2q = -1.0;
+        if (p.collision_model != SPG_COLL_NONE && kp > 0.0) {
+            if (pe > 0.0)
+                v2q = std::pow(q / kp, 1.0 / pe);
+            else if (pe == 0.0 && kp < q)
+                v2q = HUGE_VAL;
+        } else if (p.collision_model != SPG_COLL_NONE) {
+            v2q = HUGE_VAL;  // kp = 0: no collision at all
+        }
+        float f = float(v2q);
+        if (double(f) > v2q) f = std::nextafter(f, -HUGE_VALF);
+        c.v2_cand_f = f;
+    }
     return c;
 }
 

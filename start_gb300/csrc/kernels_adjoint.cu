@@ -82,7 +82,7 @@ __device__ __forceinline__ void face_normal(const TetRec &r, int f, double n[3])
 // Collision decision of step k for velocity va, exactly as the forward took
 // it (u0 < P with the reference's P), and the scattering direction.
 __device__ bool collided(const StepConst &c, uint32_t id, int64_t k, double vx, double vy, double vz, double nh[3]) {
-    const uint32_t w = decision_block(uint64_t(k), id, c.seed_lo, c.seed_hi).v[uint64_t(k) & 3];
+    const uint32_t byte = candidate_byte(candidate_block(uint64_t(k), id, c.seed_lo, c.seed_hi), uint64_t(k));
     const double vmod = sqrt(vx * vx + vy * vy + vz * vz);
     double sigma;
     if (c.model == SPG_COLL_HS) {
@@ -92,7 +92,14 @@ __device__ bool collided(const StepConst &c, uint32_t id, int64_t k, double vx, 
         sigma = kPi * (c.vhs_c1 * pow(base, c.expo));
     }
     const double P = ((sigma * vmod) * c.gas_n) * c.dt;
-    if (!(u0_from(w) < P)) return false;
+    bool hit;
+    if (P <= kCandQ) {
+        hit = byte == 0u && u01_from_block(collision_draw(uint64_t(k), 3u, id, c.seed_lo, c.seed_hi)) < P * 256.0;
+    } else {
+        hit = byte == 0u ||
+              u01_from_block(collision_draw(uint64_t(k), 4u, id, c.seed_lo, c.seed_hi)) < (P - kCandQ) / (1.0 - kCandQ);
+    }
+    if (!hit) return false;
     const Philox4 r = collision_draw(uint64_t(k), 1u, id, c.seed_lo, c.seed_hi);
     const double u1 = u01_from(r.v[0], r.v[1]);
     const double u2 = u01_from(r.v[2], r.v[3]);

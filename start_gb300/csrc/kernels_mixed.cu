@@ -228,21 +228,31 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
     }
 }
 
-// Decision word of step `step` (one Philox block per four steps).
-__device__ __forceinline__ uint32_t decision_word(const StepConst &c, uint32_t id, uint64_t step) {
-    return decision_block(step, id, c.seed_lo, c.seed_hi).v[step & 3];
+// Candidate byte of step `step` (one Philox block per sixteen steps).
+__device__ __forceinline__ uint32_t decision_byte(const StepConst &c, uint32_t id, uint64_t step) {
+    return candidate_byte(candidate_block(step, id, c.seed_lo, c.seed_hi), step);
 }
 
-// FP32 collision decision of step `step` (u0 < P, u0 the top 24 bits of the
-// step's decision word w) and, on a hit, the scattering direction's cosine
-// xc, sine xs and azimuth (cos, sin).
-__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, uint32_t w,
+// FP32 collision test of step `step` (the candidate-byte rule of philox.h
+// with P_f = kp (v^2)^pexp; `byte` is the step's candidate byte) and, on a
+// hit, the scattering direction's cosine xc, sine xs and azimuth (cos, sin).
+// A step that is no candidate with v^2 <= v2_cand_f has P_f < q: no
+// collision, decided without P_f.
+__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, uint32_t byte,
                                                   float vx, float vy, float vz, float &xc, float &xs, float &cp,
                                                   float &sp) {
+    constexpr float qf = float(kCandQ);
     const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+    if (byte != 0u && v2 <= c.v2_cand_f) return false;
     const float P = c.kp_f * exp2f(c.pexp_f * log2f(v2));
-    const float u0 = float(w >> 8) * 5.9604644775390625e-8f;
-    if (!(u0 < P)) return false;
+    bool hit;
+    if (byte == 0u)
+        hit = P > qf || float(collision_draw(step, 3u, id, c.seed_lo, c.seed_hi).v[0] >> 8) *
+                                5.9604644775390625e-8f < P * 256.0f;
+    else
+        hit = P > qf && float(collision_draw(step, 4u, id, c.seed_lo, c.seed_hi).v[0] >> 8) *
+                                5.9604644775390625e-8f < (P - qf) / (1.0f - qf);
+    if (!hit) return false;
     const Philox4 r = collision_draw(step, 1u, id, c.seed_lo, c.seed_hi);
     const float u1 = float(r.v[0] >> 8) * 5.9604644775390625e-8f;
     const float u2 = float(r.v[2] >> 8) * 5.9604644775390625e-8f;
@@ -258,11 +268,11 @@ __device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t i
 }
 
 // Collision of step `step` in FP32 (same Philox streams and laws as the FP64
-// form); w is the step's decision word.
-__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, uint32_t w, float &vx,
+// form); `byte` is the step's candidate byte.
+__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, uint32_t byte, float &vx,
                                           float &vy, float &vz) {
     float xc, xs, cp, sp;
-    if (!collision_event32(c, id, step, w, vx, vy, vz, xc, xs, cp, sp)) return false;
+    if (!collision_event32(c, id, step, byte, vx, vy, vz, xc, xs, cp, sp)) return false;
     const float mcp = c.mass_cp_f, mct = c.mass_ct_f;
     const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
     const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
@@ -382,7 +392,7 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
             }
             if (c.model != SPG_COLL_NONE) {
                 const uint32_t id = idf & kIdMask;
-                coll += collide32(c, id, uint64_t(c.step), decision_word(c, id, uint64_t(c.step)), vx, vy, vz) ? 1u
+                coll += collide32(c, id, uint64_t(c.step), decision_byte(c, id, uint64_t(c.step)), vx, vy, vz) ? 1u
                                                                                                                : 0u;
             }
         }
@@ -531,35 +541,16 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
     float x = w.x, y = w.y, z = w.z, vx = w.vx, vy = w.vy, vz = w.vz;
     const float vmin = c.vmin_f, dt = c.dt_f;
     bool dirty = false;
-    // the decision block of the last four-step group tested (block_of: its count)
+    // the candidate block of the last sixteen-step group tested (block_of: its count)
     Philox4 blk{};
     uint64_t block_of = ~uint64_t(0);
-    auto word = [&](uint64_t step) {
-        if ((step >> 2) != block_of) {
-            block_of = step >> 2;
-            blk = decision_block(step, id, c.seed_lo, c.seed_hi);
-        }
-        const uint32_t k = uint32_t(step & 3);
-        return k == 0 ? blk.v[0] : (k == 1 ? blk.v[1] : (k == 2 ? blk.v[2] : blk.v[3]));
-    };
-    // Screen of the collision test: P_f grows with v^2 (exponent pexp >= 0),
-    // so u0 >= pb, pb = P_f at a bound v2b of v^2 raised by 1e-4 (far above
-    // the few-ulp error of log2f / exp2f), decides "no collision" without
-    // evaluating P_f; below it the exact test of the single step runs. The
-    // bound is four times the v^2 at which it was last formed.
-    const bool screen = c.pexp_f >= 0.0f;
-    float v2b = -1.0f, pb = 0.0f;
     auto collide = [&](uint64_t step) -> unsigned {
-        const uint32_t wd = word(step);
-        if (screen) {
-            const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
-            if (!(v2 <= v2b)) {
-                v2b = 4.0f * v2;
-                pb = (c.kp_f * exp2f(c.pexp_f * log2f(v2b))) * 1.0001f;
-            }
-            if (!(float(wd >> 8) * 5.9604644775390625e-8f < pb)) return 0u;
+        if ((step >> 4) != block_of) {
+            block_of = step >> 4;
+            blk = candidate_block(step, id, c.seed_lo, c.seed_hi);
         }
-        return collide32(c, id, step, wd, vx, vy, vz) ? 1u : 0u;
+        const uint32_t b = candidate_byte(blk, step);
+        return collide32(c, id, step, b, vx, vy, vz) ? 1u : 0u;
     };
     for (int j = j0; j < sq.L; ++j) {
         processed++;
@@ -948,7 +939,7 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
             float xc, xs, cp, sp;
             const uint64_t sk = uint64_t(c.step + k);
             if (c.model != SPG_COLL_NONE &&
-                collision_event32(c, id, sk, decision_word(c, id, sk), vx, vy, vz, xc, xs, cp, sp)) {
+                collision_event32(c, id, sk, decision_byte(c, id, sk), vx, vy, vz, xc, xs, cp, sp)) {
                 // v' = m_cp v + m_ct |v| n:  J^T a = m_cp a + m_ct v/|v| (n . a)
                 const double vm = sqrt(wx * wx + wy * wy + wz * wz);
                 const double na = (double(xs * cp) * Vx + double(xs * sp) * Vy + double(xc) * Vz) * mct / vm;

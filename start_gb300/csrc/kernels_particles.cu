@@ -276,27 +276,54 @@ __device__ __noinline__ void scatter64(const StepConst c, double u1, double u2, 
     vz = ez + cmz;
 }
 
-// Gas collision decision and scattering. The step's decision word w gives
-// u0 = w 2^-32; the FP32 screen compares the interval of u0 known from its
-// top 24 bits with P_f (1 -+ 1e-4). P_f = kp (v^2)^pexp from 20-bit velocity
-// components has a relative error below 2e-5, so a decided screen agrees
-// with u0 < P in FP64.
+// Gas collision decision (the candidate-byte test of philox.h) and
+// scattering, bit-exact with the FP64 test and decided mostly in FP32:
+//  * a step that is no candidate (255 of 256) with v^2 at most c.v2_cand_f,
+//    computed from the 20-bit components (below the true v^2), has P below
+//    q: no collision, no FP64 instruction;
+//  * otherwise P_f = kp (v^2)^pexp from the 20-bit components (relative
+//    error below 2e-5) decides P against q outside the band q (1 -+ 1e-4),
+//    a candidate's u_acc against 256 P outside 256 P_f (1 -+ 1e-4), and
+//    u_f against (P - q) / (1 - q) outside a band of 3e-5 P_f + 2e-7;
+//  * P is computed in FP64 only inside a band.
+// The test where the common case cannot decide it: a candidate, or P that
+// may exceed q (out of line, so the step loop carries none of it).
+__device__ __noinline__ bool collision_test64(const StepConst c, uint32_t id, uint64_t step, uint32_t byte, float v2,
+                                              double vx, double vy, double vz) {
+    constexpr float qf = float(kCandQ);
+    const float pf = c.kp_f * exp2f(c.pexp_f * log2f(v2));
+    if (byte == 0u) {
+        // a candidate: P > q collides; P <= q collides iff u_acc < 256 P
+        if (pf > qf * (1.0f + 1e-4f)) return true;
+        const Philox4 r = collision_draw(step, 3u, id, c.seed_lo, c.seed_hi);
+        if (pf < qf * (1.0f - 1e-4f)) {
+            const float ulo = float(r.v[0] >> 8) * 5.9604644775390625e-8f;  // 2^-24
+            const float uhi = ulo + 5.9604644775390625e-8f;
+            const float a = pf * 256.0f;
+            if (uhi < a * (1.0f - 1e-4f)) return true;
+            if (ulo > a * (1.0f + 1e-4f)) return false;
+        }
+        const double P = probability64(c, vx, vy, vz);
+        return P > kCandQ || u01_from(r.v[0], r.v[1]) < P * 256.0;
+    }
+    if (pf < qf * (1.0f - 1e-4f)) return false;
+    const Philox4 r = collision_draw(step, 4u, id, c.seed_lo, c.seed_hi);
+    const float ulo = float(r.v[0] >> 8) * 5.9604644775390625e-8f;  // 2^-24
+    const float uhi = ulo + 5.9604644775390625e-8f;
+    const float tf = (pf - qf) / (1.0f - qf), band = 3e-5f * pf + 2e-7f;
+    if (pf > qf * (1.0f + 1e-4f) && uhi < tf - band) return true;
+    if (pf > qf * (1.0f + 1e-4f) && ulo > tf + band) return false;
+    const double P = probability64(c, vx, vy, vz);
+    return P > kCandQ && u01_from(r.v[0], r.v[1]) < (P - kCandQ) / (1.0 - kCandQ);
+}
+
 __device__ __forceinline__ bool collide(const StepConst &c, uint32_t id, double &vx, double &vy, double &vz) {
     const uint64_t step = uint64_t(c.step);
-    const uint32_t w = decision_block(step, id, c.seed_lo, c.seed_hi).v[step & 3];
+    const uint32_t byte = candidate_byte(candidate_block(step, id, c.seed_lo, c.seed_hi), step);
     const float fx = hi_float(vx), fy = hi_float(vy), fz = hi_float(vz);
     const float v2 = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
-    const float pf = c.kp_f * exp2f(c.pexp_f * log2f(v2));
-    const float ulo = float(w >> 8) * 5.9604644775390625e-8f;  // 2^-24
-    const float uhi = ulo + 5.9604644775390625e-8f;
-    bool hit;
-    if (uhi < pf * (1.0f - 1e-4f))
-        hit = true;
-    else if (ulo > pf * (1.0f + 1e-4f))
-        hit = false;
-    else
-        hit = u0_from(w) < probability64(c, vx, vy, vz);
-    if (!hit) return false;
+    if (byte != 0u && v2 <= c.v2_cand_f) return false;
+    if (!collision_test64(c, id, step, byte, v2, vx, vy, vz)) return false;
     const Philox4 r = collision_draw(step, 1u, id, c.seed_lo, c.seed_hi);
     scatter64(c, u01_from(r.v[0], r.v[1]), u01_from(r.v[2], r.v[3]), vx, vy, vz);
     return true;

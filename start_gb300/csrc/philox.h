@@ -58,14 +58,32 @@ SPG_HD Philox4 collision_draw(uint64_t step, uint32_t draw, uint32_t id, uint32_
     return philox4x32_10(c, id, seed_lo);
 }
 
-// The collision tests of a particle's steps 4m .. 4m + 3 share one block
-// (draw 2 of count m): word (step & 3) is the test's 32-bit uniform
-// u0 = word * 2^-32. A collision's two angle draws are block (step, draw 1):
-// u1 from words 0-1, u2 from words 2-3.
-SPG_HD Philox4 decision_block(uint64_t step, uint32_t id, uint32_t seed_lo, uint32_t seed_hi) {
-    return collision_draw(step >> 2, 2u, id, seed_lo, seed_hi);
+// Collision test of step s of a particle whose collision probability is P
+// (q = 1/256):
+//  * the sixteen candidate bytes of steps 16m .. 16m + 15 are one block
+//    (count m, draw 2); step s is a candidate when its byte (s & 15) is zero,
+//    probability q;
+//  * P <= q: a collision iff s is a candidate and u_acc < P / q = 256 P,
+//    u_acc from block (s, draw 3), words 0-1;
+//  * P > q: a collision iff s is a candidate or else u_f < (P - q) / (1 - q),
+//    u_f from block (s, draw 4), words 0-1;
+// so every step collides with probability exactly P, independently of the
+// others, and one Philox block serves the tests of sixteen steps. The angle
+// draws of a collision are block (s, draw 1): u1 from words 0-1, u2 from
+// words 2-3.
+constexpr double kCandQ = 1.0 / 256.0;
+
+SPG_HD Philox4 candidate_block(uint64_t step, uint32_t id, uint32_t seed_lo, uint32_t seed_hi) {
+    return collision_draw(step >> 4, 2u, id, seed_lo, seed_hi);
 }
 
-SPG_HD double u0_from(uint32_t w) { return double(w) * (1.0 / 4294967296.0); }
+// The 53-bit uniform of words 0-1 of a block.
+SPG_HD double u01_from_block(const Philox4 &r) { return u01_from(r.v[0], r.v[1]); }
+
+SPG_HD uint32_t candidate_byte(const Philox4 &b, uint64_t step) {
+    const uint32_t k = uint32_t(step & 15u);
+    const uint32_t w = k < 8u ? (k < 4u ? b.v[0] : b.v[1]) : (k < 12u ? b.v[2] : b.v[3]);
+    return (w >> (8u * (k & 3u))) & 0xffu;
+}
 
 }  // namespace spg

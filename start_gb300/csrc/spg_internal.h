@@ -135,6 +135,9 @@ struct StepConst {
     // FP32 copies for the mixed form (rounded once on the host, so no thread
     // spends FP64-pipe conversions on them)
     float lo_f[3], hi_f[3], vmin_f, dt_f, mass_cp_f, mass_ct_f, inv_alpha_f;
+    // v^2 at or below which kp (v^2)^pexp < q (1 - 2e-4), q = 1/256: a step
+    // that is no collision candidate needs no probability there (-1: none)
+    float v2_cand_f;
 };
 
 struct MeshDev {
