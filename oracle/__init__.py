@@ -70,6 +70,8 @@ def load(path: str | Path | None = None):
         "spo_collision_probability": (C.c_double, [C.POINTER(N.Params), _pd]),
         "spo_tet_map": (C.c_double, [_pd, _pd, _pd, _pd, _pd]),
         "spo_philox": (None, [_pu32, _pu32, _pu32]),
+        "spo_collides": (None, [C.POINTER(C.c_uint64), _pu32, C.c_int64, C.c_uint64, C.c_double,
+                                C.POINTER(C.c_uint8)]),
         "spo_set_ref_compat": (C.c_int, [_H, C.c_uint32, C.c_double]),
     }
     for name, (res, args) in sig.items():
@@ -328,6 +330,16 @@ def tet_map(x0, x1, x2, x3):
     M = np.zeros(9)
     det = load().spo_tet_map(*[_ptr(x, C.c_double) for x in arr], _ptr(M, C.c_double))
     return det, M.reshape(3, 3)
+
+
+def collides(steps, ids, seed, P):
+    """Collision decisions (bool array) of the (step, id) pairs at probability P."""
+    st = np.ascontiguousarray(steps, np.uint64)
+    idv = np.ascontiguousarray(ids, np.uint32)
+    out = np.zeros(len(st), np.uint8)
+    load().spo_collides(st.ctypes.data_as(C.POINTER(C.c_uint64)), _ptr(idv, C.c_uint32), len(st), int(seed),
+                        float(P), out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return out.astype(bool)
 
 
 def philox(ctr, key):

@@ -1348,6 +1348,11 @@ double spo_tet_map(const double *x0, const double *x1, const double *x2, const d
 
 void spo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox(ctr, key, out); }
 
+void spo_collides(const uint64_t *steps, const uint32_t *ids, int64_t n, uint64_t seed, double P, uint8_t *out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) out[k] = collides(steps[k], ids[k], seed, P) ? 1 : 0;
+}
+
 int spo_set_ref_compat(spo_handle *h, uint32_t flags, double cubature_w0) {
     if (!h) return fail(SPG_E_INVALID, "null handle");
     if (flags & ~uint32_t(SPO_COMPAT_ALL)) return fail(SPG_E_INVALID, "unknown compat flag");

@@ -122,6 +122,9 @@ double spo_collision_probability(const spg_params *p, const double *vel3);
 double spo_tet_map(const double *x0, const double *x1, const double *x2, const double *x3, double *M9);
 /* Philox4x32-10 block. */
 void spo_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* The collision decisions of n (step, particle id) pairs at probability P
+ * each (the candidate-byte rule of the step), 1 = a collision. */
+void spo_collides(const uint64_t *steps, const uint32_t *ids, int64_t n, uint64_t seed, double P, uint8_t *out);
 
 #ifdef __cplusplus
 }
