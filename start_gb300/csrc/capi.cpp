@@ -135,6 +135,10 @@ struct spg_handle {
     double *partials32 = nullptr;
     PcgScalars *sc32 = nullptr;
     cudaGraphExec_t pcg32_graph = nullptr;
+    // FP64 PCG with the FP32 V-cycle as one graph: a while node repeats an
+    // iteration until the device scalars say converged (no host round trip)
+    cudaGraphExec_t pcg_while = nullptr;
+    bool pcg_while_failed = false;
 
     // particles
     DevParticles P[2]{};
@@ -964,6 +968,41 @@ int do_solve64(spg_handle *h) {
 // FP32 V-cycle as the preconditioner. The V-cycle's rounding perturbs M^-1 by
 // about 1e-7 relative, far below what changes the CG iteration count, and the
 // iterate converges on the FP64 residual ||b - A x|| <= cg_rtol ||b||.
+// The while-graph of the PCG iterations (FP32 V-cycle): built once; if the
+// driver refuses a conditional node the solve keeps the chunked graph.
+void build_pcg_while(spg_handle *h, PcgDev d) {
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    cudaGraphNode_t node = nullptr;
+    cudaGraphNodeParams np = {};
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+              cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+    }
+    if (ok) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+             cudaSuccess;
+        if (ok) {
+            launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream);
+            launch_pcg_continue(cond, h->sc, h->stream);
+            ok = cudaStreamEndCapture(h->stream, &body) == cudaSuccess;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(&h->pcg_while, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        h->pcg_while = nullptr;
+        h->pcg_while_failed = true;
+        cudaGetLastError();
+    }
+}
+
 int do_solve_mixed_amg(spg_handle *h) {
     const int64_t n = h->n_nodes;
     PcgScalars init{};
@@ -974,6 +1013,20 @@ int do_solve_mixed_amg(spg_handle *h) {
     ev_begin(h, h->ev_pcg);
     launch_pcg_setup_amg_mixed(d, h->amgd32, h->b, h->r32, h->z32, h->stream);
     h->launches += 2 + h->amg_launches - pcg_rz_fused(h);
+    if (!h->pcg_while && !h->pcg_while_failed) build_pcg_while(h, d);
+    if (h->pcg_while) {
+        PcgScalars hs{};
+        CK(cudaGraphLaunch(h->pcg_while, h->stream));
+        CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        h->launches += int64_t(hs.iters + 1) * (pcg_iter_launches(h) + 1);
+        ev_end(h, h->ev_pcg);
+        if (h->prof) {  // spmv_dot 12 nnz + 24 n, update 52 n, FP32 V-cycle, r.z 12 n, p update 20 n
+            h->pcg_iters_prof += hs.iters;
+            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 108.0 * double(n) + h->amg_bytes);
+        }
+        return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
+    }
     const int chunk = pcg_chunk(h);
     if (!h->pcg32_graph) {
         cudaGraph_t g = nullptr;
@@ -1527,6 +1580,7 @@ int spg_destroy(spg_handle *h) {
     free_tracks(h);
     if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
     if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
+    if (h->pcg_while) cudaGraphExecDestroy(h->pcg_while);
     for (auto &P : h->ckpt)
         for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
                         (void *)P.tet, (void *)P.idf})

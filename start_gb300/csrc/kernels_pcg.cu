@@ -320,6 +320,12 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_rz(PcgDev d, const AmgLevel
     }
 }
 
+// The loop condition of the PCG while-graph: go on until the scalars say
+// converged (1), capped (2) or failed.
+__global__ void k_pcg_continue(cudaGraphConditionalHandle cond, const PcgScalars *sc) {
+    cudaGraphSetConditional(cond, *(volatile const int *)&sc->converged ? 0u : 1u);
+}
+
 // p = z32 + beta p (mixed form)
 __global__ void __launch_bounds__(kThreads) k_pupdate_m(PcgDev d, const float *__restrict__ z32) {
     pdl_sync();
@@ -559,6 +565,10 @@ void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double
                                 cudaStream_t s) {
     launch_pdl(k_setup_amg<true>, d.grid.setup, kThreads, s, d, b, r32);
     vcycle_rz(d, a, r32, z32, 1, s);
+}
+
+void launch_pcg_continue(cudaGraphConditionalHandle cond, const PcgScalars *sc, cudaStream_t s) {
+    k_pcg_continue<<<1, 1, 0, s>>>(cond, sc);
 }
 
 void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {

@@ -523,6 +523,8 @@ void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s);
 void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
                                 cudaStream_t s);
 void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s);
+// Last node of a PCG while-graph body: the condition stays 1 until sc->converged.
+void launch_pcg_continue(cudaGraphConditionalHandle cond, const PcgScalars *sc, cudaStream_t s);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
 void launch_pcg_rhs(const double *node_q, double inv_eps0, const double *lift, const uint8_t *is_dir,
                     const double *dir_value, double *b, int64_t n, cudaStream_t s);
