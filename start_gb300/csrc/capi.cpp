@@ -137,8 +137,8 @@ struct spg_handle {
     cudaGraphExec_t pcg32_graph = nullptr;
     // FP64 PCG with the FP32 V-cycle as one graph: a while node repeats an
     // iteration until the device scalars say converged (no host round trip)
-    cudaGraphExec_t pcg_while = nullptr;
-    bool pcg_while_failed = false;
+    cudaGraphExec_t pcg_while = nullptr, pcg64_while = nullptr;  // FP32 V-cycle; FP64 V-cycle or Jacobi
+    bool pcg_while_failed = false, pcg64_while_failed = false;
 
     // particles
     DevParticles P[2]{};
@@ -926,6 +926,44 @@ int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped
     return SPG_OK;
 }
 
+// A PCG as one graph: a while node repeats the body (one iteration, `iterate`)
+// until the device scalars say converged, capped or failed, with no host
+// round trip per iteration. Built once per solver; if the driver refuses a
+// conditional node, *failed is set and the caller keeps its chunked graph.
+template <class F>
+void build_pcg_while(spg_handle *h, F iterate, cudaGraphExec_t *exec, bool *failed) {
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    cudaGraphNode_t node = nullptr;
+    cudaGraphNodeParams np = {};
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+              cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+    }
+    if (ok) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+             cudaSuccess;
+        if (ok) {
+            iterate();
+            launch_pcg_continue(cond, h->sc, h->stream);
+            ok = cudaStreamEndCapture(h->stream, &body) == cudaSuccess;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        *exec = nullptr;
+        *failed = true;
+        cudaGetLastError();
+    }
+}
+
 int do_solve64(spg_handle *h) {
     const int64_t n = h->n_nodes;
     PcgScalars init{};
@@ -937,8 +975,15 @@ int do_solve64(spg_handle *h) {
     pcg_setup_any(h, d, h->b);
     h->launches += h->amg ? 2 + h->amg_launches : 1;
     PcgScalars hs{};
+    if (!h->pcg64_while && !h->pcg64_while_failed)
+        build_pcg_while(h, [&] { pcg_iteration_any(h, d); }, &h->pcg64_while, &h->pcg64_while_failed);
     const int chunk = pcg_chunk(h);
-    if (!h->pcg_graph) {
+    if (h->pcg64_while) {
+        CK(cudaGraphLaunch(h->pcg64_while, h->stream));
+        CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        h->launches += int64_t(hs.iters + 1) * (pcg_iter_launches(h) + 1);
+    } else if (!h->pcg_graph) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         for (int k = 0; k < chunk; ++k) pcg_iteration_any(h, d);
@@ -946,7 +991,7 @@ int do_solve64(spg_handle *h) {
         CK(cudaGraphInstantiate(&h->pcg_graph, g, 0));
         cudaGraphDestroy(g);
     }
-    for (;;) {
+    while (!h->pcg64_while) {
         CK(cudaGraphLaunch(h->pcg_graph, h->stream));
         h->launches += pcg_iter_launches(h) * chunk;
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
@@ -968,41 +1013,6 @@ int do_solve64(spg_handle *h) {
 // FP32 V-cycle as the preconditioner. The V-cycle's rounding perturbs M^-1 by
 // about 1e-7 relative, far below what changes the CG iteration count, and the
 // iterate converges on the FP64 residual ||b - A x|| <= cg_rtol ||b||.
-// The while-graph of the PCG iterations (FP32 V-cycle): built once; if the
-// driver refuses a conditional node the solve keeps the chunked graph.
-void build_pcg_while(spg_handle *h, PcgDev d) {
-    cudaGraph_t g = nullptr;
-    cudaGraphConditionalHandle cond = 0;
-    cudaGraphNode_t node = nullptr;
-    cudaGraphNodeParams np = {};
-    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
-              cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
-    if (ok) {
-        np.type = cudaGraphNodeTypeConditional;
-        np.conditional.handle = cond;
-        np.conditional.type = cudaGraphCondTypeWhile;
-        np.conditional.size = 1;
-        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
-    }
-    if (ok) {
-        cudaGraph_t body = np.conditional.phGraph_out[0];
-        ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
-             cudaSuccess;
-        if (ok) {
-            launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream);
-            launch_pcg_continue(cond, h->sc, h->stream);
-            ok = cudaStreamEndCapture(h->stream, &body) == cudaSuccess;
-        }
-    }
-    if (ok) ok = cudaGraphInstantiate(&h->pcg_while, g, 0) == cudaSuccess;
-    if (g) cudaGraphDestroy(g);
-    if (!ok) {
-        h->pcg_while = nullptr;
-        h->pcg_while_failed = true;
-        cudaGetLastError();
-    }
-}
-
 int do_solve_mixed_amg(spg_handle *h) {
     const int64_t n = h->n_nodes;
     PcgScalars init{};
@@ -1013,7 +1023,9 @@ int do_solve_mixed_amg(spg_handle *h) {
     ev_begin(h, h->ev_pcg);
     launch_pcg_setup_amg_mixed(d, h->amgd32, h->b, h->r32, h->z32, h->stream);
     h->launches += 2 + h->amg_launches - pcg_rz_fused(h);
-    if (!h->pcg_while && !h->pcg_while_failed) build_pcg_while(h, d);
+    if (!h->pcg_while && !h->pcg_while_failed)
+        build_pcg_while(h, [&] { launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream); },
+                        &h->pcg_while, &h->pcg_while_failed);
     if (h->pcg_while) {
         PcgScalars hs{};
         CK(cudaGraphLaunch(h->pcg_while, h->stream));
@@ -1581,6 +1593,7 @@ int spg_destroy(spg_handle *h) {
     if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
     if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
     if (h->pcg_while) cudaGraphExecDestroy(h->pcg_while);
+    if (h->pcg64_while) cudaGraphExecDestroy(h->pcg64_while);
     for (auto &P : h->ckpt)
         for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
                         (void *)P.tet, (void *)P.idf})
