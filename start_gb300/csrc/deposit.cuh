@@ -36,15 +36,35 @@ __device__ __forceinline__ void deposit_block_flush(int key, const long long v[4
     const unsigned grp = __match_any_sync(kAll, key);
     // Group sums of v[1..3]: each value is split into 21-bit pieces whose sums
     // over at most 32 lanes fit 32 bits (a weight is at most 2^52 in
-    // magnitude, so the signed top piece v >> 42 is at most 2^10).
-    long long sum[4];
+    // magnitude, so the signed top piece v >> 42 is at most 2^10). When every
+    // weight of the warp is below 2^41 in magnitude (one <= 2^41, more than
+    // 2e6 particles, and barycentrics in about [-1, 1]) two pieces do: the
+    // signed v >> 21 is below 2^20.
+    bool big = false;
 #pragma unroll
     for (int q = 1; q < 4; ++q) {
-        const unsigned b0 = unsigned(v[q] & 0x1FFFFF), b1 = unsigned((v[q] >> 21) & 0x1FFFFF);
-        const int b2 = int(v[q] >> 42);
-        const unsigned s0 = __reduce_add_sync(grp, b0), s1 = __reduce_add_sync(grp, b1);
-        const int s2 = __reduce_add_sync(grp, b2);
-        sum[q] = (long long)s0 + (long long)s1 * (1LL << 21) + (long long)s2 * (1LL << 42);
+        const long long t = v[q] >> 41;
+        big = big || (t != 0 && t != -1);
+    }
+    long long sum[4];
+    if (!__any_sync(kAll, big)) {
+#pragma unroll
+        for (int q = 1; q < 4; ++q) {
+            const unsigned b0 = unsigned(v[q] & 0x1FFFFF);
+            const int b1 = int(v[q] >> 21);
+            const unsigned s0 = __reduce_add_sync(grp, b0);
+            const int s1 = __reduce_add_sync(grp, b1);
+            sum[q] = (long long)s0 + (long long)s1 * (1LL << 21);
+        }
+    } else {
+#pragma unroll
+        for (int q = 1; q < 4; ++q) {
+            const unsigned b0 = unsigned(v[q] & 0x1FFFFF), b1 = unsigned((v[q] >> 21) & 0x1FFFFF);
+            const int b2 = int(v[q] >> 42);
+            const unsigned s0 = __reduce_add_sync(grp, b0), s1 = __reduce_add_sync(grp, b1);
+            const int s2 = __reduce_add_sync(grp, b2);
+            sum[q] = (long long)s0 + (long long)s1 * (1LL << 21) + (long long)s2 * (1LL << 42);
+        }
     }
     sum[0] = (long long)__popc(grp) * one - sum[1] - sum[2] - sum[3];
     __syncthreads();  // the table is cleared

@@ -709,21 +709,10 @@ __global__ void __launch_bounds__(256, 3) k_seg_resume32(MixedArgs a, StepConst 
     add_step_counters(ctr, processed, coll, lost);
 }
 
-// round(x * 2^k) of a float with integer ops (round half away from zero).
+// round(x * 2^k) of a float: the product with 2^k (k <= 52) is exact, the
+// conversion rounds to nearest even.
 __device__ __forceinline__ long long fix_round32(float x, int k) {
-    const int b = __float_as_int(x);
-    const int e = (b >> 23) & 0xff;
-    if (e == 0) return 0;
-    const long long mant = (b & 0x7fffff) | 0x800000;
-    const int sh = 150 - e - k;
-    long long r;
-    if (sh <= 0)
-        r = sh < -39 ? 0 : (mant << (-sh));
-    else if (sh > 30)
-        r = 0;
-    else
-        r = (mant + (1LL << (sh - 1))) >> sh;
-    return b < 0 ? -r : r;
+    return __float2ll_rn(x * __int_as_float((127 + k) << 23));
 }
 
 __global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned long long *__restrict__ node_fix,
