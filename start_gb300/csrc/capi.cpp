@@ -1021,11 +1021,18 @@ int do_solve_mixed_amg(spg_handle *h) {
     CK(cudaMemcpyAsync(h->sc, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     PcgDev d = pcg_dev(h);
     ev_begin(h, h->ev_pcg);
-    launch_pcg_setup_amg_mixed(d, h->amgd32, h->b, h->r32, h->z32, h->stream);
-    h->launches += 2 + h->amg_launches - pcg_rz_fused(h);
-    if (!h->pcg_while && !h->pcg_while_failed)
-        build_pcg_while(h, [&] { launch_pcg_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream); },
+    const bool rotated = pcg_rotated_ok(h->amgd32);
+    if (!h->pcg_while && !h->pcg_while_failed && rotated)
+        build_pcg_while(h, [&] { launch_pcg_rotated_iteration_amg_mixed(d, h->amgd32, h->r32, h->z32, h->stream); },
                         &h->pcg_while, &h->pcg_while_failed);
+    if (h->pcg_while) {
+        // r only; the first iteration of the graph begins with the V-cycle
+        launch_pcg_residual_amg_mixed(d, h->b, h->r32, h->stream);
+        h->launches += 1;
+    } else {
+        launch_pcg_setup_amg_mixed(d, h->amgd32, h->b, h->r32, h->z32, h->stream);
+        h->launches += 2 + h->amg_launches - pcg_rz_fused(h);
+    }
     if (h->pcg_while) {
         PcgScalars hs{};
         CK(cudaGraphLaunch(h->pcg_while, h->stream));

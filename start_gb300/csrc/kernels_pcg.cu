@@ -295,12 +295,14 @@ __global__ void __launch_bounds__(kThreads) k_rz_amg(PcgDev d, const float *__re
 
 // The V-cycle's last level-0 Jacobi step z32 = x1 + D^-1 (r32 - A x1) / theta
 // (k_jacobi_step's arithmetic) fused with k_rz_amg: rz' = r.z (FP64 r, z
-// promoted), first: p = z; else beta = rz'/rz.
-template <int First>
+// promoted), first: p = z (and beta = 0); else beta = rz'/rz. First = 2: the
+// first iteration is the one with no update yet (sc->iters == 0).
+template <int FirstArg>
 __global__ void __launch_bounds__(kThreads) k_jacobi_rz(PcgDev d, const AmgLevelDevT<float> L,
                                                         const float *__restrict__ r32, float *__restrict__ z32) {
     pdl_sync();
     if (d.sc->converged) return;
+    const bool First = FirstArg == 2 ? d.sc->iters == 0 : FirstArg == 1;
     const float *xin = L.x[1];
     double rz = 0.0;
     for (int64_t i = int64_t(blockIdx.x) * kThreads + threadIdx.x; i < d.n; i += int64_t(gridDim.x) * kThreads) {
@@ -315,7 +317,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_rz(PcgDev d, const AmgLevel
     double tot[2];
     if (block_reduce2(rz, 0.0, d.partials, d.sc, tot)) {
         PcgScalars *sc = d.sc;
-        if (!First) sc->beta = tot[0] / sc->rz;
+        sc->beta = First ? 0.0 : tot[0] / sc->rz;
         sc->rz = tot[0];
     }
 }
@@ -569,6 +571,20 @@ void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double
 
 void launch_pcg_continue(cudaGraphConditionalHandle cond, const PcgScalars *sc, cudaStream_t s) {
     k_pcg_continue<<<1, 1, 0, s>>>(cond, sc);
+}
+
+bool pcg_rotated_ok(const AmgDev32 &a) { return amg_last_step_fusable(a); }
+
+void launch_pcg_residual_amg_mixed(const PcgDev &d, const double *b, float *r32, cudaStream_t s) {
+    launch_pdl(k_setup_amg<true>, d.grid.setup, kThreads, s, d, b, r32);
+}
+
+void launch_pcg_rotated_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {
+    launch_amg_vcycle_but_last(a, r32, z32, d.sc, s);
+    launch_pdl(k_jacobi_rz<2>, d.grid.update, kThreads, s, d, a.lev[0], r32, z32);
+    launch_pdl(k_pupdate_m, d.grid.pupdate, kThreads, s, d, z32);
+    launch_pdl(k_spmv_dot, d.grid.spmv, kThreads, s, d);
+    launch_pdl(k_update_amg<true>, d.grid.update, kThreads, s, d, r32);
 }
 
 void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s) {

@@ -523,6 +523,14 @@ void launch_pcg_iteration_amg(PcgDev &d, const AmgDev &a, cudaStream_t s);
 void launch_pcg_setup_amg_mixed(const PcgDev &d, const AmgDev32 &a, const double *b, float *r32, float *z32,
                                 cudaStream_t s);
 void launch_pcg_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s);
+// The same PCG rotated for the while-graph, so that the loop stops right
+// after the update that converges: the setup only forms r (and r32); an
+// iteration is the V-cycle, r.z and beta (p = z in the first), the p update,
+// q = A p and the update of x and r with the stop test. Needs a level 0 that
+// fuses its last step with r.z (pcg_rotated_ok).
+bool pcg_rotated_ok(const AmgDev32 &a);
+void launch_pcg_residual_amg_mixed(const PcgDev &d, const double *b, float *r32, cudaStream_t s);
+void launch_pcg_rotated_iteration_amg_mixed(PcgDev &d, const AmgDev32 &a, float *r32, float *z32, cudaStream_t s);
 // Last node of a PCG while-graph body: the condition stays 1 until sc->converged.
 void launch_pcg_continue(cudaGraphConditionalHandle cond, const PcgScalars *sc, cudaStream_t s);
 // b = node_q/eps0 - lift on free rows, g on Dirichlet rows
