@@ -629,6 +629,10 @@ def run_gpu(args):
                  "breakdown_ms": {k: mp[k] for k in ("step_ms", "deposit_ms", "pcg_ms", "efield_ms", "sort_ms")},
                  "pcg_iters": mp["pcg_iters"],
                  "step_GBps": mp["step_bytes"] / (mp["step_ms"] / 1e3) / 1e9 if mp["step_ms"] > 0 else None,
+                 "step_GBps_note": ("algorithmic bytes of one step per particle-step (the state read and "
+                                    "written, the occupied tets' records); the segmented step moves the "
+                                    "state once per segment, so this effective rate exceeds its DRAM "
+                                    "traffic (profiles/k_seg32_w1_4e6ptcl.md)"),
                  "pcg_GBps": mp["pcg_bytes"] / (mp["pcg_ms"] / 1e3) / 1e9 if mp["pcg_ms"] > 0 else None,
                  "gpu_launches": mp["kernel_launches"],
                  "one_launch_per_step": single,
