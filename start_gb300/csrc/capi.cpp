@@ -928,7 +928,7 @@ int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped
 
 // A PCG as one graph: a while node repeats the body (one iteration, `iterate`)
 // until the device scalars say converged, capped or failed, with no host
-// round trip per iteration. Built once per solver; if the driver refuses a
+// round trip per iteration. Built once per solver; if the CUDA runtime refuses a
 // conditional node, *failed is set and the caller keeps its chunked graph.
 template <class F>
 void build_pcg_while(spg_handle *h, F iterate, cudaGraphExec_t *exec, bool *failed) {
