@@ -1,52 +1,58 @@
-// Block-level reduction of P1 charge contributions and the atomic flush into
-// the fixed-point node accumulators, shared by the FP64 and the mixed-form
-// deposit kernels.
+// Persistent P1 charge deposit into the fixed-point node accumulators, shared
+// by the FP64 and the mixed-form deposit kernels.
 //
-// Each thread holds one particle's fixed-point weights v[1..3] (v[0] = one -
-// v[1] - v[2] - v[3], one = 2^k) and its tet (key, -1 for none). The lanes
-// of a warp with equal keys (match_any: contiguous runs of the tet-sorted
-// order, and lanes of a tet that drifted apart since the last re-sort) are
-// summed by the integer reduce unit; the lowest lane of each group adds the
-// four node sums into a per-block hash table of nodes in shared memory, and
-// the table is flushed with one global atomic per distinct node. Integer sums
-// do not depend on order, so the result is the same as one atomic per
-// particle.
+// Each block walks one contiguous range of 256-particle tiles (the grid is
+// one wave of blocks), with the next tile's particle loads issued before the
+// current tile is reduced. A warp whose tile lies in one tet (the common case
+// in tet-sorted order: a beam puts thousands of particles in a tet) adds the
+// weights to per-lane running sums and reduces them only when its tet
+// changes. In other tiles the lanes with equal tets (match_any: the ends of
+// runs, and lanes of a tet that drifted apart since the last re-sort) are
+// summed by the integer reduce unit. Either way the lowest lane adds the four
+// node sums to the block's table of nodes in shared memory, which lives for
+// the whole range and is flushed once, with one global atomic per distinct
+// node. The table
+// takes new nodes while it is at most half full (short probe runs); past
+// that a node it does not hold goes to its global accumulator directly, so
+// a block whose range touches many nodes (particles spread over many tets)
+// degrades to one atomic per group and node. Integer sums do not depend on
+// order, so the result is the same as one atomic per particle.
 #ifndef SPG_DEPOSIT_CUH
 #define SPG_DEPOSIT_CUH
 
+#include <algorithm>
 #include <cstdint>
 
 #include "spg_internal.h"
 
 namespace spg {
 
-template <int NT>
-__device__ __forceinline__ void deposit_block_flush(int key, const long long v[4], long long one,
-                                                    const int4 *__restrict__ tet_nodes,
-                                                    unsigned long long *__restrict__ node_fix, const OccList &occ) {
+constexpr int kDepThreads = 256;
+constexpr int kDepSlots = 2048;          // node slots of a block's table
+constexpr int kDepOpen = kDepSlots / 2;  // new nodes enter while the table holds fewer
+
+struct DepositTable {
+    int node[kDepSlots];  // -1: free; a slot's node never changes once set
+    unsigned long long sum[kDepSlots];
+    unsigned int held;
+};
+
+// Sums of v[0..3] over the lanes of this lane's group (equal keys); returns
+// the group's lane mask. v[1..3] are split into 21-bit pieces whose sums over
+// at most 32 lanes fit 32 bits (a weight is at most 2^52 in magnitude, so the
+// signed top piece v >> 42 is at most 2^10). When every weight of the warp is
+// below 2^41 in magnitude (one <= 2^41, more than 2e6 particles, and
+// barycentrics in about [-1, 1]) two pieces do: the signed v >> 21 is below
+// 2^20. v[0] = one - v[1] - v[2] - v[3] sums to count * one minus the others.
+__device__ __forceinline__ unsigned group_sums(int key, const long long v[4], long long one, long long sum[4]) {
     constexpr unsigned kAll = 0xffffffffu;
-    constexpr int HS = 2 * NT;  // hash slots: node -> block sum
-    __shared__ int s_node[HS];
-    __shared__ unsigned long long s_sum[HS];
-    for (int k = threadIdx.x; k < HS; k += NT) {
-        s_node[k] = -1;
-        s_sum[k] = 0ull;
-    }
-    const int lane = threadIdx.x & 31;
     const unsigned grp = __match_any_sync(kAll, key);
-    // Group sums of v[1..3]: each value is split into 21-bit pieces whose sums
-    // over at most 32 lanes fit 32 bits (a weight is at most 2^52 in
-    // magnitude, so the signed top piece v >> 42 is at most 2^10). When every
-    // weight of the warp is below 2^41 in magnitude (one <= 2^41, more than
-    // 2e6 particles, and barycentrics in about [-1, 1]) two pieces do: the
-    // signed v >> 21 is below 2^20.
     bool big = false;
 #pragma unroll
     for (int q = 1; q < 4; ++q) {
         const long long t = v[q] >> 41;
         big = big || (t != 0 && t != -1);
     }
-    long long sum[4];
     if (!__any_sync(kAll, big)) {
 #pragma unroll
         for (int q = 1; q < 4; ++q) {
@@ -67,37 +73,163 @@ __device__ __forceinline__ void deposit_block_flush(int key, const long long v[4
         }
     }
     sum[0] = (long long)__popc(grp) * one - sum[1] - sum[2] - sum[3];
-    __syncthreads();  // the table is cleared
-    // The lowest lane of each group adds its four node sums to the block's
-    // table (open addressing, linear probing); a full table falls back to a
-    // global atomic.
-    if (key >= 0 && lane == __ffs(grp) - 1) {
-        if (occ.list && __ldcg(occ.gen_of + key) != occ.gen && atomicExch(occ.gen_of + key, occ.gen) != occ.gen)
-            occ.list[atomicAdd(occ.n, 1u)] = key;
-        const int4 tn = __ldg(tet_nodes + key);
-        const int nodes[4] = {tn.x, tn.y, tn.z, tn.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int node = nodes[q];
-            int h = int((unsigned(node) * 2654435761u) >> 8) & (HS - 1);
-            bool placed = false;
-            for (int probe = 0; probe < HS; ++probe) {
-                const int old = atomicCAS(&s_node[h], -1, node);
-                if (old == -1 || old == node) {
-                    atomicAdd(&s_sum[h], (unsigned long long)sum[q]);
-                    placed = true;
-                    break;
-                }
-                h = (h + 1) & (HS - 1);
+    return grp;
+}
+
+// Adds x to node's slot (open addressing, linear probing). A slot found free
+// is claimed by compare-and-swap only while the table is open; a closed table
+// sends a node it does not hold to the global accumulator. The probe run ends
+// at the node or a free slot: at most kDepOpen + kDepThreads slots are ever
+// taken, so a free slot exists.
+__device__ __forceinline__ void table_add(DepositTable &s, int node, unsigned long long x,
+                                          unsigned long long *__restrict__ node_fix) {
+    int h = int((unsigned(node) * 2654435761u) >> 8) & (kDepSlots - 1);
+    for (int probe = 0; probe < kDepSlots; ++probe) {
+        int cur = s.node[h];
+        if (cur == -1) {
+            if (*(volatile unsigned int *)&s.held >= unsigned(kDepOpen)) break;
+            cur = atomicCAS(&s.node[h], -1, node);
+            if (cur == -1) {
+                atomicAdd(&s.held, 1u);
+                atomicAdd(&s.sum[h], x);
+                return;
             }
-            if (!placed) atomicAdd(node_fix + node, (unsigned long long)sum[q]);
+        }
+        if (cur == node) {
+            atomicAdd(&s.sum[h], x);
+            return;
+        }
+        h = (h + 1) & (kDepSlots - 1);
+    }
+    atomicAdd(node_fix + node, x);
+}
+
+// Appends tet `key` to the list of occupied tets once per deposit (the
+// generation stamp of the tet says whether it is listed already).
+__device__ __forceinline__ void list_tet(const OccList &occ, int key) {
+    if (occ.list && __ldcg(occ.gen_of + key) != occ.gen && atomicExch(occ.gen_of + key, occ.gen) != occ.gen)
+        occ.list[atomicAdd(occ.n, 1u)] = key;
+}
+
+// Four node sums of tet `key` into the table (the lowest lane of the group
+// calls this).
+__device__ __forceinline__ void add_tet(DepositTable &s, int key, const long long sum[4],
+                                        const int4 *__restrict__ tet_nodes, unsigned long long *__restrict__ node_fix,
+                                        const OccList &occ, int &listed) {
+    if (key != listed) {
+        list_tet(occ, key);
+        listed = key;
+    }
+    const int4 tn = __ldg(tet_nodes + key);
+    table_add(s, tn.x, (unsigned long long)sum[0], node_fix);
+    table_add(s, tn.y, (unsigned long long)sum[1], node_fix);
+    table_add(s, tn.z, (unsigned long long)sum[2], node_fix);
+    table_add(s, tn.w, (unsigned long long)sum[3], node_fix);
+}
+
+// Warp sum of 64-bit values modulo 2^64 (three 21-bit pieces, the top one
+// signed): exact whenever the true sum fits 64 bits.
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+    constexpr unsigned kAll = 0xffffffffu;
+    const unsigned s0 = __reduce_add_sync(kAll, unsigned(v & 0x1FFFFFull));
+    const unsigned s1 = __reduce_add_sync(kAll, unsigned((v >> 21) & 0x1FFFFFull));
+    const int s2 = __reduce_add_sync(kAll, int((long long)v >> 42));
+    return (unsigned long long)s0 + ((unsigned long long)s1 << 21) + ((unsigned long long)(long long)s2 << 42);
+}
+
+// The warp's running sums of tet key, reduced and added to the table by lane 0.
+__device__ __forceinline__ void flush_running(DepositTable &s, int key, unsigned long long a1, unsigned long long a2,
+                                              unsigned long long a3, int acnt, long long one,
+                                              const int4 *__restrict__ tet_nodes,
+                                              unsigned long long *__restrict__ node_fix, const OccList &occ,
+                                              int &listed) {
+    long long sum[4];
+    sum[1] = (long long)warp_sum64(a1);
+    sum[2] = (long long)warp_sum64(a2);
+    sum[3] = (long long)warp_sum64(a3);
+    const unsigned long long cnt = __reduce_add_sync(0xffffffffu, unsigned(acnt));
+    sum[0] = (long long)(cnt * (unsigned long long)one - (unsigned long long)sum[1] - (unsigned long long)sum[2] -
+                         (unsigned long long)sum[3]);
+    if ((threadIdx.x & 31) == 0) add_tet(s, key, sum, tet_nodes, node_fix, occ, listed);
+}
+
+// The deposit of particles [0, n) by one block of kDepThreads threads, its
+// range of tiles given by blockIdx and gridDim. Src provides
+//   Raw load(int64_t i, int64_t n): the particle's fields (a dead marker for i >= n);
+//   int weights(const Raw &, long long v[4]): the tet (or -1: dead) and the
+//     fixed-point weights v[0..3] summing to one (zeros for a dead particle);
+//   long long one: the fixed-point one.
+// A warp whose tile holds one tet (dead lanes aside) adds the weights to its
+// lanes' running sums for that tet; the sums are reduced over the warp and
+// added to the table when the warp's tet changes (in a beam, once per some
+// hundred particles). Other tiles go through the group sums. The next tile's
+// fields are loaded before the current tile's weights are formed.
+template <class Src>
+__device__ __forceinline__ void deposit_tiles(const Src &src, int64_t n, const int4 *__restrict__ tet_nodes,
+                                              unsigned long long *__restrict__ node_fix, const OccList &occ) {
+    constexpr unsigned kAll = 0xffffffffu;
+    __shared__ DepositTable s;
+    for (int k = threadIdx.x; k < kDepSlots; k += kDepThreads) {
+        s.node[k] = -1;
+        s.sum[k] = 0ull;
+    }
+    if (threadIdx.x == 0) s.held = 0u;
+    __syncthreads();
+    const int64_t tiles = (n + kDepThreads - 1) / kDepThreads;
+    const int64_t per = (tiles + gridDim.x - 1) / gridDim.x;
+    const int64_t t0 = int64_t(blockIdx.x) * per;
+    const int64_t t1 = t0 + per < tiles ? t0 + per : tiles;
+    const int lane = threadIdx.x & 31;
+    int listed = -1;
+    int acc_key = -1;  // warp-uniform: the tet of the running sums (-1: none)
+    unsigned long long a1 = 0, a2 = 0, a3 = 0;  // modulo 2^64: the node totals fit 63 bits
+    int acnt = 0;                               // this lane's alive particles in the running sums
+    int64_t i = t0 * kDepThreads + threadIdx.x;
+    typename Src::Raw nxt = src.load(i, t0 < t1 ? n : 0);
+    for (int64_t t = t0; t < t1; ++t, i += kDepThreads) {
+        const typename Src::Raw cur = nxt;
+        nxt = src.load(i + kDepThreads, t + 1 < t1 ? n : 0);
+        long long v[4];
+        const int key = src.weights(cur, v);
+        const int kmax = __reduce_max_sync(kAll, key);
+        if (__all_sync(kAll, key == kmax || key < 0)) {
+            if (kmax != acc_key && kmax >= 0) {
+                if (acc_key >= 0) {
+                    flush_running(s, acc_key, a1, a2, a3, acnt, src.one, tet_nodes, node_fix, occ, listed);
+                }
+                acc_key = kmax;
+                a1 = a2 = a3 = 0;
+                acnt = 0;
+            }
+            a1 += (unsigned long long)v[1];
+            a2 += (unsigned long long)v[2];
+            a3 += (unsigned long long)v[3];
+            acnt += key >= 0;
+        } else {
+            long long sum[4];
+            const unsigned grp = group_sums(key, v, src.one, sum);
+            if (key >= 0 && lane == __ffs(grp) - 1) add_tet(s, key, sum, tet_nodes, node_fix, occ, listed);
         }
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < HS; k += NT) {
-        const int node = s_node[k];
-        if (node >= 0) atomicAdd(node_fix + node, s_sum[k]);
+    if (acc_key >= 0) {
+        flush_running(s, acc_key, a1, a2, a3, acnt, src.one, tet_nodes, node_fix, occ, listed);
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kDepSlots; k += kDepThreads) {
+        const int node = s.node[k];
+        const unsigned long long x = s.sum[k];
+        if (node >= 0 && x != 0ull) atomicAdd(node_fix + node, x);
+    }
+}
+
+// Blocks of `kernel` resident on the whole GPU at once (the deposit's one wave).
+template <class K>
+inline int resident_blocks(K kernel, int threads) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    return std::max(1, sms * std::max(1, per_sm));
 }
 
 }  // namespace spg

@@ -715,23 +715,48 @@ __device__ __forceinline__ long long fix_round32(float x, int k) {
     return __float2ll_rn(x * __int_as_float((127 + k) << 23));
 }
 
-__global__ void __launch_bounds__(256) k_deposit32(MixedArgs a, int k, unsigned long long *__restrict__ node_fix,
-                                                   const OccList occ) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    int key = -1;
-    long long v[4] = {0, 0, 0, 0};
-    if (i < a.n && !(a.p.idf[i] & kDead)) {
-        key = a.p.tet[i];
+// The mixed form's particles for deposit_tiles: FP32 barycentrics of the
+// tet-local position (20 B per particle).
+struct DepSrc32 {
+    struct Raw {
+        uint32_t idf;
+        int32_t tet;
+        float x, y, z;
+    };
+    DevParticles32 p;
+    const TetRec32 *rec;
+    int k;
+    long long one;
+    __device__ __forceinline__ Raw load(int64_t i, int64_t n) const {
+        Raw r{kDead, -1, 0.f, 0.f, 0.f};
+        if (i < n) {
+            r.idf = __ldg(p.idf + i);
+            r.tet = __ldg(p.tet + i);
+            r.x = __ldg(p.x + i);
+            r.y = __ldg(p.y + i);
+            r.z = __ldg(p.z + i);
+        }
+        return r;
+    }
+    __device__ __forceinline__ int weights(const Raw &r, long long v[4]) const {
+        v[0] = v[1] = v[2] = v[3] = 0;
+        if (r.idf & kDead) return -1;
         Geo32 g;
-        load_geo32(a.rec, key, g);
+        load_geo32(rec, r.tet, g);
         float l[4];
-        bary32(g, a.p.x[i], a.p.y[i], a.p.z[i], l);
+        bary32(g, r.x, r.y, r.z, l);
         v[1] = fix_round32(l[1], k);
         v[2] = fix_round32(l[2], k);
         v[3] = fix_round32(l[3], k);
-        v[0] = (1LL << k) - v[1] - v[2] - v[3];
+        v[0] = one - v[1] - v[2] - v[3];
+        return r.tet;
     }
-    deposit_block_flush<256>(key, v, 1LL << k, a.tet_nodes, node_fix, occ);
+};
+
+__global__ void __launch_bounds__(kDepThreads)
+    k_deposit32(const DepSrc32 src, int64_t n, const int4 *__restrict__ tet_nodes,
+                unsigned long long *__restrict__ node_fix, const OccList occ) {
+    deposit_tiles(src, n, tet_nodes, node_fix, occ);
 }
 
 // The field of the tets listed by the deposit (each once).
@@ -1067,7 +1092,11 @@ int launch_segment32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, con
 void launch_deposit32(const DevParticles32 &p, int64_t n, const MeshDev32 &m, int k, unsigned long long *node_fix,
                       const OccList &occ, cudaStream_t s) {
     if (n <= 0) return;
-    k_deposit32<<<grid_for(n, 256), 256, 0, s>>>(make_args(p, n, m), k, node_fix, occ);
+    static int blocks = 0;  // one wave
+    if (blocks == 0) blocks = resident_blocks(k_deposit32, kDepThreads);
+    const DepSrc32 src{p, m.rec, k, 1LL << k};
+    const unsigned grid = unsigned(std::min<int64_t>(grid_for(n, kDepThreads), blocks));
+    k_deposit32<<<grid, kDepThreads, 0, s>>>(src, n, m.tet_nodes, node_fix, occ);
 }
 
 void launch_record32(const DevParticles32 &p, int64_t n, const AdjHist &h, int k, cudaStream_t s) {

@@ -539,27 +539,50 @@ __device__ __forceinline__ long long fix_round(double x, int k) {
 // exactly 2^k and charge is conserved exactly. Integer sums do not depend on
 // summation order, so the result is the same for any particle order, grid
 // or atomic interleaving. Lanes of a warp hold consecutive (tet-sorted)
-// particles; runs of equal tet are summed over the block (deposit.cuh) and
-// the last thread of each run issues the four atomics.
-__global__ void __launch_bounds__(256) k_deposit64(DevParticles p, int64_t n, MeshDev m, int k,
-                                                   unsigned long long *__restrict__ node_fix, const OccList occ) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    int key = -1;
-    long long v[4] = {0, 0, 0, 0};
-    if (i < n && !(p.idf[i] & kDead)) {
-        key = p.tet[i];
+// particles; runs of equal tet are summed per warp and merged in the
+// block's node table over its range of tiles (deposit.cuh).
+struct DepSrc64 {
+    struct Raw {
+        uint32_t idf;
+        int32_t tet;
+        double x, y, z;
+    };
+    DevParticles p;
+    const TetRec *rec;
+    int k;
+    long long one;
+    __device__ __forceinline__ Raw load(int64_t i, int64_t n) const {
+        Raw r{kDead, -1, 0.0, 0.0, 0.0};
+        if (i < n) {
+            r.idf = __ldg(p.idf + i);
+            r.tet = __ldg(p.tet + i);
+            r.x = __ldg(p.x + i);
+            r.y = __ldg(p.y + i);
+            r.z = __ldg(p.z + i);
+        }
+        return r;
+    }
+    __device__ __forceinline__ int weights(const Raw &r, long long v[4]) const {
+        v[0] = v[1] = v[2] = v[3] = 0;
+        if (r.idf & kDead) return -1;
         TetGeo g;
-        load_geo(m.rec, key, g);
-        const double d0 = p.x[i] - g.x0[0], d1 = p.y[i] - g.x0[1], d2 = p.z[i] - g.x0[2];
+        load_geo(rec, r.tet, g);
+        const double d0 = r.x - g.x0[0], d1 = r.y - g.x0[1], d2 = r.z - g.x0[2];
         const double l1 = g.M[0] * d0 + g.M[1] * d1 + g.M[2] * d2;
         const double l2 = g.M[3] * d0 + g.M[4] * d1 + g.M[5] * d2;
         const double l3 = g.M[6] * d0 + g.M[7] * d1 + g.M[8] * d2;
         v[1] = fix_round(l1, k);
         v[2] = fix_round(l2, k);
         v[3] = fix_round(l3, k);
-        v[0] = (1LL << k) - v[1] - v[2] - v[3];
+        v[0] = one - v[1] - v[2] - v[3];
+        return r.tet;
     }
-    deposit_block_flush<256>(key, v, 1LL << k, m.tet_nodes, node_fix, occ);
+};
+
+__global__ void __launch_bounds__(kDepThreads)
+    k_deposit64(const DepSrc64 src, int64_t n, const int4 *__restrict__ tet_nodes,
+                unsigned long long *__restrict__ node_fix, const OccList occ) {
+    deposit_tiles(src, n, tet_nodes, node_fix, occ);
 }
 
 __global__ void k_fix_to_charge(const unsigned long long *__restrict__ node_fix, double scale,
@@ -907,7 +930,11 @@ void launch_step64(const DevParticles &p, int64_t n, const MeshDev &m, const Ste
 void launch_deposit64(const DevParticles &p, int64_t n, const MeshDev &m, int k, unsigned long long *node_fix,
                       const OccList &occ, cudaStream_t s) {
     if (n <= 0) return;
-    k_deposit64<<<grid_for(n, 256), 256, 0, s>>>(p, n, m, k, node_fix, occ);
+    static int blocks = 0;  // one wave
+    if (blocks == 0) blocks = resident_blocks(k_deposit64, kDepThreads);
+    const DepSrc64 src{p, m.rec, k, 1LL << k};
+    const unsigned grid = unsigned(std::min<int64_t>(grid_for(n, kDepThreads), blocks));
+    k_deposit64<<<grid, kDepThreads, 0, s>>>(src, n, m.tet_nodes, node_fix, occ);
 }
 
 void launch_fix_to_charge(const unsigned long long *node_fix, double scale, double *node_q, int64_t n,
