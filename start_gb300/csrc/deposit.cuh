@@ -6,17 +6,17 @@
 // current tile is reduced. A warp whose tile lies in one tet (the common case
 // in tet-sorted order: a beam puts thousands of particles in a tet) adds the
 // weights to per-lane running sums and reduces them only when its tet
-// changes. In other tiles the lanes with equal tets (match_any: the ends of
-// runs, and lanes of a tet that drifted apart since the last re-sort) are
-// summed by the integer reduce unit. Either way the lowest lane adds the four
-// node sums to the block's table of nodes in shared memory, which lives for
-// the whole range and is flushed once, with one global atomic per distinct
-// node. The table
-// takes new nodes while it is at most half full (short probe runs); past
-// that a node it does not hold goes to its global accumulator directly, so
-// a block whose range touches many nodes (particles spread over many tets)
-// degrades to one atomic per group and node. Integer sums do not depend on
-// order, so the result is the same as one atomic per particle.
+// changes. In other tiles (the ends of runs, and particles that moved to
+// other tets since the last re-sort) the lanes with equal tets (match_any)
+// are summed by the integer reduce unit. Either way the lowest lane adds the
+// tet's four sums to the block's table of tets in shared memory: one probe,
+// four adds to adjacent words. The table is flushed into the node
+// accumulators at the end of the range (four global atomics per listed tet),
+// and also every kDepCheckTiles tiles if it is more than half full, so a
+// range whose particles are spread over many tets keeps aggregating. While
+// the table is over half full a tet it does not hold goes to the node
+// accumulators directly. Integer sums do not depend on order, so the result
+// is the same as one atomic per particle.
 #ifndef SPG_DEPOSIT_CUH
 #define SPG_DEPOSIT_CUH
 
@@ -28,12 +28,13 @@
 namespace spg {
 
 constexpr int kDepThreads = 256;
-constexpr int kDepSlots = 2048;          // node slots of a block's table
-constexpr int kDepOpen = kDepSlots / 2;  // new nodes enter while the table holds fewer
+constexpr int kDepSlots = 1024;          // tet slots of a block's table
+constexpr int kDepOpen = kDepSlots / 2;  // new tets enter while the table holds fewer
+constexpr int kDepCheckTiles = 16;       // tiles between checks of the table's fill
 
 struct DepositTable {
-    int node[kDepSlots];  // -1: free; a slot's node never changes once set
-    unsigned long long sum[kDepSlots];
+    int tet[kDepSlots];  // -1: free; a slot's tet does not change until the table is cleared
+    unsigned long long sum[kDepSlots][4];
     unsigned int held;
 };
 
@@ -76,34 +77,6 @@ __device__ __forceinline__ unsigned group_sums(int key, const long long v[4], lo
     return grp;
 }
 
-// Adds x to node's slot (open addressing, linear probing). A slot found free
-// is claimed by compare-and-swap only while the table is open; a closed table
-// sends a node it does not hold to the global accumulator. The probe run ends
-// at the node or a free slot: at most kDepOpen + kDepThreads slots are ever
-// taken, so a free slot exists.
-__device__ __forceinline__ void table_add(DepositTable &s, int node, unsigned long long x,
-                                          unsigned long long *__restrict__ node_fix) {
-    int h = int((unsigned(node) * 2654435761u) >> 8) & (kDepSlots - 1);
-    for (int probe = 0; probe < kDepSlots; ++probe) {
-        int cur = s.node[h];
-        if (cur == -1) {
-            if (*(volatile unsigned int *)&s.held >= unsigned(kDepOpen)) break;
-            cur = atomicCAS(&s.node[h], -1, node);
-            if (cur == -1) {
-                atomicAdd(&s.held, 1u);
-                atomicAdd(&s.sum[h], x);
-                return;
-            }
-        }
-        if (cur == node) {
-            atomicAdd(&s.sum[h], x);
-            return;
-        }
-        h = (h + 1) & (kDepSlots - 1);
-    }
-    atomicAdd(node_fix + node, x);
-}
-
 // Appends tet `key` to the list of occupied tets once per deposit (the
 // generation stamp of the tet says whether it is listed already).
 __device__ __forceinline__ void list_tet(const OccList &occ, int key) {
@@ -111,20 +84,64 @@ __device__ __forceinline__ void list_tet(const OccList &occ, int key) {
         occ.list[atomicAdd(occ.n, 1u)] = key;
 }
 
-// Four node sums of tet `key` into the table (the lowest lane of the group
-// calls this).
-__device__ __forceinline__ void add_tet(DepositTable &s, int key, const long long sum[4],
-                                        const int4 *__restrict__ tet_nodes, unsigned long long *__restrict__ node_fix,
-                                        const OccList &occ, int &listed) {
-    if (key != listed) {
-        list_tet(occ, key);
-        listed = key;
-    }
+// A tet's four node sums into the node accumulators.
+__device__ __forceinline__ void tet_to_nodes(int key, const unsigned long long sum[4],
+                                             const int4 *__restrict__ tet_nodes,
+                                             unsigned long long *__restrict__ node_fix, const OccList &occ) {
+    list_tet(occ, key);
     const int4 tn = __ldg(tet_nodes + key);
-    table_add(s, tn.x, (unsigned long long)sum[0], node_fix);
-    table_add(s, tn.y, (unsigned long long)sum[1], node_fix);
-    table_add(s, tn.z, (unsigned long long)sum[2], node_fix);
-    table_add(s, tn.w, (unsigned long long)sum[3], node_fix);
+    if (sum[0]) atomicAdd(node_fix + tn.x, sum[0]);
+    if (sum[1]) atomicAdd(node_fix + tn.y, sum[1]);
+    if (sum[2]) atomicAdd(node_fix + tn.z, sum[2]);
+    if (sum[3]) atomicAdd(node_fix + tn.w, sum[3]);
+}
+
+// Adds a tet's four sums to its slot (open addressing, linear probing). A
+// free slot is claimed by compare-and-swap only while the table is at most
+// half full; otherwise a tet the table does not hold goes to the node
+// accumulators. The probe run ends at the tet or a free slot: fewer than
+// kDepOpen + kDepThreads slots are ever taken between clears.
+__device__ __forceinline__ void table_add(DepositTable &s, int key, const long long sum[4],
+                                          const int4 *__restrict__ tet_nodes,
+                                          unsigned long long *__restrict__ node_fix, const OccList &occ) {
+    int h = int((unsigned(key) * 2654435761u) >> 8) & (kDepSlots - 1);
+    for (int probe = 0; probe < kDepSlots; ++probe) {
+        int cur = s.tet[h];
+        if (cur == -1) {
+            if (*(volatile unsigned int *)&s.held >= unsigned(kDepOpen)) break;
+            cur = atomicCAS(&s.tet[h], -1, key);
+            if (cur == -1) {
+                atomicAdd(&s.held, 1u);
+                cur = key;
+            }
+        }
+        if (cur == key) {
+            atomicAdd(&s.sum[h][0], (unsigned long long)sum[0]);
+            atomicAdd(&s.sum[h][1], (unsigned long long)sum[1]);
+            atomicAdd(&s.sum[h][2], (unsigned long long)sum[2]);
+            atomicAdd(&s.sum[h][3], (unsigned long long)sum[3]);
+            return;
+        }
+        h = (h + 1) & (kDepSlots - 1);
+    }
+    const unsigned long long u[4] = {(unsigned long long)sum[0], (unsigned long long)sum[1],
+                                     (unsigned long long)sum[2], (unsigned long long)sum[3]};
+    tet_to_nodes(key, u, tet_nodes, node_fix, occ);
+}
+
+__device__ __forceinline__ void table_clear(DepositTable &s) {
+    for (int k = threadIdx.x; k < kDepSlots; k += kDepThreads) {
+        s.tet[k] = -1;
+        s.sum[k][0] = s.sum[k][1] = s.sum[k][2] = s.sum[k][3] = 0ull;
+    }
+    if (threadIdx.x == 0) s.held = 0u;
+}
+
+// Every held tet's sums into the node accumulators (after a barrier).
+__device__ __forceinline__ void table_flush(const DepositTable &s, const int4 *__restrict__ tet_nodes,
+                                            unsigned long long *__restrict__ node_fix, const OccList &occ) {
+    for (int k = threadIdx.x; k < kDepSlots; k += kDepThreads)
+        if (s.tet[k] >= 0) tet_to_nodes(s.tet[k], s.sum[k], tet_nodes, node_fix, occ);
 }
 
 // Warp sum of 64-bit values modulo 2^64 (three 21-bit pieces, the top one
@@ -141,8 +158,7 @@ __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
 __device__ __forceinline__ void flush_running(DepositTable &s, int key, unsigned long long a1, unsigned long long a2,
                                               unsigned long long a3, int acnt, long long one,
                                               const int4 *__restrict__ tet_nodes,
-                                              unsigned long long *__restrict__ node_fix, const OccList &occ,
-                                              int &listed) {
+                                              unsigned long long *__restrict__ node_fix, const OccList &occ) {
     long long sum[4];
     sum[1] = (long long)warp_sum64(a1);
     sum[2] = (long long)warp_sum64(a2);
@@ -150,7 +166,7 @@ __device__ __forceinline__ void flush_running(DepositTable &s, int key, unsigned
     const unsigned long long cnt = __reduce_add_sync(0xffffffffu, unsigned(acnt));
     sum[0] = (long long)(cnt * (unsigned long long)one - (unsigned long long)sum[1] - (unsigned long long)sum[2] -
                          (unsigned long long)sum[3]);
-    if ((threadIdx.x & 31) == 0) add_tet(s, key, sum, tet_nodes, node_fix, occ, listed);
+    if ((threadIdx.x & 31) == 0) table_add(s, key, sum, tet_nodes, node_fix, occ);
 }
 
 // The deposit of particles [0, n) by one block of kDepThreads threads, its
@@ -159,34 +175,33 @@ __device__ __forceinline__ void flush_running(DepositTable &s, int key, unsigned
 //   int weights(const Raw &, long long v[4]): the tet (or -1: dead) and the
 //     fixed-point weights v[0..3] summing to one (zeros for a dead particle);
 //   long long one: the fixed-point one.
-// A warp whose tile holds one tet (dead lanes aside) adds the weights to its
-// lanes' running sums for that tet; the sums are reduced over the warp and
-// added to the table when the warp's tet changes (in a beam, once per some
-// hundred particles). Other tiles go through the group sums. The next tile's
-// fields are loaded before the current tile's weights are formed.
 template <class Src>
 __device__ __forceinline__ void deposit_tiles(const Src &src, int64_t n, const int4 *__restrict__ tet_nodes,
                                               unsigned long long *__restrict__ node_fix, const OccList &occ) {
     constexpr unsigned kAll = 0xffffffffu;
     __shared__ DepositTable s;
-    for (int k = threadIdx.x; k < kDepSlots; k += kDepThreads) {
-        s.node[k] = -1;
-        s.sum[k] = 0ull;
-    }
-    if (threadIdx.x == 0) s.held = 0u;
+    table_clear(s);
     __syncthreads();
     const int64_t tiles = (n + kDepThreads - 1) / kDepThreads;
     const int64_t per = (tiles + gridDim.x - 1) / gridDim.x;
     const int64_t t0 = int64_t(blockIdx.x) * per;
     const int64_t t1 = t0 + per < tiles ? t0 + per : tiles;
     const int lane = threadIdx.x & 31;
-    int listed = -1;
-    int acc_key = -1;  // warp-uniform: the tet of the running sums (-1: none)
+    int acc_key = -1;                           // warp-uniform: the tet of the running sums (-1: none)
     unsigned long long a1 = 0, a2 = 0, a3 = 0;  // modulo 2^64: the node totals fit 63 bits
     int acnt = 0;                               // this lane's alive particles in the running sums
     int64_t i = t0 * kDepThreads + threadIdx.x;
     typename Src::Raw nxt = src.load(i, t0 < t1 ? n : 0);
     for (int64_t t = t0; t < t1; ++t, i += kDepThreads) {
+        if ((t - t0) % kDepCheckTiles == kDepCheckTiles - 1) {  // block-uniform
+            __syncthreads();
+            if (s.held >= unsigned(kDepOpen)) {
+                table_flush(s, tet_nodes, node_fix, occ);
+                __syncthreads();
+                table_clear(s);
+            }
+            __syncthreads();
+        }
         const typename Src::Raw cur = nxt;
         nxt = src.load(i + kDepThreads, t + 1 < t1 ? n : 0);
         long long v[4];
@@ -194,9 +209,7 @@ __device__ __forceinline__ void deposit_tiles(const Src &src, int64_t n, const i
         const int kmax = __reduce_max_sync(kAll, key);
         if (__all_sync(kAll, key == kmax || key < 0)) {
             if (kmax != acc_key && kmax >= 0) {
-                if (acc_key >= 0) {
-                    flush_running(s, acc_key, a1, a2, a3, acnt, src.one, tet_nodes, node_fix, occ, listed);
-                }
+                if (acc_key >= 0) flush_running(s, acc_key, a1, a2, a3, acnt, src.one, tet_nodes, node_fix, occ);
                 acc_key = kmax;
                 a1 = a2 = a3 = 0;
                 acnt = 0;
@@ -208,18 +221,12 @@ __device__ __forceinline__ void deposit_tiles(const Src &src, int64_t n, const i
         } else {
             long long sum[4];
             const unsigned grp = group_sums(key, v, src.one, sum);
-            if (key >= 0 && lane == __ffs(grp) - 1) add_tet(s, key, sum, tet_nodes, node_fix, occ, listed);
+            if (key >= 0 && lane == __ffs(grp) - 1) table_add(s, key, sum, tet_nodes, node_fix, occ);
         }
     }
-    if (acc_key >= 0) {
-        flush_running(s, acc_key, a1, a2, a3, acnt, src.one, tet_nodes, node_fix, occ, listed);
-    }
+    if (acc_key >= 0) flush_running(s, acc_key, a1, a2, a3, acnt, src.one, tet_nodes, node_fix, occ);
     __syncthreads();
-    for (int k = threadIdx.x; k < kDepSlots; k += kDepThreads) {
-        const int node = s.node[k];
-        const unsigned long long x = s.sum[k];
-        if (node >= 0 && x != 0ull) atomicAdd(node_fix + node, x);
-    }
+    table_flush(s, tet_nodes, node_fix, occ);
 }
 
 // Blocks of `kernel` resident on the whole GPU at once (the deposit's one wave).

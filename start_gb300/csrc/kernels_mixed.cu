@@ -709,10 +709,27 @@ __global__ void __launch_bounds__(256, 3) k_seg_resume32(MixedArgs a, StepConst 
     add_step_counters(ctr, processed, coll, lost);
 }
 
-// round(x * 2^k) of a float: the product with 2^k (k <= 52) is exact, the
-// conversion rounds to nearest even.
+// round(x * 2^k) of a float (k <= 52), to nearest with ties to even, from the
+// float's bits with 32-bit integer operations: a conversion to a 64-bit
+// integer issues on the FP64 pipe, three per particle. x = mant 2^(e - 150),
+// so x 2^k = mant 2^-sh with sh = 150 - e - k; a left shift past 39 bits
+// (|x| 2^k >= 2^63, no barycentric) is clamped.
 __device__ __forceinline__ long long fix_round32(float x, int k) {
-    return __float2ll_rn(x * __int_as_float((127 + k) << 23));
+    const int b = __float_as_int(x);
+    const int e = (b >> 23) & 0xff;
+    if (e == 0) return 0;  // zero or subnormal: |x| 2^k < 2^-74
+    const unsigned mant = unsigned(b & 0x7FFFFF) | 0x800000u;
+    const int sh = 150 - e - k;
+    unsigned long long r;
+    if (sh <= 0) {
+        r = (unsigned long long)mant << min(-sh, 39);
+    } else if (sh > 24) {
+        r = 0;  // below half of one: mant < 2^24 <= 2^(sh - 1)
+    } else {
+        const unsigned q = mant >> sh, rem = mant & ((1u << sh) - 1u), half = 1u << (sh - 1);
+        r = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+    }
+    return b < 0 ? -(long long)r : (long long)r;
 }
 
 // The mixed form's particles for deposit_tiles: FP32 barycentrics of the
