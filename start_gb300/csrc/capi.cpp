@@ -1495,6 +1495,13 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
         std::vector<TetRec32> r32(hm.n_tets);
         std::vector<double> cen(3 * hm.n_tets);
         std::vector<float> cen_lo(3 * hm.n_tets);
+        // Interior tets: every vertex inside the modelling box by 1e-5 of its
+        // extent plus its largest coordinate, some hundred times the FP32
+        // rounding of a centroid-plus-local position and of the box bounds.
+        double margin = 0.0;
+        for (int c = 0; c < 3; ++c)
+            margin = std::max(margin, 1e-5 * ((hm.bbox_hi[c] - hm.bbox_lo[c]) +
+                                              std::max(std::fabs(hm.bbox_lo[c]), std::fabs(hm.bbox_hi[c]))));
         for (int64_t t = 0; t < hm.n_tets; ++t) {
             for (int c = 0; c < 3; ++c) {
                 double acc = 0.0;
@@ -1508,7 +1515,13 @@ int spg_create(const spg_mesh_desc *mesh, const spg_params *params, spg_handle *
                 q.cen[c] = float(cen[3 * t + c]);
                 cen_lo[3 * t + c] = float(cen[3 * t + c] - double(q.cen[c]));
             }
-            q.ezero = 1u;
+            bool interior = true;
+            for (int k = 0; k < 4; ++k)
+                for (int c = 0; c < 3; ++c) {
+                    const double v = hm.node_xyz[3 * int64_t(hm.tet_nodes[4 * t + k]) + c];
+                    interior = interior && v >= hm.bbox_lo[c] + margin && v <= hm.bbox_hi[c] - margin;
+                }
+            q.ezero = kRecEzero | (interior ? kRecInterior : 0u);
         }
         CK(upload(&h->rec32, r32, s));
         CK(upload(&h->cen, cen, s));

@@ -72,6 +72,13 @@ __device__ __noinline__ void bary64_local(const TetRec *__restrict__ rec64, int 
         if (l[k] == 0.0f && (k == 0 ? l0 : (k == 1 ? l1 : (k == 2 ? l2 : l3))) < 0.0) l[k] = -1e-30f;
 }
 
+// The modelling-box test of a global FP32 position (the particle's tet's
+// centroid plus its local position).
+__device__ __forceinline__ bool in_box32(const StepConst &c, float gx, float gy, float gz) {
+    return gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] && gz >= c.lo_f[2] &&
+           gz <= c.hi_f[2];
+}
+
 __device__ __forceinline__ int comp(const int4 &v, int f) {
     return f == 0 ? v.x : (f == 1 ? v.y : (f == 2 ? v.z : v.w));
 }
@@ -361,11 +368,9 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
         const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
         const float vmin = c.vmin_f;
         const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
-        const float gx = r3.x + x, gy = r3.y + y, gz = r3.z + z;
-        const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
-                            gz >= c.lo_f[2] && gz <= c.hi_f[2];
-        if (slow || !in_box) continue;
-        if (!__float_as_uint(r3.w)) {
+        const uint32_t flags = __float_as_uint(r3.w);
+        if (slow || (!(flags & kRecInterior) && !in_box32(c, r3.x + x, r3.y + y, r3.z + z))) continue;
+        if (!(flags & kRecEzero)) {
             const float hx = r2.y, hy = r2.z, hz = r2.w;
             vx = (vx + hx) + hx;
             vy = (vy + hy) + hy;
@@ -429,7 +434,8 @@ __device__ __forceinline__ void field_of_tet32(const FieldArgs &f, int64_t t) {
         f.efield[3 * t + k] = E[k];
         f.rec32[t].H[k] = float(E[k] * f.c32);
     }
-    f.rec32[t].ezero = (E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0) ? 1u : 0u;
+    const bool null_field = E[0] == 0.0 && E[1] == 0.0 && E[2] == 0.0;
+    f.rec32[t].ezero = (f.rec32[t].ezero & kRecInterior) | (null_field ? kRecEzero : 0u);
 }
 
 // With land != nullptr a particle that settles records the step, the exit
@@ -535,7 +541,8 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
     const float4 *rp = reinterpret_cast<const float4 *>(a.rec + w.t);
     const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
     const Geo32 g{{r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x}};
-    const bool push = !__float_as_uint(r3.w);
+    const uint32_t flags = __float_as_uint(r3.w);
+    const bool push = !(flags & kRecEzero), interior = flags & kRecInterior;
     const float hx = r2.y, hy = r2.z, hz = r2.w;
     const uint32_t id = w.idf & kIdMask;
     float x = w.x, y = w.y, z = w.z, vx = w.vx, vy = w.vy, vz = w.vz;
@@ -555,10 +562,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
     for (int j = j0; j < sq.L; ++j) {
         processed++;
         const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
-        const float gx = r3.x + x, gy = r3.y + y, gz = r3.z + z;
-        const bool in_box = gx >= c.lo_f[0] && gx <= c.hi_f[0] && gy >= c.lo_f[1] && gy <= c.hi_f[1] &&
-                            gz >= c.lo_f[2] && gz <= c.hi_f[2];
-        if (slow || !in_box) {
+        if (slow || (!interior && !in_box32(c, r3.x + x, r3.y + y, r3.z + z))) {
             processed += unsigned(sq.L - 1 - j);
             break;
         }
@@ -944,7 +948,7 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
         float vx = float(h.vx[o]), vy = float(h.vy[o]), vz = float(h.vz[o]);
         if (fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin) continue;  // the step did not move it
         const TetRec32 &R = a.rec[t];
-        if (!R.ezero) {
+        if (!(R.ezero & kRecEzero)) {
             vx = (vx + R.H[0]) + R.H[0];
             vy = (vy + R.H[1]) + R.H[1];
             vz = (vz + R.H[2]) + R.H[2];
@@ -997,7 +1001,7 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
         Vx = bx;
         Vy = by;
         Vz = bz;
-        if (G && !R.ezero) {
+        if (G && !(R.ezero & kRecEzero)) {
             // the pushed velocity's dependence on the position through the
             // recovered field: abar_x += cq G^T abar_va
             const double *g = G + 9 * int64_t(t);

@@ -633,7 +633,7 @@ __global__ void k_zero_field(const __grid_constant__ FieldArgs f, int64_t n) {
         f.rec32[t].H[0] = 0.0f;
         f.rec32[t].H[1] = 0.0f;
         f.rec32[t].H[2] = 0.0f;
-        f.rec32[t].ezero = 1u;
+        f.rec32[t].ezero = (f.rec32[t].ezero & kRecInterior) | kRecEzero;
     }
     f.efield[3 * t] = 0.0;
     f.efield[3 * t + 1] = 0.0;

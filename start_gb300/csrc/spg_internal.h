@@ -256,12 +256,17 @@ int32_t *sort_offsets(int32_t *scratch);
 // ---------------------------------------------------------- mixed precision
 // Per-tet record of the mixed form (64 B): FP32 barycentric map about the
 // centroid, lambda_{1..3} = 1/4 + M (x - c); FP32 push increment; FP32
-// centroid (modelling-box test only); E-null flag.
+// centroid (modelling-box test only); flags: kRecEzero (E = 0, no push) and
+// kRecInterior (the tet lies inside the modelling box with a margin far above
+// the FP32 rounding of centroid + local position, so a particle inside it
+// passes the box test: the test is skipped).
+constexpr uint32_t kRecEzero = 1u;
+constexpr uint32_t kRecInterior = 2u;
 struct alignas(64) TetRec32 {
     float M[9];
     float H[3];
     float cen[3];
-    uint32_t ezero;
+    uint32_t ezero;  // kRecEzero | kRecInterior
 };
 static_assert(sizeof(TetRec32) == 64, "TetRec32 must be 64 bytes");
 
