@@ -235,25 +235,27 @@ __device__ __noinline__ Walk32 walk32(const MixedArgs a, int t, float p0x, float
     }
 }
 
-// Candidate byte of step `step` (one Philox block per sixteen steps).
-__device__ __forceinline__ uint32_t decision_byte(const StepConst &c, uint32_t id, uint64_t step) {
-    return candidate_byte(candidate_block(step, id, c.seed_lo, c.seed_hi), step);
+// Whether step `step` is a candidate: its byte of the step's Philox block
+// (one per sixteen steps) is zero.
+__device__ __forceinline__ bool is_candidate(const StepConst &c, uint32_t id, uint64_t step) {
+    return candidate_byte(candidate_block(step, id, c.seed_lo, c.seed_hi), step) == 0u;
 }
 
+// |v|^2 in the order every FP32 collision test and slow-particle test uses.
+__device__ __forceinline__ float speed2(float vx, float vy, float vz) { return fmaf(vz, vz, fmaf(vy, vy, vx * vx)); }
+
 // FP32 collision test of step `step` (the candidate-byte rule of philox.h
-// with P_f = kp (v^2)^pexp; `byte` is the step's candidate byte) and, on a
-// hit, the scattering direction's cosine xc, sine xs and azimuth (cos, sin).
-// A step that is no candidate with v^2 <= v2_cand_f has P_f < q: no
-// collision, decided without P_f.
-__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, uint32_t byte,
-                                                  float vx, float vy, float vz, float &xc, float &xs, float &cp,
-                                                  float &sp) {
+// with P_f = kp (v^2)^pexp; `cand`: the step's candidate byte is zero; v2 =
+// speed2 of the velocity) and, on a hit, the scattering direction's cosine
+// xc, sine xs and azimuth (cos, sin). A step that is no candidate with
+// v^2 <= v2_cand_f has P_f < q: no collision, decided without P_f.
+__device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t id, uint64_t step, bool cand,
+                                                  float v2, float &xc, float &xs, float &cp, float &sp) {
     constexpr float qf = float(kCandQ);
-    const float v2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
-    if (byte != 0u && v2 <= c.v2_cand_f) return false;
+    if (!cand && v2 <= c.v2_cand_f) return false;
     const float P = c.kp_f * exp2f(c.pexp_f * log2f(v2));
     bool hit;
-    if (byte == 0u)
+    if (cand)
         hit = P > qf || float(collision_draw(step, 3u, id, c.seed_lo, c.seed_hi).v[0] >> 8) *
                                 5.9604644775390625e-8f < P * 256.0f;
     else
@@ -275,11 +277,11 @@ __device__ __forceinline__ bool collision_event32(const StepConst &c, uint32_t i
 }
 
 // Collision of step `step` in FP32 (same Philox streams and laws as the FP64
-// form); `byte` is the step's candidate byte.
-__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, uint32_t byte, float &vx,
-                                          float &vy, float &vz) {
+// form); `cand` and v2 as for collision_event32.
+__device__ __forceinline__ bool collide32(const StepConst &c, uint32_t id, uint64_t step, bool cand, float v2,
+                                          float &vx, float &vy, float &vz) {
     float xc, xs, cp, sp;
-    if (!collision_event32(c, id, step, byte, vx, vy, vz, xc, xs, cp, sp)) return false;
+    if (!collision_event32(c, id, step, cand, v2, xc, xs, cp, sp)) return false;
     const float mcp = c.mass_cp_f, mct = c.mass_ct_f;
     const float pvx = mct * vx, pvy = mct * vy, pvz = mct * vz;
     const float mp = sqrtf(fmaf(pvz, pvz, fmaf(pvy, pvy, pvx * pvx)));
@@ -397,8 +399,8 @@ __global__ void __launch_bounds__(256, 4) k_step32(MixedArgs a, StepConst c, Wal
             }
             if (c.model != SPG_COLL_NONE) {
                 const uint32_t id = idf & kIdMask;
-                coll += collide32(c, id, uint64_t(c.step), decision_byte(c, id, uint64_t(c.step)), vx, vy, vz) ? 1u
-                                                                                                               : 0u;
+                const uint64_t step = uint64_t(c.step);
+                coll += collide32(c, id, step, is_candidate(c, id, step), speed2(vx, vy, vz), vx, vy, vz) ? 1u : 0u;
             }
         }
         a.p.vx[i] = vx;
@@ -546,22 +548,28 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
     const float hx = r2.y, hy = r2.z, hz = r2.w;
     const uint32_t id = w.idf & kIdMask;
     float x = w.x, y = w.y, z = w.z, vx = w.vx, vy = w.vy, vz = w.vz;
-    const float vmin = c.vmin_f, dt = c.dt_f;
+    const float vmin2 = c.vmin_f * c.vmin_f, dt = c.dt_f;
+    float v2 = speed2(vx, vy, vz);  // of the current velocity
     bool dirty = false;
-    // the candidate block of the last sixteen-step group tested (block_of: its count)
-    Philox4 blk{};
-    uint64_t block_of = ~uint64_t(0);
-    auto collide = [&](uint64_t step) -> unsigned {
-        if ((step >> 4) != block_of) {
-            block_of = step >> 4;
-            blk = candidate_block(step, id, c.seed_lo, c.seed_hi);
+    // the candidate steps of the last sixteen-step group tested (cgroup: the
+    // low 32 bits of its count; steps in a segment are consecutive, so the
+    // key changes exactly when the group does)
+    uint32_t cmask = 0u, cgroup = ~0u;
+    const uint32_t step_lo = uint32_t(c.step);
+    auto collide = [&](int j) -> unsigned {
+        const uint32_t sj = step_lo + uint32_t(j);
+        const uint64_t step = uint64_t(c.step) + uint64_t(j);
+        if ((sj >> 4) != cgroup) {
+            cgroup = sj >> 4;
+            cmask = candidate_mask(candidate_block(step, id, c.seed_lo, c.seed_hi));
         }
-        const uint32_t b = candidate_byte(blk, step);
-        return collide32(c, id, step, b, vx, vy, vz) ? 1u : 0u;
+        if (!collide32(c, id, step, (cmask >> (sj & 15u)) & 1u, v2, vx, vy, vz)) return 0u;
+        v2 = speed2(vx, vy, vz);
+        return 1u;
     };
     for (int j = j0; j < sq.L; ++j) {
         processed++;
-        const bool slow = fmaf(vz, vz, fmaf(vy, vy, vx * vx)) < vmin * vmin;
+        const bool slow = v2 < vmin2;
         if (slow || (!interior && !in_box32(c, r3.x + x, r3.y + y, r3.z + z))) {
             processed += unsigned(sq.L - 1 - j);
             break;
@@ -570,15 +578,15 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
             vx = (vx + hx) + hx;
             vy = (vy + hy) + hy;
             vz = (vz + hz) + hz;
+            v2 = speed2(vx, vy, vz);
             dirty = true;
         }
         const float nx = fmaf(vx, dt, x), ny = fmaf(vy, dt, y), nz = fmaf(vz, dt, z);
         if (nx == x && ny == y && nz == z) continue;
-        const uint64_t step = uint64_t(c.step) + uint64_t(j);
         if (!(isfinite(nx) && isfinite(ny) && isfinite(nz))) {
             a.p.idf[i] = w.idf | kLost;
             lost++;
-            if (c.model != SPG_COLL_NONE) coll += collide(step);
+            if (c.model != SPG_COLL_NONE) coll += collide(j);
             a.p.x[i] = x;
             a.p.y[i] = y;
             a.p.z[i] = z;
@@ -592,7 +600,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         const float mn = fminf(fminf(l[0], l[1]), fminf(l[2], l[3]));
         if (!(mn > kNearZero)) {
             queue_seg32(sq.wq, qn, i, j, x, y, z);
-            if (c.model != SPG_COLL_NONE) coll += collide(step);
+            if (c.model != SPG_COLL_NONE) coll += collide(j);
             a.p.x[i] = nx;
             a.p.y[i] = ny;
             a.p.z[i] = nz;
@@ -604,7 +612,7 @@ __device__ __forceinline__ void seg_steps32(const MixedArgs &a, const StepConst 
         x = nx;
         y = ny;
         z = nz;
-        if (c.model != SPG_COLL_NONE) coll += collide(step);
+        if (c.model != SPG_COLL_NONE) coll += collide(j);
         dirty = true;
     }
     if (dirty) {
@@ -974,7 +982,7 @@ __global__ void __launch_bounds__(128) k_backward32(MixedArgs a, AdjHist h, int 
             float xc, xs, cp, sp;
             const uint64_t sk = uint64_t(c.step + k);
             if (c.model != SPG_COLL_NONE &&
-                collision_event32(c, id, sk, decision_byte(c, id, sk), vx, vy, vz, xc, xs, cp, sp)) {
+                collision_event32(c, id, sk, is_candidate(c, id, sk), speed2(vx, vy, vz), xc, xs, cp, sp)) {
                 // v' = m_cp v + m_ct |v| n:  J^T a = m_cp a + m_ct v/|v| (n . a)
                 const double vm = sqrt(wx * wx + wy * wy + wz * wz);
                 const double na = (double(xs * cp) * Vx + double(xs * sp) * Vy + double(xc) * Vz) * mct / vm;

@@ -86,4 +86,21 @@ SPG_HD uint32_t candidate_byte(const Philox4 &b, uint64_t step) {
     return (w >> (8u * (k & 3u))) & 0xffu;
 }
 
+// Bit k (0..15) set iff candidate_byte(b, 16 g + k) == 0: the candidate
+// steps of the block's sixteen, so a step's test is one shift and one and.
+SPG_HD uint32_t candidate_mask(const Philox4 &b) {
+    uint32_t m = 0u;
+    for (int q = 0; q < 4; ++q) {
+        const uint32_t w = b.v[q];
+        // 0x80 in each zero byte of w: (w & 0x7f) + 0x7f <= 0xfe, so no carry
+        // crosses a byte, and the sum's top bit or w's is set iff the byte is not zero
+        const uint32_t z = ~(((w & 0x7f7f7f7fu) + 0x7f7f7f7fu) | w) & 0x80808080u;
+        // the byte flags at bits 0, 8, 16, 24 times 2^24 + 2^17 + 2^10 + 2^3:
+        // flag i lands on bit 24 + i, every other partial product on a distinct
+        // bit below 24 (no carry) or beyond 31
+        m |= ((((z >> 7) * 0x01020408u) >> 24) & 0xfu) << (4 * q);
+    }
+    return m;
+}
+
 }  // namespace spg

@@ -9,11 +9,19 @@ iff a candidate or else u_f < (P - q) / (1 - q) (block (step, draw 4)).
 
 Checked here: the oracle's decisions against a restatement of that rule on
 the pinned Philox (tests/test_oracle_pins.py holds its known answers), the
-collision rate against P on both sides of q (binomial, 5 sigma), and the
-independence of consecutive steps (the rate of colliding pairs against P^2).
+collision rate against P on both sides of q (binomial, 5 sigma), the
+independence of consecutive steps (the rate of colliding pairs against P^2),
+and the kernels' sixteen-step candidate mask (philox.h candidate_mask, built
+for the host) against the candidate bytes.
 """
+import shutil
+import subprocess
+from pathlib import Path
+
 import numpy as np
 import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
 
 import oracle as O
 
@@ -88,3 +96,15 @@ def test_rate_and_independence(P):
     npair = n_ids * (n_steps - 1)
     ep = npair * P * P
     assert abs(pairs - ep) <= 5 * np.sqrt(ep) + 3, (pairs, ep)
+
+
+def test_candidate_mask_matches_candidate_bytes(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    exe = tmp_path / "candidate_mask_check"
+    subprocess.run([gxx, "-O2", "-std=c++17", f"-I{ROOT / 'start_gb300' / 'csrc'}",
+                    str(ROOT / "tests" / "native" / "candidate_mask_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe), "1000000"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    assert "mismatches 0" in out.stdout
