@@ -111,3 +111,44 @@ def test_segment_setting_checked(built):
             g.set_step_segments(bad)
     g.set_step_segments(64)
     g.close()
+
+
+def test_box_inside_mesh(built):
+    """A modelling box inside the mesh (bbox_expansion 0.8: [0.01, 0.09]^3 of the
+    0.1 m cube). Tets that reach outside it carry no interior flag, so the
+    mixed step runs the per-step box test there; particles that leave the box
+    stop. Segments stay identical to one launch per step, and the particles
+    stopped outside the box are those the FP64 oracle stops."""
+    import oracle
+    from start_gb300 import StartPIC
+    from start_gb300.workloads import workload0
+
+    w = workload0(n_particles=10, collisions=False, steps=100)
+    w.params.update(bbox_expansion=0.8, cg_rtol=1e-12)
+    rng = np.random.default_rng(9)
+    n = 20000
+    pos = rng.uniform(0.02, 0.08, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    vel = 1.5e4 * d / np.linalg.norm(d, axis=1, keepdims=True)
+    runs = []
+    for m in (1, 32):
+        g = StartPIC(w.mesh, dict(w.params, precision=1))
+        g.set_step_segments(m)
+        g.set_particles(pos, vel)
+        runs.append((g, g.run(100)))
+    (a, sa), (b, sb) = runs
+    _same(a, b, sa, sb)
+    o = oracle.Oracle(w.mesh, dict(w.params, precision=0))
+    o.set_particles(pos, vel)
+    o.run(100)
+
+    def stopped(p):
+        alive = (p["flags"] & 3) == 0
+        out = ((p["pos"] < 0.01) | (p["pos"] > 0.09)).any(axis=1)
+        return alive & out
+
+    sm, so = stopped(a.particles()), stopped(o.particles())
+    assert so.sum() > 500, so.sum()
+    assert (sm ^ so).sum() <= 0.005 * so.sum() + 2, ((sm ^ so).sum(), so.sum())
+    a.close()
+    b.close()
