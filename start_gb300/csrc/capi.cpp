@@ -26,6 +26,9 @@ thread_local std::string g_create_error;
 
 constexpr int kEventPool = 8192;
 constexpr int kPcgChunk = 8;
+// Solver scalars held back per run (pinned host records, read when the run
+// ends or the records are full).
+constexpr int kSolveRecs = 64;
 // Order of the extrapolated initial guess of the AMG run solves (1: linear
 // in the last two potentials, 2: quadratic in the last three).
 constexpr int kExtrapOrder = 2;
@@ -92,6 +95,13 @@ struct spg_handle {
     uint32_t field_epoch = 0;                 // epoch of the current potential's field
     bool field_full = true;                   // every tet's field is of field_epoch
     bool in_run = false;                      // inside spg_run: solves refresh the occupied tets only
+    // Inside spg_run a while-graph solve does not wait for the host: its
+    // scalars go to a pinned record, read when the run ends.
+    bool defer_solves = false;
+    PcgScalars *solve_rec = nullptr;          // pinned, kSolveRecs records
+    uint8_t solve_kind[kSolveRecs] = {};      // 0: do_solve64, 1: do_solve_mixed_amg
+    int n_solve_rec = 0;
+    bool deferred_capped = false;             // a drained record had hit max_iter
     bool occ_fresh = false;                   // no particle has moved since the deposit listed the tets
     int64_t resorted_at = -1;                 // step of the last periodic re-sort
     int32_t *occ_list = nullptr;              // tets holding particles at the last deposit
@@ -911,9 +921,8 @@ void zero_field(spg_handle *h) {
     launch_zero_field(field_args(h), h->n_tets, h->stream);
 }
 
-int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped) {
-    int rc = update_field(h, h->in_run);
-    if (rc) return rc;
+// The statistics of a finished solve; SPG_E_NOT_CONVERGED if it hit max_iter.
+int record_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped) {
     h->cg_iters_last = iters;
     h->cg_iters_total += iters;
     h->cg_solves++;
@@ -924,6 +933,57 @@ int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped
         return fail(h, SPG_E_NOT_CONVERGED, os.str());
     }
     return SPG_OK;
+}
+
+int finish_solve(spg_handle *h, int32_t iters, double rr, double bb, bool capped) {
+    int rc = update_field(h, h->in_run);
+    if (rc) return rc;
+    return record_solve(h, iters, rr, bb, capped);
+}
+
+// Launch count and profiled bytes of a while-graph solve (kind 0: do_solve64,
+// 1: do_solve_mixed_amg) that ran hs.iters iterations.
+void account_while_solve(spg_handle *h, int kind, const PcgScalars &hs) {
+    h->launches += int64_t(hs.iters + 1) * (pcg_iter_launches(h) + 1);
+    if (!h->prof) return;
+    const double n = double(h->n_nodes), nnz = double(h->nnz_kept);
+    h->pcg_iters_prof += hs.iters;
+    if (kind == 1)  // spmv_dot 12 nnz + 24 n, update 52 n, FP32 V-cycle, r.z 12 n, p update 20 n
+        h->pcg_bytes += double(hs.iters + 1) * (12.0 * nnz + 108.0 * n + h->amg_bytes);
+    else if (h->amg)  // spmv_dot 12 nnz + 24 n, update 48 n, V-cycle, r.z 16 n, p update 24 n
+        h->pcg_bytes += double(hs.iters + 1) * (12.0 * nnz + 112.0 * n + h->amg_bytes);
+    else
+        h->pcg_bytes += double(hs.iters) * (12.0 * nnz + 4.0 * (n + 1.0) + 72.0 * n);
+}
+
+// The statistics of the solves held back by the run (one synchronisation).
+int drain_solves(spg_handle *h) {
+    if (h->n_solve_rec == 0) return SPG_OK;
+    CK(cudaStreamSynchronize(h->stream));
+    const int n = h->n_solve_rec;
+    h->n_solve_rec = 0;
+    for (int k = 0; k < n; ++k) {
+        const PcgScalars hs = h->solve_rec[k];
+        account_while_solve(h, h->solve_kind[k], hs);
+        if (record_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2) == SPG_E_NOT_CONVERGED)
+            h->deferred_capped = true;
+    }
+    return SPG_OK;
+}
+
+// After the while graph of a solve inside spg_run: its scalars into the next
+// pinned record (stream-ordered, the host goes on), then the field.
+int defer_solve(spg_handle *h, int kind) {
+    if (!h->solve_rec) CK(cudaHostAlloc(reinterpret_cast<void **>(&h->solve_rec), sizeof(PcgScalars) * kSolveRecs,
+                                        cudaHostAllocDefault));
+    if (h->n_solve_rec == kSolveRecs) {
+        const int rc = drain_solves(h);
+        if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(&h->solve_rec[h->n_solve_rec], h->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, h->stream));
+    h->solve_kind[h->n_solve_rec++] = uint8_t(kind);
+    ev_end(h, h->ev_pcg);
+    return update_field(h, h->in_run);
 }
 
 // A PCG as one graph: a while node repeats the body (one iteration, `iterate`)
@@ -980,9 +1040,12 @@ int do_solve64(spg_handle *h) {
     const int chunk = pcg_chunk(h);
     if (h->pcg64_while) {
         CK(cudaGraphLaunch(h->pcg64_while, h->stream));
+        if (h->defer_solves) return defer_solve(h, 0);
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
-        h->launches += int64_t(hs.iters + 1) * (pcg_iter_launches(h) + 1);
+        ev_end(h, h->ev_pcg);
+        account_while_solve(h, 0, hs);
+        return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
     } else if (!h->pcg_graph) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -991,7 +1054,7 @@ int do_solve64(spg_handle *h) {
         CK(cudaGraphInstantiate(&h->pcg_graph, g, 0));
         cudaGraphDestroy(g);
     }
-    while (!h->pcg64_while) {
+    for (;;) {
         CK(cudaGraphLaunch(h->pcg_graph, h->stream));
         h->launches += pcg_iter_launches(h) * chunk;
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
@@ -1034,16 +1097,13 @@ int do_solve_mixed_amg(spg_handle *h) {
         h->launches += 2 + h->amg_launches - pcg_rz_fused(h);
     }
     if (h->pcg_while) {
-        PcgScalars hs{};
         CK(cudaGraphLaunch(h->pcg_while, h->stream));
+        if (h->defer_solves) return defer_solve(h, 1);
+        PcgScalars hs{};
         CK(cudaMemcpyAsync(&hs, h->sc, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
-        h->launches += int64_t(hs.iters + 1) * (pcg_iter_launches(h) + 1);
         ev_end(h, h->ev_pcg);
-        if (h->prof) {  // spmv_dot 12 nnz + 24 n, update 52 n, FP32 V-cycle, r.z 12 n, p update 20 n
-            h->pcg_iters_prof += hs.iters;
-            h->pcg_bytes += double(hs.iters + 1) * (12.0 * double(h->nnz_kept) + 108.0 * double(n) + h->amg_bytes);
-        }
+        account_while_solve(h, 1, hs);
         return finish_solve(h, hs.iters, hs.rr, hs.bb, hs.converged == 2);
     }
     const int chunk = pcg_chunk(h);
@@ -1613,6 +1673,7 @@ int spg_destroy(spg_handle *h) {
     if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
     if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
     if (h->pcg_while) cudaGraphExecDestroy(h->pcg_while);
+    if (h->solve_rec) cudaFreeHost(h->solve_rec);
     if (h->pcg64_while) cudaGraphExecDestroy(h->pcg64_while);
     for (auto &P : h->ckpt)
         for (void *q : {(void *)P.x, (void *)P.y, (void *)P.z, (void *)P.vx, (void *)P.vy, (void *)P.vz,
@@ -2152,10 +2213,18 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
     if (!h->have_particles) return fail(h, SPG_E_STATE, "run: no particles set");
     if (nsteps < 0) return fail(h, SPG_E_INVALID, "run: nsteps < 0");
     CK(cudaSetDevice(h->device));
-    struct InRun {  // solves of the run refresh the occupied tets only
+    struct InRun {  // solves of the run refresh the occupied tets only and do not wait for the host
         spg_handle *h;
-        explicit InRun(spg_handle *hh) : h(hh) { h->in_run = true; }
-        ~InRun() { h->in_run = false; }
+        explicit InRun(spg_handle *hh) : h(hh) {
+            h->in_run = true;
+            h->defer_solves = true;
+            h->deferred_capped = false;
+        }
+        ~InRun() {
+            h->in_run = false;
+            h->defer_solves = false;
+            drain_solves(h);  // on an early (error) return; empty otherwise
+        }
     } in_run(h);
     int status = SPG_OK;
     for (int32_t k = 0; k < nsteps;) {
@@ -2175,7 +2244,10 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
         if (rc) return rc;
         k += l;
     }
-    int rc = fill_stats(h, stats);
+    int rc = drain_solves(h);
+    if (rc) return rc;
+    if (h->deferred_capped) status = SPG_E_NOT_CONVERGED;
+    rc = fill_stats(h, stats);
     return rc ? rc : status;
 }
 
