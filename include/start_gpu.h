@@ -278,7 +278,12 @@ int spg_solve(spg_handle *h, const double *rho_or_null, double *phi_out, int32_t
 /* (c)(d)(e) nsteps particle steps with the current E (no deposit, no solve). */
 int spg_process(spg_handle *h, int32_t nsteps, spg_stats *stats);
 /* The whole loop: per step, gather+solve when step % poisson_every == 0,
- * re-sort when step % resort_every == 0, then process. */
+ * re-sort when step % resort_every == 0, then process. The host does not
+ * wait for the solves: their iteration counts and residuals are read when
+ * the call ends, and a solve that reached cg_max_iter makes the call return
+ * SPG_E_NOT_CONVERGED then (the run goes on with its potential, as the
+ * reference's loop does: src/FiniteElementMethod/Solvers/
+ * MatrixEquationSolver.cpp:405-412 logs the failure and returns). */
 int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats);
 /* Re-sorts particles by tet now (settled/lost particles move to the end). */
 int spg_resort(spg_handle *h);
