@@ -2223,7 +2223,11 @@ int spg_run(spg_handle *h, int32_t nsteps, spg_stats *stats) {
         ~InRun() {
             h->in_run = false;
             h->defer_solves = false;
-            drain_solves(h);  // on an early (error) return; empty otherwise
+            if (h->n_solve_rec) {  // an early (error) return: keep its message
+                const std::string err = h->err;
+                drain_solves(h);
+                h->err = err;
+            }
         }
     } in_run(h);
     int status = SPG_OK;
