@@ -38,3 +38,21 @@ def test_run_reports_capped_solves_at_the_end(built, precond, precision):
     assert st["step"] == 25 and st["cg_solves"] == 3 and st["cg_iters_total"] >= 3, st
     assert 0.0 < st["cg_relres_last"] <= 1e-10, st
     g.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_run_with_more_solves_than_held_records(built, precision):
+    """A solve every step for 70 steps: more solves than the run holds back
+    (64), so the records are read in the middle of the run as well; every
+    solve is counted once."""
+    from start_gb300 import StartPIC
+    from start_gb300.workloads import workload0
+
+    w = workload0(n_particles=2000, collisions=False, steps=70)
+    w.params.update(preconditioner=2, precision=precision, poisson_every=1, cg_rtol=1e-10)
+    g = StartPIC(w.mesh, w.params)
+    g.set_particles(w.pos, w.vel)
+    st = g.run(70)
+    assert st["step"] == 70 and st["cg_solves"] == 70, st
+    assert st["cg_iters_total"] >= 70 and 0.0 < st["cg_relres_last"] <= 1e-10, st
+    g.close()
